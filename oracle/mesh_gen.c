@@ -1,0 +1,150 @@
+/* Structured QUAD9 / HEX27 box mesh generator for the CPU oracle.  See
+ * mesh_gen.h for the numbering conventions. */
+#include "mesh_gen.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* grid offsets (0..2) of the QUAD9 local nodes, Goma order */
+const int gb_quad9_local[9][2] = {{0, 0}, {2, 0}, {2, 2}, {0, 2}, {1, 0},
+                                  {2, 1}, {1, 2}, {0, 1}, {1, 1}};
+/* grid offsets (0..2) of the HEX27 local nodes, Goma order */
+const int gb_hex27_local[27][3] = {
+    {0, 0, 0}, {2, 0, 0}, {2, 2, 0}, {0, 2, 0}, {0, 0, 2}, {2, 0, 2}, {2, 2, 2},
+    {0, 2, 2}, {1, 0, 0}, {2, 1, 0}, {1, 2, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 1},
+    {2, 2, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 2}, {1, 2, 2}, {0, 1, 2}, {1, 1, 1},
+    {1, 1, 0}, {1, 1, 2}, {0, 1, 1}, {2, 1, 1}, {1, 0, 1}, {1, 2, 1}};
+
+static int add_set(gb_mesh *m, int s, int *tmp, int n) {
+  m->set_nodes[s] = (int *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+  if (!m->set_nodes[s]) return -1;
+  memcpy(m->set_nodes[s], tmp, (size_t)n * sizeof(int));
+  m->set_len[s] = n;
+  return 0;
+}
+
+int gb_mesh_build(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double ly, double lz) {
+  memset(m, 0, sizeof(*m));
+  if (dim != 2 && dim != 3) return -1;
+  if (nx < 1 || ny < 1 || (dim == 3 && nz < 1)) return -1;
+  if (dim == 2) {
+    nz = 1;
+    lz = 0.0;
+  }
+  m->dim = dim;
+  m->nx = nx;
+  m->ny = ny;
+  m->nz = nz;
+  m->lx = lx;
+  m->ly = ly;
+  m->lz = lz;
+  const int NX = 2 * nx + 1, NY = 2 * ny + 1, NZ = dim == 3 ? 2 * nz + 1 : 1;
+  m->num_nodes = NX * NY * NZ;
+  m->num_elems = nx * ny * (dim == 3 ? nz : 1);
+  m->nodes_per_elem = dim == 3 ? 27 : 9;
+  m->x = (double *)malloc((size_t)m->num_nodes * sizeof(double));
+  m->y = (double *)malloc((size_t)m->num_nodes * sizeof(double));
+  m->z = dim == 3 ? (double *)malloc((size_t)m->num_nodes * sizeof(double)) : NULL;
+  m->conn = (int *)malloc((size_t)m->num_elems * m->nodes_per_elem * sizeof(int));
+  if (!m->x || !m->y || (dim == 3 && !m->z) || !m->conn) return -1;
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        int n = i + NX * (j + NY * k);
+        m->x[n] = lx * (double)i / (double)(NX - 1);
+        m->y[n] = ly * (double)j / (double)(NY - 1);
+        if (dim == 3) m->z[n] = lz * (double)k / (double)(NZ - 1);
+      }
+  if (dim == 2) {
+    for (int ey = 0; ey < ny; ey++)
+      for (int ex = 0; ex < nx; ex++) {
+        int e = ex + nx * ey;
+        for (int l = 0; l < 9; l++) {
+          int i = 2 * ex + gb_quad9_local[l][0], j = 2 * ey + gb_quad9_local[l][1];
+          m->conn[e * 9 + l] = i + NX * j;
+        }
+      }
+  } else {
+    for (int ez = 0; ez < nz; ez++)
+      for (int ey = 0; ey < ny; ey++)
+        for (int ex = 0; ex < nx; ex++) {
+          int e = ex + nx * (ey + ny * ez);
+          for (int l = 0; l < 27; l++) {
+            int i = 2 * ex + gb_hex27_local[l][0], j = 2 * ey + gb_hex27_local[l][1],
+                k = 2 * ez + gb_hex27_local[l][2];
+            m->conn[e * 27 + l] = i + NX * (j + NY * k);
+          }
+        }
+  }
+  int *tmp = (int *)malloc((size_t)m->num_nodes * sizeof(int));
+  if (!tmp) return -1;
+  if (dim == 2) {
+    m->num_sets = 6;
+    for (int s = 0; s < 6; s++) {
+      int n = 0;
+      for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++) {
+          int on = 0;
+          switch (s) {
+          case 0: on = (j == 0); break;
+          case 1: on = (i == NX - 1); break;
+          case 2: on = (j == NY - 1); break;
+          case 3: on = (i == 0); break;
+          case 4: on = (i == 0) && (2 * j <= NY - 1); break;
+          case 5: on = (i == 0) && (2 * j >= NY - 1); break;
+          }
+          if (on) tmp[n++] = i + NX * j;
+        }
+      if (add_set(m, s, tmp, n)) return -1;
+    }
+  } else {
+    m->num_sets = 6;
+    for (int s = 0; s < 6; s++) {
+      int n = 0;
+      for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+          for (int i = 0; i < NX; i++) {
+            int on = 0;
+            switch (s) {
+            case 0: on = (i == 0); break;
+            case 1: on = (i == NX - 1); break;
+            case 2: on = (j == 0); break;
+            case 3: on = (j == NY - 1); break;
+            case 4: on = (k == 0); break;
+            case 5: on = (k == NZ - 1); break;
+            }
+            if (on) tmp[n++] = i + NX * (j + NY * k);
+          }
+      if (add_set(m, s, tmp, n)) return -1;
+    }
+  }
+  free(tmp);
+  return 0;
+}
+
+int gb_mesh_build_from_spec(gb_mesh *m, const char *spec) {
+  char kind[16];
+  int nx = 0, ny = 0, nz = 0;
+  double lx = 1, ly = 1, lz = 1;
+  if (!spec || sscanf(spec, "%15s", kind) != 1) return -1;
+  if (strcmp(kind, "quad9") == 0) {
+    if (sscanf(spec, "%15s %d %d %lf %lf", kind, &nx, &ny, &lx, &ly) != 5) return -1;
+    return gb_mesh_build(m, 2, nx, ny, 1, lx, ly, 0.0);
+  }
+  if (strcmp(kind, "hex27") == 0) {
+    if (sscanf(spec, "%15s %d %d %d %lf %lf %lf", kind, &nx, &ny, &nz, &lx, &ly, &lz) != 7)
+      return -1;
+    return gb_mesh_build(m, 3, nx, ny, nz, lx, ly, lz);
+  }
+  return -1;
+}
+
+void gb_mesh_free(gb_mesh *m) {
+  free(m->x);
+  free(m->y);
+  free(m->z);
+  free(m->conn);
+  for (int s = 0; s < m->num_sets; s++) free(m->set_nodes[s]);
+  memset(m, 0, sizeof(*m));
+}
