@@ -2,6 +2,7 @@
  * mesh_gen.h for the numbering conventions. */
 #include "mesh_gen.h"
 
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -24,7 +25,26 @@ static int add_set(gb_mesh *m, int s, int *tmp, int n) {
   return 0;
 }
 
+/* splitmix64 finaliser: a fixed integer hash, so the perturbation is the
+ * same on every machine and in every implementation of the generator */
+static uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+double gb_mesh_jitter(uint64_t seed, uint64_t node, int axis) {
+  uint64_t h = mix64(seed * 0x100000001B3ull + node * 3ull + (uint64_t)axis);
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
 int gb_mesh_build(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double ly, double lz) {
+  return gb_mesh_build_perturbed(m, dim, nx, ny, nz, lx, ly, lz, 0.0, 0);
+}
+
+int gb_mesh_build_perturbed(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double ly,
+                            double lz, double amp, uint64_t seed) {
   memset(m, 0, sizeof(*m));
   if (dim != 2 && dim != 3) return -1;
   if (nx < 1 || ny < 1 || (dim == 3 && nz < 1)) return -1;
@@ -55,6 +75,14 @@ int gb_mesh_build(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double
         m->x[n] = lx * (double)i / (double)(NX - 1);
         m->y[n] = ly * (double)j / (double)(NY - 1);
         if (dim == 3) m->z[n] = lz * (double)k / (double)(NZ - 1);
+        int interior = i > 0 && i < NX - 1 && j > 0 && j < NY - 1 &&
+                       (dim == 2 || (k > 0 && k < NZ - 1));
+        if (amp != 0.0 && interior) {
+          m->x[n] += amp * (lx / (double)(NX - 1)) * gb_mesh_jitter(seed, (uint64_t)n, 0);
+          m->y[n] += amp * (ly / (double)(NY - 1)) * gb_mesh_jitter(seed, (uint64_t)n, 1);
+          if (dim == 3)
+            m->z[n] += amp * (lz / (double)(NZ - 1)) * gb_mesh_jitter(seed, (uint64_t)n, 2);
+        }
       }
   if (dim == 2) {
     for (int ey = 0; ey < ny; ey++)
@@ -126,16 +154,20 @@ int gb_mesh_build(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double
 int gb_mesh_build_from_spec(gb_mesh *m, const char *spec) {
   char kind[16];
   int nx = 0, ny = 0, nz = 0;
-  double lx = 1, ly = 1, lz = 1;
+  double lx = 1, ly = 1, lz = 1, amp = 0.0;
+  unsigned long long seed = 0;
+  int got;
   if (!spec || sscanf(spec, "%15s", kind) != 1) return -1;
   if (strcmp(kind, "quad9") == 0) {
-    if (sscanf(spec, "%15s %d %d %lf %lf", kind, &nx, &ny, &lx, &ly) != 5) return -1;
-    return gb_mesh_build(m, 2, nx, ny, 1, lx, ly, 0.0);
+    got = sscanf(spec, "%15s %d %d %lf %lf %lf %llu", kind, &nx, &ny, &lx, &ly, &amp, &seed);
+    if (got != 5 && got != 7) return -1;
+    return gb_mesh_build_perturbed(m, 2, nx, ny, 1, lx, ly, 0.0, amp, (uint64_t)seed);
   }
   if (strcmp(kind, "hex27") == 0) {
-    if (sscanf(spec, "%15s %d %d %d %lf %lf %lf", kind, &nx, &ny, &nz, &lx, &ly, &lz) != 7)
-      return -1;
-    return gb_mesh_build(m, 3, nx, ny, nz, lx, ly, lz);
+    got = sscanf(spec, "%15s %d %d %d %lf %lf %lf %lf %llu", kind, &nx, &ny, &nz, &lx, &ly, &lz,
+                 &amp, &seed);
+    if (got != 7 && got != 9) return -1;
+    return gb_mesh_build_perturbed(m, 3, nx, ny, nz, lx, ly, lz, amp, (uint64_t)seed);
   }
   return -1;
 }

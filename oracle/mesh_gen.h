@@ -19,6 +19,8 @@
  */
 #ifndef GB_ORACLE_MESH_GEN_H
 #define GB_ORACLE_MESH_GEN_H
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -45,7 +47,13 @@ extern const int gb_quad9_local[9][2];
 extern const int gb_hex27_local[27][3];
 
 int gb_mesh_build(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double ly, double lz);
-/* Parse "quad9 NX NY LX LY" or "hex27 NX NY NZ LX LY LZ". */
+/* Same grid with every strictly interior node moved by amp * (node spacing)
+ * * U(-1,1) per axis, U drawn from a fixed integer hash of (seed, node,
+ * axis); amp <= 0.2 keeps every element valid. */
+int gb_mesh_build_perturbed(gb_mesh *m, int dim, int nx, int ny, int nz, double lx, double ly,
+                            double lz, double amp, uint64_t seed);
+double gb_mesh_jitter(uint64_t seed, uint64_t node, int axis);
+/* Parse "quad9 NX NY LX LY [AMP SEED]" or "hex27 NX NY NZ LX LY LZ [AMP SEED]". */
 int gb_mesh_build_from_spec(gb_mesh *m, const char *spec);
 void gb_mesh_free(gb_mesh *m);
 

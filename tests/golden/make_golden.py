@@ -1,0 +1,223 @@
+"""Generate the golden vectors that pin the CPU oracle to the reference.
+
+Runs the unmodified reference Goma (built by ``oracle/build_ref.sh`` into
+``oracle/_ref/goma_ref``) on small seeded cases and stores what its
+``matrix_fill_full`` (src/mm_fill.c:158) assembled -- the MSR pattern
+``ija``, the MSR values ``a`` and the residual ``R`` -- and, for the
+``solve`` cases, the converged Newton solution written by
+``write_ascii_soln`` (src/rf_util.c:2387).  Each case is one ``.npz`` file
+next to this script.  Test infrastructure only: needs the reference tree,
+so it runs in the build container, never on the GPU machine.
+
+    python tests/golden/make_golden.py [--ref /root/reference] [case ...]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+GOMA = os.path.join(REPO, "oracle", "_ref", "goma_ref")
+
+# ---------------------------------------------------------------- cases
+# phys: "ns" (momentum + continuity), "nst" (+ energy, Boussinesq source)
+# visc: ("newtonian", mu) or ("carreau", mu0, muinf, lam, aexp, nexp)
+CASES = {
+    # 2-D lid-driven cavity, seeded state, affine and perturbed elements
+    "cav2d_2x2": dict(mesh="quad9 2 2 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
+                      bc="cavity2d", datum=True, mode="assemble", seed=1),
+    "cav2d_3x2_pert": dict(mesh="quad9 3 2 1.5 1 0.15 7", phys="ns", rho=100.0,
+                           visc=("newtonian", 1.0), bc="cavity2d", datum=True,
+                           mode="assemble", seed=2),
+    # Carreau-Yasuda channel with a plug inlet on the upper half of x = 0
+    "bfs2d_4x2_carreau": dict(mesh="quad9 4 2 3 1 0.1 11", phys="ns", rho=50.0,
+                              visc=("carreau", 1.0, 0.01, 1.0, 2.0, 0.5), bc="bfs2d",
+                              datum=False, mode="assemble", seed=3),
+    # 3-D Boussinesq natural convection in a (perturbed) box
+    "box3d_2x2x2_bouss": dict(mesh="hex27 2 2 2 1 1 1 0.1 5", phys="nst", rho=1.0,
+                              visc=("newtonian", 0.71), bc="cube_heated", datum=True,
+                              mode="assemble", seed=4, ra_pr=71000.0),
+    "box3d_2x1x3_carreau_t": dict(mesh="hex27 2 1 3 1 0.5 1.5 0.12 9", phys="nst", rho=3.0,
+                                  visc=("carreau", 2.0, 0.1, 0.5, 2.0, 0.6),
+                                  bc="cube_heated", datum=True, mode="assemble", seed=6,
+                                  ra_pr=500.0),
+    # converged Newton solutions from a zero initial guess
+    "cav2d_4x4_solve": dict(mesh="quad9 4 4 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
+                            bc="cavity2d", datum=True, mode="solve", tol=1e-12),
+    "cav2d_8x8_solve": dict(mesh="quad9 8 8 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
+                            bc="cavity2d", datum=True, mode="solve", tol=1e-12),
+    "bfs2d_6x2_carreau_solve": dict(mesh="quad9 6 2 3 1", phys="ns", rho=20.0,
+                                    visc=("carreau", 1.0, 0.01, 1.0, 2.0, 0.5), bc="bfs2d",
+                                    datum=False, mode="solve", tol=1e-12),
+    "box3d_3x3x3_bouss_solve": dict(mesh="hex27 3 3 3 1 1 1", phys="nst", rho=1.0,
+                                    visc=("newtonian", 0.71), bc="cube_heated", datum=True,
+                                    mode="solve", tol=1e-12, ra_pr=7100.0),
+}
+
+# Dirichlet sets: (variable, node set id, value), applied in this order
+BCS = {
+    "cavity2d": [("U", 1, 0.0), ("V", 1, 0.0), ("U", 2, 0.0), ("V", 2, 0.0), ("U", 4, 0.0),
+                 ("V", 4, 0.0), ("U", 3, 1.0), ("V", 3, 0.0)],
+    "bfs2d": [("U", 1, 0.0), ("V", 1, 0.0), ("U", 3, 0.0), ("V", 3, 0.0), ("U", 5, 0.0),
+              ("V", 5, 0.0), ("U", 6, 1.0), ("V", 6, 0.0)],
+    "cube_heated": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
+    + [("T", 1, 1.0), ("T", 2, 0.0)],
+}
+
+
+def deck_text(case):
+    dim = 3 if case["mesh"].startswith("hex27") else 2
+    newton = 1 if case["mode"] == "assemble" else 40
+    lines = [
+        "FEM File Specifications",
+        "FEM file = mesh.exoII",
+        "Output EXODUS II file = out.exoII",
+        "GUESS file = guess.dat",
+        "SOLN file = soln.dat",
+        "Write intermediate results = no",
+        "",
+        "General Specifications",
+        "Output Level = 0",
+        "Debug = 0",
+        "Initial Guess = zero",
+        "",
+        "Time Integration Specifications",
+        "Time integration = steady",
+        "",
+        "Solver Specifications",
+        "Solution Algorithm = lu",
+        "Matrix storage format = msr",
+        "Number of Newton Iterations = %d" % newton,
+        "Newton correction factor = 1",
+        "Normalized Residual Tolerance = %g" % case.get("tol", 1e-10),
+        "",
+        "Boundary Condition Specifications",
+        "Number of BC = %d" % len(BCS[case["bc"]]),
+    ]
+    for var, ns, val in BCS[case["bc"]]:
+        if dim == 2 and var == "W":
+            continue
+        lines.append("BC = %s NS %d %.17g" % (var, ns, val))
+    lines.append("END OF BC")
+    if case["datum"]:
+        lines += ["", "PRESSURE DATUM = 0 0."]
+    lines += [
+        "",
+        "Problem Description",
+        "Number of Materials = 1",
+        "MAT = fluid 1",
+        "Coordinate System = CARTESIAN",
+        "Element Mapping = isoparametric",
+        "Mesh Motion = ARBITRARY",
+        "Number of bulk species = 0",
+        "Number of EQ = -1",
+    ]
+    for a in range(dim):
+        lines.append("EQ = momentum%d Q2 U%d Q2 0. 1. 1. 1. 1. 0." % (a + 1, a + 1))
+    if case["phys"] == "nst":
+        lines.append("EQ = energy Q2 T Q2 0. 1. 1. 1. 1.")
+    lines += ["EQ = continuity P1 P P1 1. 0.", "END OF EQ", "END OF MAT", "",
+              "Post Processing Specifications", ""]
+    # the BC count line must match what was written
+    nbc = sum(1 for v, _, _ in BCS[case["bc"]] if not (dim == 2 and v == "W"))
+    lines[lines.index("Number of BC = %d" % len(BCS[case["bc"]]))] = "Number of BC = %d" % nbc
+    return "\n".join(lines)
+
+
+def mat_text(case):
+    visc = case["visc"]
+    if visc[0] == "newtonian":
+        vl = ["Liquid Constitutive Equation = NEWTONIAN", "Viscosity = CONSTANT %.17g" % visc[1]]
+    else:
+        _, mu0, muinf, lam, aexp, nexp = visc
+        vl = ["Liquid Constitutive Equation = CARREAU", "Low Rate Viscosity = CONSTANT %.17g" % mu0,
+              "Power Law Exponent = CONSTANT %.17g" % nexp,
+              "High Rate Viscosity = CONSTANT %.17g" % muinf,
+              "Time Constant = CONSTANT %.17g" % lam, "Aexp = CONSTANT %.17g" % aexp]
+    if case["phys"] == "nst":
+        src = "Navier-Stokes Source = BOUSSINESQ 0. 0. %.17g" % (-case["ra_pr"])
+    else:
+        src = "Navier-Stokes Source = CONSTANT 0. 0. 0."
+    return "\n".join([
+        "---Physical Properties", "Density = CONSTANT %.17g" % case["rho"], "",
+        "---Mechanical Properties and Constitutive Equations",
+        "Solid Constitutive Equation = NONE", "Plasticity Equation = NONE",
+        "Lame MU = CONSTANT 1.", "Lame LAMBDA = CONSTANT 1."] + vl + [
+        "Polymer Constitutive Equation = NOPOLYMER", "",
+        "---Thermal Properties", "Conductivity = CONSTANT 1.", "Heat Capacity = CONSTANT 1.",
+        "Volume Expansion = CONSTANT 1.", "Reference Temperature = CONSTANT 0.5",
+        "Liquidus Temperature = CONSTANT 0.", "Solidus Temperature = CONSTANT 0.", "",
+        "---Electrical Properties", "Electrical Conductivity = CONSTANT 0.", "",
+        "---Microstructure Properties", "Media Type = CONTINUOUS", "Porosity = CONSTANT 0.",
+        "Permeability = CONSTANT 0.", "",
+        "---Species Properties", "Diffusion Constitutive Equation = NONE", "",
+        "---Source Terms", src, "Solid Body Source = CONSTANT 0. 0. 0.",
+        "Mass Source = CONSTANT 0.", "Heat Source = CONSTANT 0.", "Current Source = CONSTANT 0.",
+        ""])
+
+
+def run_case(name, case, outdir):
+    with tempfile.TemporaryDirectory() as tmp:
+        with open(os.path.join(tmp, "input"), "w") as f:
+            f.write(deck_text(case))
+        with open(os.path.join(tmp, "fluid.mat"), "w") as f:
+            f.write(mat_text(case))
+        env = dict(os.environ, GB_REF_MESH=case["mesh"], GB_REF_DUMP=os.path.join(tmp, "d"))
+        rec = {"name": name, "case": json.dumps(case), "deck": deck_text(case),
+               "mat": mat_text(case)}
+        if case["mode"] == "assemble":
+            # first pass: learn N from the dump of the zero state
+            env1 = dict(env, GB_REF_EXIT="1")
+            subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env1, check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            n = np.fromfile(os.path.join(tmp, "d.R")).size
+            rng = np.random.default_rng(case["seed"])
+            x = rng.uniform(-1.0, 1.0, n)
+            x.astype("<f8").tofile(os.path.join(tmp, "xin.bin"))
+            env2 = dict(env1, GB_REF_X_IN=os.path.join(tmp, "xin.bin"))
+            subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env2, check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
+            assert np.array_equal(rec["x"], x)
+        else:
+            p = subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env, check=True,
+                               stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+            if "converged SS!" not in p.stdout:
+                raise RuntimeError("%s: reference Newton did not converge:\n%s" % (name, p.stdout[-3000:]))
+            vals = []
+            with open(os.path.join(tmp, "soln.dat")) as f:
+                for line in f:
+                    parts = line.split()
+                    if parts and parts[0][0] in "-0123456789":
+                        vals.append(float(parts[0]))
+            rec["x_converged"] = np.array(vals)
+            rec["newton_log"] = "\n".join(l for l in p.stdout.splitlines() if "]" in l[:14])
+            rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
+        rec["ija"] = np.fromfile(os.path.join(tmp, "d.ija"), dtype="<i4")
+        rec["a"] = np.fromfile(os.path.join(tmp, "d.a"))
+        rec["R"] = np.fromfile(os.path.join(tmp, "d.R"))
+    np.savez_compressed(os.path.join(outdir, name + ".npz"), **rec)
+    return rec
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("cases", nargs="*")
+    args = ap.parse_args()
+    if not os.path.exists(GOMA):
+        subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), args.ref], check=True)
+    names = args.cases or list(CASES)
+    for name in names:
+        rec = run_case(name, CASES[name], HERE)
+        n = rec["R"].size
+        print("%-28s N=%6d msr_len=%8d %s" % (name, n, rec["ija"][n], CASES[name]["mode"]))
+
+
+if __name__ == "__main__":
+    sys.exit(main())
