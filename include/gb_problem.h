@@ -1,0 +1,81 @@
+/* Problem description shared by the GB300 Newton library (libgbnewton.so)
+ * and its CPU oracle: a Q2/P1 finite-element mesh, one material and its
+ * strong (Dirichlet) boundary conditions, as plain arrays.
+ *
+ * It carries what the reference reads from its input deck, material file
+ * and Exodus mesh for the path this library replaces:
+ *   - mesh: coordinates and QUAD9/HEX27 connectivity in the Exodus/Goma local
+ *     node order (src/rf_shape.c:361 BIQUAD_QUAD, :1105 TRIQUAD_HEX);
+ *   - equations: momentum (Q2), continuity (P1 discontinuous pressure,
+ *     basis {1,s,t[,u]} in reference coordinates), optional energy (Q2);
+ *   - material: density, Newtonian or Carreau-Yasuda viscosity
+ *     (src/mm_viscosity.c:981), heat capacity, Fourier conductivity,
+ *     CONSTANT or BOUSSINESQ momentum source (src/mm_std_models.c:125);
+ *   - "BC = U|V|W|T NS <id> <value>" cards in deck order
+ *     (src/mm_input_bc.c), hard-set Dirichlet (src/bc_dirich.c:44), and the
+ *     PRESSURE DATUM card (src/mm_input_bc.c:3215, src/mm_bc.c:388).
+ */
+#ifndef GB_PROBLEM_H
+#define GB_PROBLEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Variable numbering follows the reference's variable types
+ * (include/rf_fem_const.h:174-200). */
+#define GB_VAR_U1 0
+#define GB_VAR_U2 1
+#define GB_VAR_U3 2
+#define GB_VAR_T 3
+#define GB_VAR_P 9
+
+#define GB_VISC_NEWTONIAN 0
+#define GB_VISC_CARREAU 1
+
+#define GB_SOURCE_CONSTANT 0
+#define GB_SOURCE_BOUSSINESQ 1
+
+typedef struct gb_material {
+  double density;          /* "Density = CONSTANT" */
+  int viscosity_model;     /* GB_VISC_* ("Liquid Constitutive Equation") */
+  double viscosity;        /* Newtonian "Viscosity = CONSTANT" */
+  double mu0;              /* Carreau "Low Rate Viscosity" */
+  double mu_inf;           /* Carreau "High Rate Viscosity" */
+  double lambda;           /* Carreau "Time Constant" */
+  double aexp;             /* Carreau "Aexp" */
+  double nexp;             /* Carreau "Power Law Exponent" */
+  double heat_capacity;    /* "Heat Capacity = CONSTANT" */
+  double conductivity;     /* "Conductivity = CONSTANT" (Fourier heat flux) */
+  int momentum_source_model;     /* GB_SOURCE_* ("Navier-Stokes Source") */
+  double momentum_source[3];     /* constant force or gravity vector */
+  double volume_expansion;       /* "Volume Expansion = CONSTANT" (beta) */
+  double reference_temperature;  /* "Reference Temperature = CONSTANT" */
+} gb_material;
+
+typedef struct gb_problem_desc {
+  int dim;        /* 2 (QUAD9) or 3 (HEX27) */
+  int num_nodes;
+  int num_elems;
+  const double *coords; /* num_nodes * dim, interleaved (x, y[, z]) */
+  const int *conn;      /* num_elems * (9 | 27), 0-based node ids */
+  int energy;           /* 1: solve the energy equation (variable T) */
+  gb_material mat;
+  /* Dirichlet cards, applied in order (a later card wins on a shared
+   * node): card c sets variable bc_var[c] to bc_value[c] on the nodes
+   * bc_nodes[bc_ptr[c] .. bc_ptr[c+1]-1]. */
+  int num_bc;
+  const int *bc_var;
+  const double *bc_value;
+  const int *bc_ptr;
+  const int *bc_nodes;
+  /* PRESSURE DATUM: element (0-based) whose first pressure unknown is
+   * pinned to pressure_datum_value; -1 for none. */
+  int pressure_datum_elem;
+  double pressure_datum_value;
+} gb_problem_desc;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,159 @@
+"""ctypes binding of the CPU oracle (oracle/gb_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke``
+and by the CPU-baseline leg of ``bench.py``, always as the checker or the
+timed CPU reference, never as part of the product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liborc.so")
+SRCS = [os.path.join(HERE, "gb_oracle.c"), os.path.join(HERE, "mesh_gen.c")]
+
+
+def build(force=False):
+    """Compile the oracle (plain C, portable flags) into oracle/liborc.so."""
+    newest = max(os.path.getmtime(s) for s in SRCS + [os.path.join(HERE, "gb_oracle.h"),
+                                                       os.path.join(HERE, "mesh_gen.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.run(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-o", tmp] + SRCS + ["-lm"],
+                   check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [vp]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_num_unknowns.argtypes = [vp]
+        L.orc_msr_len.restype = ctypes.c_long
+        L.orc_msr_len.argtypes = [vp]
+        L.orc_msr_pattern.argtypes = [vp, ip]
+        L.orc_first_unknown.argtypes = [vp, ip]
+        L.orc_dirichlet_mask.argtypes = [vp, ip]
+        L.orc_dirichlet_init.argtypes = [vp, dp]
+        L.orc_matrix_fill.argtypes = [vp, dp, dp, dp, ctypes.c_int, ctypes.c_int]
+        L.orc_element.argtypes = [vp, ctypes.c_int, dp, dp, dp, ctypes.c_int]
+        L.orc_local_size.argtypes = [vp]
+        L.orc_element_dofs.argtypes = [vp, ctypes.c_int, ip]
+        L.orc_row_sum_scale.argtypes = [vp, dp, dp, dp]
+        L.orc_newton.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp]
+        L.orc_mesh_sizes.argtypes = [ctypes.c_char_p, ip, ip, ip]
+        L.orc_mesh_fill.argtypes = [ctypes.c_char_p, dp, ip, ip, ip]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+class Oracle:
+    """CPU restatement of the reference path for one problem."""
+
+    def __init__(self, problem):
+        from goma_gb300.problem import make_desc
+        self._desc, self._keep = make_desc(problem)
+        self.h = lib().orc_create(ctypes.byref(self._desc))
+        if not self.h:
+            raise RuntimeError("orc_create failed")
+        self.N = lib().orc_num_unknowns(self.h)
+        self.msr_len = lib().orc_msr_len(self.h)
+        self.nloc = lib().orc_local_size(self.h)
+        self.num_elems = problem.mesh.num_elems
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def ija(self):
+        out = np.empty(self.msr_len, np.int32)
+        lib().orc_msr_pattern(self.h, _p(out, ctypes.c_int))
+        return out
+
+    def first_unknown(self, num_nodes):
+        out = np.empty(num_nodes + 1, np.int32)
+        lib().orc_first_unknown(self.h, _p(out, ctypes.c_int))
+        return out
+
+    def dirichlet_mask(self):
+        out = np.empty(self.N, np.int32)
+        lib().orc_dirichlet_mask(self.h, _p(out, ctypes.c_int))
+        return out.astype(bool)
+
+    def dirichlet_init(self, x):
+        x = np.ascontiguousarray(x, np.float64).copy()
+        lib().orc_dirichlet_init(self.h, _p(x, ctypes.c_double))
+        return x
+
+    def matrix_fill(self, x, jacobian=True, e0=0, e1=None):
+        """Returns (R, a_msr or None, status)."""
+        x = np.ascontiguousarray(x, np.float64)
+        R = np.zeros(self.N)
+        a = np.zeros(self.msr_len) if jacobian else None
+        st = lib().orc_matrix_fill(self.h, _p(x, ctypes.c_double), _p(R, ctypes.c_double),
+                                   _p(a, ctypes.c_double) if a is not None else None, e0,
+                                   self.num_elems if e1 is None else e1)
+        return R, a, st
+
+    def element(self, e, x, apply_bc=True):
+        x = np.ascontiguousarray(x, np.float64)
+        Re = np.zeros(self.nloc)
+        Je = np.zeros((self.nloc, self.nloc))
+        st = lib().orc_element(self.h, e, _p(x, ctypes.c_double), _p(Re, ctypes.c_double),
+                               _p(Je, ctypes.c_double), 1 if apply_bc else 0)
+        g = np.empty(self.nloc, np.int32)
+        lib().orc_element_dofs(self.h, e, _p(g, ctypes.c_int))
+        return Re, Je, g, st
+
+    def row_sum_scale(self, a, R):
+        a = a.copy()
+        R = R.copy()
+        s = np.empty(self.N)
+        lib().orc_row_sum_scale(self.h, _p(a, ctypes.c_double), _p(R, ctypes.c_double),
+                                _p(s, ctypes.c_double))
+        return a, R, s
+
+    def newton(self, x0, max_it=40, tol=1e-10):
+        x = np.ascontiguousarray(x0, np.float64).copy()
+        norms = np.full(max_it, np.nan)
+        it = lib().orc_newton(self.h, _p(x, ctypes.c_double), max_it, tol,
+                              _p(norms, ctypes.c_double))
+        return x, it, norms[:max(it + 1, 0)] if it >= 0 else norms
+
+
+def mesh_from_spec(spec):
+    """The oracle generator's mesh: (coords, conn, [node sets])."""
+    L = lib()
+    nn, ne, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    if L.orc_mesh_sizes(spec.encode(), ctypes.byref(nn), ctypes.byref(ne), ctypes.byref(st)):
+        raise ValueError(spec)
+    dim = 3 if spec.startswith("hex27") else 2
+    npe = 27 if dim == 3 else 9
+    coords = np.empty((nn.value, dim))
+    conn = np.empty((ne.value, npe), np.int32)
+    lens = np.empty(6, np.int32)
+    nodes = np.empty(max(st.value, 1), np.int32)
+    L.orc_mesh_fill(spec.encode(), _p(coords, ctypes.c_double), _p(conn, ctypes.c_int),
+                    _p(lens, ctypes.c_int), _p(nodes, ctypes.c_int))
+    sets, off = [], 0
+    for n in lens:
+        sets.append(nodes[off:off + n].copy())
+        off += n
+    return coords, conn, sets

@@ -1,0 +1,710 @@
+/* CPU oracle for the Q2/P1 Newton hot path -- TEST INFRASTRUCTURE ONLY.
+ * See gb_oracle.h for scope.  Every routine names the reference code it
+ * restates; the restatement is pinned by tests/test_oracle_golden.py
+ * against vectors the reference produced (tests/golden/make_golden.py). */
+#include "gb_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_problem {
+  gb_problem_desc d; /* copy; the arrays below are owned copies */
+  double *coords;
+  int *conn;
+  int nn;       /* nodes per element: 9 or 27 */
+  int centroid; /* local index of the centroid node: 8 or 20 */
+  int nvn;      /* nodal fields per node: dim + energy */
+  int npres;    /* P1 pressure unknowns per element: dim + 1 */
+  int nloc;     /* nvn * nn + npres */
+  int N;
+  int *fu;    /* first unknown per node, num_nodes + 1 */
+  int *ija;   /* MSR pattern */
+  long msr_len;
+  int *dbc;   /* per unknown: -1, or index of the Dirichlet card (datum: -2) */
+  double *dbc_val;
+};
+
+/* ---------------------------------------------------------------- basis */
+
+/* Gauss-Legendre constants as the reference writes them
+ * (src/el_elm_info.c:1642 and :3484-3485). */
+static const double GQ_PT = 0.77459666924148340428;
+static const double GQ_W0 = 0.55555555555555555556;
+static const double GQ_W1 = 0.88888888888888888888;
+
+static const int LOC9[9][2] = {{0, 0}, {2, 0}, {2, 2}, {0, 2}, {1, 0},
+                               {2, 1}, {1, 2}, {0, 1}, {1, 1}};
+static const int LOC27[27][3] = {
+    {0, 0, 0}, {2, 0, 0}, {2, 2, 0}, {0, 2, 0}, {0, 0, 2}, {2, 0, 2}, {2, 2, 2},
+    {0, 2, 2}, {1, 0, 0}, {2, 1, 0}, {1, 2, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 1},
+    {2, 2, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 2}, {1, 2, 2}, {0, 1, 2}, {1, 1, 1},
+    {1, 1, 0}, {1, 1, 2}, {0, 1, 1}, {2, 1, 1}, {1, 0, 1}, {1, 2, 1}};
+
+/* 1-D quadratic Lagrange polynomials on the nodes -1, 0, +1 */
+static double lag(int g, double s) {
+  return g == 0 ? 0.5 * s * (s - 1.0) : (g == 1 ? 1.0 - s * s : 0.5 * s * (s + 1.0));
+}
+static double dlag(int g, double s) { return g == 0 ? s - 0.5 : (g == 1 ? -2.0 * s : s + 0.5); }
+
+/* Quadrature point iq in the reference order (src/el_elm_info.c:1748 for
+ * QUAD9, :1802 for HEX27): s runs fastest from +sqrt(3/5) down, then t,
+ * then u; weight = w_s * w_t * w_u (src/el_elm_info.c:3554, :3646). */
+static void quad_point(int dim, int iq, double xi[3], double *w) {
+  static const double pt[3] = {0.77459666924148340428, 0.0, -0.77459666924148340428};
+  static const double wt[3] = {0.55555555555555555556, 0.88888888888888888888,
+                               0.55555555555555555556};
+  int is = iq % 3, it = (iq % 9) / 3, iu = iq / 9;
+  (void)GQ_PT;
+  (void)GQ_W0;
+  (void)GQ_W1;
+  xi[0] = pt[is];
+  xi[1] = pt[it];
+  xi[2] = dim == 3 ? pt[iu] : 0.0;
+  *w = dim == 3 ? wt[is] * wt[it] * wt[iu] : wt[is] * wt[it];
+}
+
+/* phi and d(phi)/d(xi) of the Q2 basis at xi */
+static void q2_basis(int dim, const double xi[3], double *phi, double (*dphi)[3]) {
+  if (dim == 2) {
+    for (int k = 0; k < 9; k++) {
+      int gx = LOC9[k][0], gy = LOC9[k][1];
+      double ls = lag(gx, xi[0]), lt = lag(gy, xi[1]);
+      phi[k] = ls * lt;
+      dphi[k][0] = dlag(gx, xi[0]) * lt;
+      dphi[k][1] = ls * dlag(gy, xi[1]);
+      dphi[k][2] = 0.0;
+    }
+  } else {
+    for (int k = 0; k < 27; k++) {
+      int gx = LOC27[k][0], gy = LOC27[k][1], gz = LOC27[k][2];
+      double ls = lag(gx, xi[0]), lt = lag(gy, xi[1]), lu = lag(gz, xi[2]);
+      phi[k] = ls * lt * lu;
+      dphi[k][0] = dlag(gx, xi[0]) * lt * lu;
+      dphi[k][1] = ls * dlag(gy, xi[1]) * lu;
+      dphi[k][2] = ls * lt * dlag(gz, xi[2]);
+    }
+  }
+}
+
+/* ---------------------------------------------------------------- setup */
+
+static int cmp_int(const void *a, const void *b) {
+  int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+/* DOF numbering (src/mm_unknown_map.c:758, Index_Solution :5268): node by
+ * node in node order; at every node the velocity components, then T, and
+ * at an element's centroid node its dim+1 P1 pressure unknowns.
+ * Sparsity (src/exo_conn.c:204 build_node_node, src/mm_fill_util.c:3229
+ * find_MSR_problem_graph): unknown i couples with every unknown of every
+ * node sharing an element with its node; a centroid node also couples with
+ * the centroid nodes of the face neighbours of its element
+ * (src/exo_conn.c:300-330).  Off-diagonal columns ascend. */
+orc_problem *orc_create(const gb_problem_desc *desc) {
+  orc_problem *p = (orc_problem *)calloc(1, sizeof(*p));
+  if (!p) return NULL;
+  p->d = *desc;
+  const int dim = desc->dim, nnod = desc->num_nodes, ne = desc->num_elems;
+  p->nn = dim == 2 ? 9 : 27;
+  p->centroid = dim == 2 ? 8 : 20;
+  p->nvn = dim + (desc->energy ? 1 : 0);
+  p->npres = dim + 1;
+  p->nloc = p->nvn * p->nn + p->npres;
+  p->coords = (double *)malloc(sizeof(double) * (size_t)nnod * dim);
+  p->conn = (int *)malloc(sizeof(int) * (size_t)ne * p->nn);
+  memcpy(p->coords, desc->coords, sizeof(double) * (size_t)nnod * dim);
+  memcpy(p->conn, desc->conn, sizeof(int) * (size_t)ne * p->nn);
+  p->d.coords = p->coords;
+  p->d.conn = p->conn;
+
+  /* centroid flag and unknowns per node */
+  int *is_cent = (int *)calloc((size_t)nnod, sizeof(int));
+  int *cent_elem = (int *)malloc(sizeof(int) * (size_t)nnod);
+  for (int i = 0; i < nnod; i++) cent_elem[i] = -1;
+  for (int e = 0; e < ne; e++) {
+    int c = p->conn[e * p->nn + p->centroid];
+    is_cent[c] = 1;
+    cent_elem[c] = e;
+  }
+  p->fu = (int *)malloc(sizeof(int) * (size_t)(nnod + 1));
+  p->fu[0] = 0;
+  for (int i = 0; i < nnod; i++) p->fu[i + 1] = p->fu[i] + p->nvn + (is_cent[i] ? p->npres : 0);
+  p->N = p->fu[nnod];
+
+  /* node -> elements */
+  int *ne_ptr = (int *)calloc((size_t)nnod + 1, sizeof(int));
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < p->nn; k++) ne_ptr[p->conn[e * p->nn + k] + 1]++;
+  for (int i = 0; i < nnod; i++) ne_ptr[i + 1] += ne_ptr[i];
+  int *ne_list = (int *)malloc(sizeof(int) * (size_t)ne_ptr[nnod]);
+  int *fill = (int *)calloc((size_t)nnod, sizeof(int));
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < p->nn; k++) {
+      int n = p->conn[e * p->nn + k];
+      ne_list[ne_ptr[n] + fill[n]++] = e;
+    }
+  /* face neighbours: elements sharing a mid-side node (QUAD9 local 4..7,
+   * HEX27 local 21..26) */
+  const int side0 = dim == 2 ? 4 : 21, side1 = dim == 2 ? 8 : 27;
+
+  /* node -> neighbour nodes, then rows */
+  int maxnb = 8 * p->nn + 16;
+  int *nb = (int *)malloc(sizeof(int) * (size_t)maxnb);
+  int **nbl = (int **)malloc(sizeof(int *) * (size_t)nnod);
+  int *nbn = (int *)malloc(sizeof(int) * (size_t)nnod);
+  for (int n = 0; n < nnod; n++) {
+    int cnt = 0;
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; q++) {
+      int e = ne_list[q];
+      for (int k = 0; k < p->nn; k++) {
+        int m = p->conn[e * p->nn + k], dup = 0;
+        for (int r = 0; r < cnt; r++)
+          if (nb[r] == m) {
+            dup = 1;
+            break;
+          }
+        if (!dup) nb[cnt++] = m;
+      }
+    }
+    if (is_cent[n] && ne_ptr[n + 1] - ne_ptr[n] == 1) {
+      int e = cent_elem[n];
+      for (int k = side0; k < side1; k++) {
+        int m = p->conn[e * p->nn + k];
+        for (int q = ne_ptr[m]; q < ne_ptr[m + 1]; q++) {
+          int f = ne_list[q];
+          if (f == e) continue;
+          int c = p->conn[f * p->nn + p->centroid], dup = 0;
+          for (int r = 0; r < cnt; r++)
+            if (nb[r] == c) {
+              dup = 1;
+              break;
+            }
+          if (!dup) nb[cnt++] = c;
+        }
+      }
+    }
+    qsort(nb, (size_t)cnt, sizeof(int), cmp_int);
+    nbl[n] = (int *)malloc(sizeof(int) * (size_t)cnt);
+    memcpy(nbl[n], nb, sizeof(int) * (size_t)cnt);
+    nbn[n] = cnt;
+  }
+  /* Interaction mask (src/mm_unknown_map.c:1125 set_interaction_masks):
+   * every equation couples with every variable except energy with
+   * pressure.  An unknown's variable: offset < nvn is a nodal field
+   * (offset == dim is T when energy is on), offset >= nvn is pressure. */
+  long off = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    long pos = p->N + 1;
+    for (int n = 0; n < nnod; n++) {
+      for (int i = p->fu[n]; i < p->fu[n + 1]; i++) {
+        const int row_is_T = desc->energy && (i - p->fu[n]) == dim;
+        if (pass) p->ija[i] = (int)pos;
+        for (int r = 0; r < nbn[n]; r++) {
+          int mm = nbl[n][r];
+          for (int j = p->fu[mm]; j < p->fu[mm + 1]; j++) {
+            if (j == i) continue;
+            if (row_is_T && (j - p->fu[mm]) >= p->nvn) continue;
+            if (pass) p->ija[pos] = j;
+            pos++;
+          }
+        }
+      }
+    }
+    if (!pass) {
+      off = pos - (p->N + 1);
+      p->msr_len = (long)p->N + 1 + off;
+      p->ija = (int *)malloc(sizeof(int) * (size_t)p->msr_len);
+    } else {
+      p->ija[p->N] = (int)pos;
+    }
+  }
+
+  /* Dirichlet cards in order: a later card overwrites (src/mm_bc.c:132) */
+  p->dbc = (int *)malloc(sizeof(int) * (size_t)p->N);
+  p->dbc_val = (double *)calloc((size_t)p->N, sizeof(double));
+  for (int i = 0; i < p->N; i++) p->dbc[i] = -1;
+  for (int c = 0; c < desc->num_bc; c++) {
+    int var = desc->bc_var[c];
+    int offv = var == GB_VAR_T ? dim : var;
+    if (var == GB_VAR_T && !desc->energy) continue;
+    for (int q = desc->bc_ptr[c]; q < desc->bc_ptr[c + 1]; q++) {
+      int n = desc->bc_nodes[q];
+      p->dbc[p->fu[n] + offv] = c;
+      p->dbc_val[p->fu[n] + offv] = desc->bc_value[c];
+    }
+  }
+  if (desc->pressure_datum_elem >= 0 && desc->pressure_datum_elem < ne) {
+    int c = p->conn[desc->pressure_datum_elem * p->nn + p->centroid];
+    int i = p->fu[c] + p->nvn;
+    p->dbc[i] = -2;
+    p->dbc_val[i] = desc->pressure_datum_value;
+  }
+
+  for (int n = 0; n < nnod; n++) free(nbl[n]);
+  free(nbl);
+  free(nbn);
+  free(nb);
+  free(fill);
+  free(ne_list);
+  free(ne_ptr);
+  free(is_cent);
+  free(cent_elem);
+  return p;
+}
+
+void orc_destroy(orc_problem *p) {
+  if (!p) return;
+  free(p->coords);
+  free(p->conn);
+  free(p->fu);
+  free(p->ija);
+  free(p->dbc);
+  free(p->dbc_val);
+  free(p);
+}
+
+int orc_num_unknowns(const orc_problem *p) { return p->N; }
+long orc_msr_len(const orc_problem *p) { return p->msr_len; }
+void orc_msr_pattern(const orc_problem *p, int *ija) {
+  memcpy(ija, p->ija, sizeof(int) * (size_t)p->msr_len);
+}
+void orc_first_unknown(const orc_problem *p, int *fu) {
+  memcpy(fu, p->fu, sizeof(int) * (size_t)(p->d.num_nodes + 1));
+}
+void orc_dirichlet_mask(const orc_problem *p, int *mask) {
+  for (int i = 0; i < p->N; i++) mask[i] = p->dbc[i] != -1;
+}
+void orc_dirichlet_init(const orc_problem *p, double *x) {
+  for (int i = 0; i < p->N; i++)
+    if (p->dbc[i] != -1) x[i] = p->dbc_val[i];
+}
+int orc_local_size(const orc_problem *p) { return p->nloc; }
+
+void orc_element_dofs(const orc_problem *p, int e, int *g) {
+  const int nn = p->nn, dim = p->d.dim;
+  const int *cn = p->conn + (size_t)e * nn;
+  for (int a = 0; a < dim; a++)
+    for (int k = 0; k < nn; k++) g[a * nn + k] = p->fu[cn[k]] + a;
+  if (p->d.energy)
+    for (int k = 0; k < nn; k++) g[dim * nn + k] = p->fu[cn[k]] + dim;
+  for (int l = 0; l < p->npres; l++) g[p->nvn * nn + l] = p->fu[cn[p->centroid]] + p->nvn + l;
+}
+
+/* ------------------------------------------------------------- element */
+
+/* One element's residual and Jacobian.  Follows, per quadrature point:
+ *   geometry            beer_belly           src/mm_fill_util.c:140
+ *   field values/grads  load_fv, load_fv_grads src/load_field_variables.c
+ *   viscosity           viscosity / carreau_viscosity, calc_shearrate
+ *                       src/mm_viscosity.c:108,:981, src/mm_fill_util.c:4564
+ *   stress Pi = -P I + mu gamma and its derivatives
+ *                       fluid_stress          src/mm_fill_momentum.c:2834
+ *   body force          bouss_momentum_source src/mm_std_models.c:125
+ *   momentum R, J_m_v, J_m_P, J_m_T           src/mm_fill_momentum.c:471-2116
+ *   continuity R, J_c_v                       src/mm_fill_continuity.c:430-700
+ *   energy R, J_e_T, J_e_v (Fourier flux)     src/mm_fill_energy.c:315-560,
+ *                                             heat_flux :1629
+ * then the hard-set Dirichlet rows of put_dirichlet_in_matrix
+ * (src/bc_dirich.c:44): row zeroed, diagonal DIRICHLET_PENALTY = 1,
+ * residual 0. */
+int orc_element(const orc_problem *p, int e, const double *x, double *Re, double *Je,
+                int apply_bc) {
+  const int nn = p->nn, dim = p->d.dim, nloc = p->nloc, nq = dim == 2 ? 9 : 27;
+  const int en = p->d.energy, npr = p->npres;
+  const int oT = dim * nn, oP = p->nvn * nn;
+  const gb_material *m = &p->d.mat;
+  const int *cn = p->conn + (size_t)e * nn;
+  int status = 0;
+  double X[27][3], U[27][3], Tn[27], Pn[4];
+  int g[27 * 4 + 4];
+  orc_element_dofs(p, e, g);
+  for (int k = 0; k < nn; k++) {
+    for (int j = 0; j < dim; j++) X[k][j] = p->coords[(size_t)cn[k] * dim + j];
+    for (int a = 0; a < dim; a++) U[k][a] = x[g[a * nn + k]];
+    Tn[k] = en ? x[g[oT + k]] : 0.0;
+  }
+  for (int l = 0; l < npr; l++) Pn[l] = x[g[oP + l]];
+  memset(Re, 0, sizeof(double) * (size_t)nloc);
+  memset(Je, 0, sizeof(double) * (size_t)nloc * nloc);
+#define JE(r, c) Je[(size_t)(r) * nloc + (c)]
+
+  for (int iq = 0; iq < nq; iq++) {
+    double xi[3], wq, phi[27], dphi[27][3], gphi[27][3];
+    quad_point(dim, iq, xi, &wq);
+    q2_basis(dim, xi, phi, dphi);
+    /* J[i][j] = sum_k dphi_k/dxi_i * x_k,j ; B = J^-1 */
+    double Jm[3][3] = {{0}}, B[3][3] = {{0}}, det;
+    for (int i = 0; i < dim; i++)
+      for (int j = 0; j < dim; j++) {
+        double s = 0.0;
+        for (int k = 0; k < nn; k++) s += dphi[k][i] * X[k][j];
+        Jm[i][j] = s;
+      }
+    if (dim == 2) {
+      det = Jm[0][0] * Jm[1][1] - Jm[0][1] * Jm[1][0];
+      B[0][0] = Jm[1][1] / det;
+      B[1][1] = Jm[0][0] / det;
+      B[0][1] = -Jm[0][1] / det;
+      B[1][0] = -Jm[1][0] / det;
+    } else {
+      det = Jm[0][0] * (Jm[1][1] * Jm[2][2] - Jm[1][2] * Jm[2][1]) -
+            Jm[0][1] * (Jm[1][0] * Jm[2][2] - Jm[1][2] * Jm[2][0]) +
+            Jm[0][2] * (Jm[1][0] * Jm[2][1] - Jm[1][1] * Jm[2][0]);
+      B[0][0] = (Jm[1][1] * Jm[2][2] - Jm[2][1] * Jm[1][2]) / det;
+      B[0][1] = -(Jm[0][1] * Jm[2][2] - Jm[2][1] * Jm[0][2]) / det;
+      B[0][2] = (Jm[0][1] * Jm[1][2] - Jm[1][1] * Jm[0][2]) / det;
+      B[1][0] = -(Jm[1][0] * Jm[2][2] - Jm[2][0] * Jm[1][2]) / det;
+      B[1][1] = (Jm[0][0] * Jm[2][2] - Jm[2][0] * Jm[0][2]) / det;
+      B[1][2] = -(Jm[0][0] * Jm[1][2] - Jm[1][0] * Jm[0][2]) / det;
+      B[2][0] = (Jm[1][0] * Jm[2][1] - Jm[2][0] * Jm[1][1]) / det;
+      B[2][1] = -(Jm[0][0] * Jm[2][1] - Jm[2][0] * Jm[0][1]) / det;
+      B[2][2] = (Jm[0][0] * Jm[1][1] - Jm[1][0] * Jm[0][1]) / det;
+    }
+    if (!(det > 0.0)) status = -1;
+    /* grad phi_k (physical) = B * dphi/dxi:  d/dx_p = sum_i B[p][i] d/dxi_i */
+    for (int k = 0; k < nn; k++)
+      for (int pp = 0; pp < dim; pp++) {
+        double s = 0.0;
+        for (int i = 0; i < dim; i++) s += B[pp][i] * dphi[k][i];
+        gphi[k][pp] = s;
+      }
+    /* P1 pressure basis {1, s, t[, u]} in reference coordinates */
+    double psi[4];
+    psi[0] = 1.0;
+    for (int i = 0; i < dim; i++) psi[1 + i] = xi[i];
+    const double dA = wq * det;
+
+    /* fields */
+    double v[3] = {0}, gv[3][3] = {{0}}, T = 0.0, gT[3] = {0}, P = 0.0;
+    for (int k = 0; k < nn; k++) {
+      for (int a = 0; a < dim; a++) {
+        v[a] += U[k][a] * phi[k];
+        for (int pp = 0; pp < dim; pp++) gv[pp][a] += U[k][a] * gphi[k][pp];
+      }
+      if (en) {
+        T += Tn[k] * phi[k];
+        for (int pp = 0; pp < dim; pp++) gT[pp] += Tn[k] * gphi[k][pp];
+      }
+    }
+    for (int l = 0; l < npr; l++) P += Pn[l] * psi[l];
+    double divv = 0.0;
+    for (int a = 0; a < dim; a++) divv += gv[a][a];
+    double gam[3][3];
+    for (int a = 0; a < dim; a++)
+      for (int b = 0; b < dim; b++) gam[a][b] = gv[a][b] + gv[b][a];
+
+    /* viscosity and d mu / d v_{b,j} */
+    double mu, dmu_dgd = 0.0, gd = 0.0;
+    if (m->viscosity_model == GB_VISC_CARREAU) {
+      double s = 0.0;
+      for (int a = 0; a < dim; a++)
+        for (int b = 0; b < dim; b++) s += gam[a][b] * gam[b][a];
+      gd = sqrt(0.5 * fabs(s));
+      double val2 = gd > 1.0e-298 ? pow(m->lambda * gd, m->aexp) : 0.0;
+      mu = m->mu_inf + (m->mu0 - m->mu_inf) * pow(1.0 + val2, (m->nexp - 1.0) / m->aexp);
+      double val = gd > 1.0e-298 ? pow(m->lambda * gd, m->aexp - 1.0) : 0.0;
+      double val1 = pow(1.0 + val2, (m->nexp - 1.0 - m->aexp) / m->aexp);
+      dmu_dgd = (m->mu0 - m->mu_inf) * (m->nexp - 1.0) * m->lambda * val * val1;
+    } else {
+      mu = m->viscosity;
+    }
+    /* dmu_v[b][j] = dmu/dgd * (sum_p dphi_j/dx_p gam[b][p]) / gd */
+    double dmu_v[3][27];
+    for (int b = 0; b < dim; b++)
+      for (int j = 0; j < nn; j++) {
+        double s = 0.0;
+        if (m->viscosity_model == GB_VISC_CARREAU && gd != 0.0 && gd > 1.0e-298) {
+          for (int pp = 0; pp < dim; pp++) s += gphi[j][pp] * gam[b][pp];
+          s = dmu_dgd * (s / gd);
+        }
+        dmu_v[b][j] = s;
+      }
+    double Pi[3][3];
+    for (int a = 0; a < dim; a++)
+      for (int b = 0; b < dim; b++) Pi[a][b] = (a == b ? -P : 0.0) + mu * gam[a][b];
+
+    /* body force f and df/dT_j = dfT[a] * phi_j */
+    double f[3] = {0, 0, 0}, dfT[3] = {0, 0, 0};
+    if (m->momentum_source_model == GB_SOURCE_BOUSSINESQ) {
+      if (en)
+        for (int a = 0; a < dim; a++) {
+          f[a] = m->density * m->momentum_source[a] *
+                 (-m->volume_expansion * (T - m->reference_temperature));
+          dfT[a] = -m->density * m->momentum_source[a] * m->volume_expansion;
+        }
+    } else {
+      for (int a = 0; a < dim; a++) f[a] = m->momentum_source[a];
+    }
+    const double rho = m->density, rcp = m->density * m->heat_capacity, kc = m->conductivity;
+
+    /* momentum */
+    for (int a = 0; a < dim; a++) {
+      double adv_a = 0.0;
+      for (int pp = 0; pp < dim; pp++) adv_a += v[pp] * gv[pp][a];
+      for (int i = 0; i < nn; i++) {
+        const int ri = a * nn + i;
+        double adv = adv_a * rho * (-phi[i] * dA);
+        double dif = 0.0;
+        for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * Pi[a][pp];
+        dif *= -dA;
+        double src = f[a] * (phi[i] * dA);
+        Re[ri] += adv + dif + src;
+        /* J_m_v */
+        double gi_dot_gam = 0.0;
+        for (int pp = 0; pp < dim; pp++) gi_dot_gam += gphi[i][pp] * gam[a][pp];
+        for (int b = 0; b < dim; b++)
+          for (int j = 0; j < nn; j++) {
+            double adv_j = phi[j] * gv[b][a];
+            if (a == b)
+              for (int pp = 0; pp < dim; pp++) adv_j += v[pp] * gphi[j][pp];
+            adv_j *= rho * (-phi[i] * dA);
+            double dd = mu * gphi[i][b] * gphi[j][a];
+            if (a == b)
+              for (int pp = 0; pp < dim; pp++) dd += mu * gphi[i][pp] * gphi[j][pp];
+            dd += dmu_v[b][j] * gi_dot_gam;
+            dd *= -dA;
+            JE(ri, b * nn + j) += adv_j + dd;
+          }
+        /* J_m_P */
+        for (int l = 0; l < npr; l++) JE(ri, oP + l) += gphi[i][a] * psi[l] * dA;
+        /* J_m_T */
+        if (en)
+          for (int j = 0; j < nn; j++) JE(ri, oT + j) += phi[i] * (dfT[a] * phi[j]) * dA;
+      }
+    }
+    /* continuity */
+    for (int l = 0; l < npr; l++) {
+      const int rl = oP + l;
+      Re[rl] += divv * (psi[l] * dA);
+      for (int b = 0; b < dim; b++)
+        for (int j = 0; j < nn; j++) JE(rl, b * nn + j) += psi[l] * gphi[j][b] * dA;
+    }
+    /* energy */
+    if (en) {
+      double vgT = 0.0;
+      for (int pp = 0; pp < dim; pp++) vgT += v[pp] * gT[pp];
+      for (int i = 0; i < nn; i++) {
+        const int ri = oT + i;
+        double adv = vgT * (-phi[i] * rcp * dA);
+        double dif = 0.0;
+        for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * (-kc * gT[pp]);
+        dif *= dA;
+        Re[ri] += adv + dif;
+        for (int j = 0; j < nn; j++) {
+          double vgj = 0.0, gij = 0.0;
+          for (int pp = 0; pp < dim; pp++) {
+            vgj += v[pp] * gphi[j][pp];
+            gij += gphi[i][pp] * gphi[j][pp];
+          }
+          JE(ri, oT + j) += rcp * vgj * (-phi[i] * dA) - kc * gij * dA;
+          for (int b = 0; b < dim; b++)
+            JE(ri, b * nn + j) += rcp * phi[j] * gT[b] * (-phi[i] * dA);
+        }
+      }
+    }
+  }
+  if (apply_bc) {
+    for (int r = 0; r < nloc; r++) {
+      if (p->dbc[g[r]] == -1) continue;
+      for (int c = 0; c < nloc; c++) JE(r, c) = 0.0;
+      JE(r, r) = 1.0;
+      Re[r] = 0.0;
+    }
+  }
+#undef JE
+  return status;
+}
+
+/* Scatter of load_lec (src/mm_fill.c:5241): a[diag] / a[off-diag slot]
+ * += element entries, elements in order. */
+int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1) {
+  const int nloc = p->nloc;
+  double *Re = (double *)malloc(sizeof(double) * (size_t)nloc);
+  double *Je = (double *)malloc(sizeof(double) * (size_t)nloc * nloc);
+  int g[27 * 4 + 4];
+  int status = 0;
+  for (int e = e0; e < e1; e++) {
+    if (orc_element(p, e, x, Re, Je, 1) != 0) status = -1;
+    orc_element_dofs(p, e, g);
+    for (int r = 0; r < nloc; r++) {
+      const int gr = g[r];
+      R[gr] += Re[r];
+      if (!a) continue;
+      const int s0 = p->ija[gr], s1 = p->ija[gr + 1];
+      for (int c = 0; c < nloc; c++) {
+        const int gc = g[c];
+        const double v = Je[(size_t)r * nloc + c];
+        if (gc == gr) {
+          a[gr] += v;
+          continue;
+        }
+        int lo = s0, hi = s1 - 1; /* columns ascend: bisection */
+        while (lo <= hi) {
+          int mid = (lo + hi) >> 1;
+          if (p->ija[mid] < gc)
+            lo = mid + 1;
+          else
+            hi = mid - 1;
+        }
+        if (lo >= s1 || p->ija[lo] != gc) {
+          /* masked pair (energy row, pressure column): always zero */
+          if (v == 0.0) continue;
+          fprintf(stderr, "oracle: missing MSR slot (%d,%d)\n", gr, gc);
+          abort();
+        }
+        a[lo] += v;
+      }
+    }
+  }
+  free(Re);
+  free(Je);
+  return status;
+}
+
+/* row_sum_scale_MSR (src/sl_matrix_util.c:506) */
+void orc_row_sum_scale(const orc_problem *p, double *a, double *R, double *scale) {
+  for (int i = 0; i < p->N; i++) {
+    double s = fabs(a[i]);
+    for (int k = p->ija[i]; k < p->ija[i + 1]; k++) s += fabs(a[k]);
+    if (fabs(a[i]) > 1.0e-200) s = a[i] < 0.0 ? -s : s;
+    if (s == 0.0) s = 1.0; /* the reference warns and keeps going */
+    scale[i] = s;
+    R[i] = R[i] / s;
+    a[i] = a[i] / s;
+    for (int k = p->ija[i]; k < p->ija[i + 1]; k++) a[k] /= s;
+  }
+}
+
+/* Banded Gaussian elimination with partial pivoting on the MSR system
+ * (the oracle's stand-in for the Krylov solve; only converged fields are
+ * compared). */
+static int band_solve(int N, const int *ija, const double *a, double *xb) {
+  int kl = 0, ku = 0;
+  for (int i = 0; i < N; i++)
+    for (int k = ija[i]; k < ija[i + 1]; k++) {
+      int j = ija[k];
+      if (i - j > kl) kl = i - j;
+      if (j - i > ku) ku = j - i;
+    }
+  const long w = 2L * kl + ku + 1;
+  double *Bd = (double *)calloc((size_t)N * (size_t)w, sizeof(double));
+  if (!Bd) return -1;
+#define BD(i, j) Bd[(size_t)(i) * (size_t)w + (size_t)((j) - (i) + kl)]
+  for (int i = 0; i < N; i++) {
+    BD(i, i) = a[i];
+    for (int k = ija[i]; k < ija[i + 1]; k++) BD(i, ija[k]) += a[k];
+  }
+  for (int c = 0; c < N; c++) {
+    int last = c + kl < N - 1 ? c + kl : N - 1, piv = c;
+    double best = fabs(BD(c, c));
+    for (int r = c + 1; r <= last; r++)
+      if (fabs(BD(r, c)) > best) {
+        best = fabs(BD(r, c));
+        piv = r;
+      }
+    if (best == 0.0) {
+      free(Bd);
+      return -1;
+    }
+    int cmax = c + kl + ku < N - 1 ? c + kl + ku : N - 1;
+    if (piv != c) {
+      for (int j = c; j <= cmax; j++) {
+        double t = BD(c, j);
+        BD(c, j) = BD(piv, j);
+        BD(piv, j) = t;
+      }
+      double t = xb[c];
+      xb[c] = xb[piv];
+      xb[piv] = t;
+    }
+    for (int r = c + 1; r <= last; r++) {
+      double fct = BD(r, c) / BD(c, c);
+      if (fct == 0.0) continue;
+      BD(r, c) = 0.0;
+      for (int j = c + 1; j <= cmax; j++) BD(r, j) -= fct * BD(c, j);
+      xb[r] -= fct * xb[c];
+    }
+  }
+  for (int i = N - 1; i >= 0; i--) {
+    int cmax = i + kl + ku < N - 1 ? i + kl + ku : N - 1;
+    double s = xb[i];
+    for (int j = i + 1; j <= cmax; j++) s -= BD(i, j) * xb[j];
+    xb[i] = s / BD(i, i);
+  }
+#undef BD
+  free(Bd);
+  return 0;
+}
+
+/* Newton loop of solve_nonlinear_problem (src/mm_sol_nonlinear.c:1108):
+ * assemble, row-sum scale, converged when after at least one update the
+ * scaled residual has L2 and L-infinity norms below tol (:1482-1486),
+ * otherwise solve and take the full step x -= dx (:2553-2557). */
+int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *norms) {
+  const int N = p->N;
+  double *R = (double *)malloc(sizeof(double) * (size_t)N);
+  double *a = (double *)malloc(sizeof(double) * (size_t)p->msr_len);
+  double *sc = (double *)malloc(sizeof(double) * (size_t)N);
+  int result = -1;
+  for (int it = 0; it < max_it; it++) {
+    memset(R, 0, sizeof(double) * (size_t)N);
+    memset(a, 0, sizeof(double) * (size_t)p->msr_len);
+    if (orc_matrix_fill(p, x, R, a, 0, p->d.num_elems) != 0) break;
+    orc_row_sum_scale(p, a, R, sc);
+    double l2 = 0.0, loo = 0.0;
+    for (int i = 0; i < N; i++) {
+      l2 += R[i] * R[i];
+      if (fabs(R[i]) > loo) loo = fabs(R[i]);
+    }
+    l2 = sqrt(l2);
+    if (norms) norms[it] = l2;
+    if (!isfinite(l2)) break;
+    if (it > 0 && l2 < tol && loo < tol) {
+      result = it;
+      break;
+    }
+    if (band_solve(N, p->ija, a, R) != 0) break;
+    for (int i = 0; i < N; i++) x[i] -= R[i];
+  }
+  free(R);
+  free(a);
+  free(sc);
+  return result;
+}
+
+/* ------------------------------------------------- mesh generator access */
+#include "mesh_gen.h"
+
+int orc_mesh_sizes(const char *spec, int *num_nodes, int *num_elems, int *set_total) {
+  gb_mesh m;
+  if (gb_mesh_build_from_spec(&m, spec) != 0) return -1;
+  *num_nodes = m.num_nodes;
+  *num_elems = m.num_elems;
+  *set_total = 0;
+  for (int s = 0; s < m.num_sets; s++) *set_total += m.set_len[s];
+  gb_mesh_free(&m);
+  return 0;
+}
+
+int orc_mesh_fill(const char *spec, double *coords, int *conn, int *set_len, int *set_nodes) {
+  gb_mesh m;
+  if (gb_mesh_build_from_spec(&m, spec) != 0) return -1;
+  for (int i = 0; i < m.num_nodes; i++) {
+    coords[(size_t)i * m.dim + 0] = m.x[i];
+    coords[(size_t)i * m.dim + 1] = m.y[i];
+    if (m.dim == 3) coords[(size_t)i * m.dim + 2] = m.z[i];
+  }
+  memcpy(conn, m.conn, sizeof(int) * (size_t)m.num_elems * m.nodes_per_elem);
+  int off = 0;
+  for (int s = 0; s < m.num_sets; s++) {
+    set_len[s] = m.set_len[s];
+    memcpy(set_nodes + off, m.set_nodes[s], sizeof(int) * (size_t)m.set_len[s]);
+    off += m.set_len[s];
+  }
+  gb_mesh_free(&m);
+  return 0;
+}

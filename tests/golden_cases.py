@@ -1,0 +1,59 @@
+"""Build the problems of the golden cases (tests/golden/*.npz) with the
+package's own problem description, so every consumer compares like with
+like."""
+import json
+import os
+
+import numpy as np
+
+from goma_gb300 import problem as pb
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names(mode=None):
+    out = []
+    for f in sorted(os.listdir(GOLDEN)):
+        if f.endswith(".npz"):
+            n = f[:-4]
+            if mode is None or load(n)[1]["mode"] == mode:
+                out.append(n)
+    return out
+
+
+def load(name):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return g, json.loads(str(g["case"]))
+
+
+def problem_from_case(case):
+    mesh = pb.mesh_from_spec(case["mesh"])
+    v = case["visc"]
+    if v[0] == "newtonian":
+        mat = pb.Material(density=case["rho"], viscosity=v[1])
+    else:
+        mat = pb.Material(density=case["rho"], viscosity_model=pb.VISC_CARREAU, mu0=v[1],
+                          mu_inf=v[2], lam=v[3], aexp=v[4], nexp=v[5])
+    energy = case["phys"] == "nst"
+    if energy:
+        mat.momentum_source_model = pb.SOURCE_BOUSSINESQ
+        mat.momentum_source = (0.0, 0.0, -case["ra_pr"])
+        mat.volume_expansion = 1.0
+        mat.reference_temperature = 0.5
+        mat.heat_capacity = 1.0
+        mat.conductivity = 1.0
+    bcs = {"cavity2d": pb.CAVITY2D_BCS, "bfs2d": pb.BFS2D_BCS,
+           "cube_heated": pb.HEATED3D_BCS}[case["bc"]]
+    return pb.Problem(mesh, mat, energy, list(bcs), (0, 0.0) if case["datum"] else (-1, 0.0))
+
+
+def msr_row_scaled_error(ija, a, ref):
+    """max over rows of max_j |a_ij - ref_ij| / max_j |ref_ij| (MSR)."""
+    N = ija[0] - 1
+    worst = 0.0
+    for i in range(N):
+        lo, hi = ija[i], ija[i + 1]
+        scale = max(abs(ref[i]), np.abs(ref[lo:hi]).max() if hi > lo else 0.0, 1e-300)
+        d = max(abs(a[i] - ref[i]), np.abs(a[lo:hi] - ref[lo:hi]).max() if hi > lo else 0.0)
+        worst = max(worst, d / scale)
+    return worst
