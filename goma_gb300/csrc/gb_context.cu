@@ -1,0 +1,358 @@
+// Problem context: device copies of the layout, the reference-element
+// tables, the assembly driver and the C ABI of include/gb_newton.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gb_newton.h"
+#include "gb_context.h"
+
+namespace gb {
+
+thread_local std::string g_err;
+
+int fail(const std::string &m) {
+  g_err = m;
+  return -1;
+}
+int cuda_fail(cudaError_t e, const char *where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return -1;
+}
+
+// Reference-element tables at the Gauss points, in the reference's point
+// order (src/el_elm_info.c:1748 QUAD9, :1802 HEX27) and with its literal
+// constants (:1642 abscissa, :3484-3485 weights); Q2 basis as tensor
+// products of the 1-D quadratic Lagrange polynomials on -1, 0, +1 (the
+// polynomials of src/rf_shape.c:361 BIQUAD_QUAD and :1105 TRIQUAD_HEX).
+static const int kLoc9[9][2] = {{0, 0}, {2, 0}, {2, 2}, {0, 2}, {1, 0},
+                                {2, 1}, {1, 2}, {0, 1}, {1, 1}};
+static const int kLoc27[27][3] = {
+    {0, 0, 0}, {2, 0, 0}, {2, 2, 0}, {0, 2, 0}, {0, 0, 2}, {2, 0, 2}, {2, 2, 2},
+    {0, 2, 2}, {1, 0, 0}, {2, 1, 0}, {1, 2, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 1},
+    {2, 2, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 2}, {1, 2, 2}, {0, 1, 2}, {1, 1, 1},
+    {1, 1, 0}, {1, 1, 2}, {0, 1, 1}, {2, 1, 1}, {1, 0, 1}, {1, 2, 1}};
+static const double kPt[3] = {0.77459666924148340428, 0.0, -0.77459666924148340428};
+static const double kWt[3] = {0.55555555555555555556, 0.88888888888888888888,
+                              0.55555555555555555556};
+static double lag(int g, double s) {
+  return g == 0 ? 0.5 * s * (s - 1.0) : (g == 1 ? 1.0 - s * s : 0.5 * s * (s + 1.0));
+}
+static double dlag(int g, double s) { return g == 0 ? s - 0.5 : (g == 1 ? -2.0 * s : s + 0.5); }
+
+void build_tables(int dim, std::vector<double> &phi, std::vector<double> &dphi,
+                  std::vector<double> &w) {
+  const int nn = dim == 2 ? 9 : 27, nq = nn;
+  phi.assign(nq * nn, 0.0);
+  dphi.assign(nq * nn * dim, 0.0);
+  w.assign(nq, 0.0);
+  for (int q = 0; q < nq; q++) {
+    const int is = q % 3, it = (q % 9) / 3, iu = q / 9;
+    const double s = kPt[is], t = kPt[it], u = dim == 3 ? kPt[iu] : 0.0;
+    w[q] = dim == 3 ? kWt[is] * kWt[it] * kWt[iu] : kWt[is] * kWt[it];
+    for (int k = 0; k < nn; k++) {
+      if (dim == 2) {
+        const int gx = kLoc9[k][0], gy = kLoc9[k][1];
+        phi[q * nn + k] = lag(gx, s) * lag(gy, t);
+        dphi[(q * nn + k) * 2 + 0] = dlag(gx, s) * lag(gy, t);
+        dphi[(q * nn + k) * 2 + 1] = lag(gx, s) * dlag(gy, t);
+      } else {
+        const int gx = kLoc27[k][0], gy = kLoc27[k][1], gz = kLoc27[k][2];
+        phi[q * nn + k] = lag(gx, s) * lag(gy, t) * lag(gz, u);
+        dphi[(q * nn + k) * 3 + 0] = dlag(gx, s) * lag(gy, t) * lag(gz, u);
+        dphi[(q * nn + k) * 3 + 1] = lag(gx, s) * dlag(gy, t) * lag(gz, u);
+        dphi[(q * nn + k) * 3 + 2] = lag(gx, s) * lag(gy, t) * dlag(gz, u);
+      }
+    }
+  }
+}
+
+template <class T>
+static int upload(T **dst, const std::vector<T> &src, const char *what) {
+  size_t n = src.size() ? src.size() : 1;
+  cudaError_t e = cudaMalloc((void **)dst, n * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  if (src.size()) {
+    e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+  }
+  return 0;
+}
+
+// CSR value k of row i lands at MSR position i (diagonal) or
+// N + 1 + k - i - (k > diag(i)).
+__global__ void csr_to_msr_kernel(int N, const int64_t *__restrict__ rowptr,
+                                  const int *__restrict__ colidx, const double *__restrict__ vals,
+                                  double *__restrict__ msr) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= N) return;
+  const int i = warp;
+  const int64_t r0 = rowptr[i], r1 = rowptr[i + 1];
+  for (int64_t k = r0 + lane; k < r1; k += 32) {
+    const int c = colidx[k];
+    if (c == i) {
+      msr[i] = vals[k];
+    } else {
+      const int64_t pos = (int64_t)N + 1 + k - i - (c > i ? 1 : 0);
+      msr[pos] = vals[k];
+    }
+  }
+  if (i == 0 && lane == 0) msr[N] = 0.0;
+}
+
+Context::~Context() {
+  void *ptrs[] = {d_coords, d_conn,   d_fu,     d_dbc,     d_dbc_val, d_rowptr, d_colidx,
+                  d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
+                  d_tab_pt, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int Context::init(const gb_problem_desc *d) {
+  desc = *d;
+  if (build_layout(d, L, g_err) != 0) return -1;
+  const gb_material &m = d->mat;
+  if (m.viscosity_model != GB_VISC_NEWTONIAN && m.viscosity_model != GB_VISC_CARREAU)
+    return fail("unsupported viscosity model");
+  if (m.momentum_source_model != GB_SOURCE_CONSTANT &&
+      m.momentum_source_model != GB_SOURCE_BOUSSINESQ)
+    return fail("unsupported momentum source model");
+  mat.density = m.density;
+  mat.viscosity = m.viscosity;
+  mat.mu0 = m.mu0;
+  mat.mu_inf = m.mu_inf;
+  mat.lambda = m.lambda;
+  mat.aexp = m.aexp;
+  mat.nexp = m.nexp;
+  mat.heat_capacity = m.heat_capacity;
+  mat.conductivity = m.conductivity;
+  mat.source_model = m.momentum_source_model;
+  for (int a = 0; a < 3; a++) mat.source[a] = m.momentum_source[a];
+  mat.beta = m.volume_expansion;
+  mat.Tref = m.reference_temperature;
+  carreau = m.viscosity_model == GB_VISC_CARREAU;
+
+  cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+  std::vector<double> coords(d->coords, d->coords + (size_t)d->num_nodes * d->dim);
+  std::vector<int> conn(d->conn, d->conn + (size_t)d->num_elems * L.nn);
+  std::vector<double> tphi, tdphi, tw;
+  build_tables(L.dim, tphi, tdphi, tw);
+  std::vector<double> tpt(kPt, kPt + 3);
+  if (upload(&d_coords, coords, "coords") || upload(&d_conn, conn, "conn") ||
+      upload(&d_fu, L.fu, "fu") || upload(&d_dbc, L.dbc, "dbc") ||
+      upload(&d_dbc_val, L.dbc_val, "dbc_val") || upload(&d_rowptr, L.rowptr, "rowptr") ||
+      upload(&d_colidx, L.colidx, "colidx") || upload(&d_nbr_ptr, L.nbr_ptr, "nbr_ptr") ||
+      upload(&d_nbr_off, L.nbr_off, "nbr_off") || upload(&d_nbr_offT, L.nbr_offT, "nbr_offT") ||
+      upload(&d_nslot, L.elem_nslot, "elem_nslot") || upload(&d_tab_phi, tphi, "tab") ||
+      upload(&d_tab_dphi, tdphi, "tab") || upload(&d_tab_w, tw, "tab") ||
+      upload(&d_tab_pt, tpt, "tab") || upload(&d_color_elems, L.color_elems, "colors"))
+    return -1;
+  if ((e = cudaMalloc(&d_x, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "x");
+  if ((e = cudaMalloc(&d_R, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "R");
+  if ((e = cudaMalloc(&d_vals, sizeof(double) * L.nnz)) != cudaSuccess)
+    return cuda_fail(e, "CSR values");
+  if ((e = cudaMalloc(&d_status, sizeof(int) * 2)) != cudaSuccess) return cuda_fail(e, "status");
+  return reset_status();
+}
+
+int Context::reset_status() {
+  int h[2] = {0, 0x7fffffff};
+  cudaError_t e = cudaMemcpyAsync(d_status, h, sizeof(h), cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "status reset");
+}
+
+AsmArgs Context::args(const double *x, double *R, double *vals) const {
+  AsmArgs a;
+  a.coords = d_coords;
+  a.conn = d_conn;
+  a.fu = d_fu;
+  a.dbc = d_dbc;
+  a.rowptr = d_rowptr;
+  a.nbr_ptr = d_nbr_ptr;
+  a.nbr_off = d_nbr_off;
+  a.nbr_offT = d_nbr_offT;
+  a.elem_nslot = d_nslot;
+  a.tab_phi = d_tab_phi;
+  a.tab_dphi = d_tab_dphi;
+  a.tab_w = d_tab_w;
+  a.tab_pt = d_tab_pt;
+  a.x = x;
+  a.R = R;
+  a.vals = vals;
+  a.status = d_status;
+  a.mat = mat;
+  return a;
+}
+
+int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st) {
+  if (!st) st = stream;
+  cudaError_t e = cudaMemsetAsync(R, 0, sizeof(double) * L.N, st);
+  if (e == cudaSuccess && vals) e = cudaMemsetAsync(vals, 0, sizeof(double) * L.nnz, st);
+  if (e != cudaSuccess) return cuda_fail(e, "assembly zeroing");
+  AsmArgs a = args(x, R, vals);
+  const int ncol = (int)L.color_ptr.size() - 1;
+  for (int c = 0; c < ncol; c++) {
+    const int n = L.color_ptr[c + 1] - L.color_ptr[c];
+    e = launch_assemble(a, L.dim, L.energy != 0, carreau, vals != nullptr,
+                        d_color_elems + L.color_ptr[c], n, st);
+    if (e != cudaSuccess) return cuda_fail(e, "assembly launch");
+  }
+  return 0;
+}
+
+int Context::check_status() {
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(e, "stream");
+  int h[2];
+  e = cudaMemcpy(h, d_status, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "status");
+  if (reset_status()) return -1;
+  if (h[0] > 0) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "%d element(s) with non-positive Jacobian determinant (first %d)",
+             h[0], h[1]);
+    return fail(buf);
+  }
+  return 0;
+}
+
+int Context::to_msr_host(const double *vals, double *a_msr) {
+  cudaError_t e;
+  const int64_t len = layout_msr_length(L);
+  if (!d_msr) {
+    e = cudaMalloc(&d_msr, sizeof(double) * len);
+    if (e != cudaSuccess) return cuda_fail(e, "msr buffer");
+  }
+  const int threads = 256, blocks = (int)(((int64_t)L.N * 32 + threads - 1) / threads);
+  csr_to_msr_kernel<<<blocks, threads, 0, stream>>>(L.N, d_rowptr, d_colidx, vals, d_msr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "csr_to_msr");
+  e = cudaMemcpyAsync(a_msr, d_msr, sizeof(double) * len, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return e == cudaSuccess ? 0 : cuda_fail(e, "msr copy");
+}
+
+}  // namespace gb
+
+using gb::Context;
+using gb::fail;
+using gb::cuda_fail;
+
+struct gb_ctx {
+  Context c;
+};
+
+extern "C" {
+
+const char *gb_last_error(void) { return gb::g_err.c_str(); }
+
+int gb_create(const gb_problem_desc *desc, gb_ctx **out) {
+  if (!out) return fail("out is NULL");
+  *out = nullptr;
+  gb_ctx *h = new (std::nothrow) gb_ctx;
+  if (!h) return fail("out of host memory");
+  if (h->c.init(desc) != 0) {
+    delete h;
+    return -1;
+  }
+  *out = h;
+  return 0;
+}
+
+void gb_destroy(gb_ctx *ctx) { delete ctx; }
+
+int gb_num_unknowns(const gb_ctx *ctx) { return ctx ? ctx->c.L.N : -1; }
+long long gb_msr_length(const gb_ctx *ctx) { return ctx ? gb::layout_msr_length(ctx->c.L) : -1; }
+long long gb_csr_nnz(const gb_ctx *ctx) { return ctx ? ctx->c.L.nnz : -1; }
+int gb_num_colors(const gb_ctx *ctx) { return ctx ? (int)ctx->c.L.color_ptr.size() - 1 : -1; }
+
+int gb_msr_pattern(const gb_ctx *ctx, int *ija) {
+  if (!ctx || !ija) return fail("NULL argument");
+  if (gb::layout_msr_length(ctx->c.L) > 2147483647LL)
+    return fail("MSR length exceeds the reference's 32-bit int indexing");
+  gb::layout_msr_pattern(ctx->c.L, ija);
+  return 0;
+}
+
+int gb_msr_pattern_host(const gb_problem_desc *desc, int *ija, long long *msr_length) {
+  gb::Layout L;
+  if (gb::build_layout(desc, L, gb::g_err) != 0) return -1;
+  const long long len = gb::layout_msr_length(L);
+  if (msr_length) *msr_length = len;
+  if (len > 2147483647LL) return fail("MSR length exceeds the reference's 32-bit int indexing");
+  if (ija) gb::layout_msr_pattern(L, ija);
+  return 0;
+}
+
+int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx) {
+  if (!ctx || !rowptr || !colidx) return fail("NULL argument");
+  const gb::Layout &L = ctx->c.L;
+  for (int i = 0; i <= L.N; i++) rowptr[i] = L.rowptr[i];
+  memcpy(colidx, L.colidx.data(), sizeof(int) * L.colidx.size());
+  return 0;
+}
+
+int gb_first_unknown(const gb_ctx *ctx, int *fu) {
+  if (!ctx || !fu) return fail("NULL argument");
+  memcpy(fu, ctx->c.L.fu.data(), sizeof(int) * ctx->c.L.fu.size());
+  return 0;
+}
+
+int gb_dirichlet_init(const gb_ctx *ctx, double *x) {
+  if (!ctx || !x) return fail("NULL argument");
+  const gb::Layout &L = ctx->c.L;
+  for (int i = 0; i < L.N; i++)
+    if (L.dbc[i]) x[i] = L.dbc_val[i];
+  return 0;
+}
+
+int gb_matrix_fill_full_device(gb_ctx *ctx, const double *d_x, double *d_R, double *d_vals,
+                               void *stream) {
+  if (!ctx || !d_x || !d_R) return fail("NULL argument");
+  return ctx->c.assemble(d_x, d_R, d_vals, (cudaStream_t)stream);
+}
+
+int gb_status(gb_ctx *ctx) {
+  if (!ctx) return fail("NULL argument");
+  return ctx->c.check_status();
+}
+
+int gb_matrix_fill_full(gb_ctx *ctx, const double *x, double *resid_vector, double *a_msr) {
+  if (!ctx || !x || !resid_vector) return fail("NULL argument");
+  Context &c = ctx->c;
+  cudaError_t e = cudaMemcpyAsync(c.d_x, x, sizeof(double) * c.L.N, cudaMemcpyHostToDevice,
+                                  c.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "x copy");
+  if (c.assemble(c.d_x, c.d_R, a_msr ? c.d_vals : nullptr, c.stream)) return -1;
+  e = cudaMemcpyAsync(resid_vector, c.d_R, sizeof(double) * c.L.N, cudaMemcpyDeviceToHost,
+                      c.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "R copy");
+  if (a_msr && c.to_msr_host(c.d_vals, a_msr)) return -1;
+  return c.check_status();
+}
+
+int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
+                      const long long **d_rowptr, const int **d_colidx) {
+  if (!ctx) return fail("NULL argument");
+  if (d_x) *d_x = ctx->c.d_x;
+  if (d_R) *d_R = ctx->c.d_R;
+  if (d_vals) *d_vals = ctx->c.d_vals;
+  if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
+  if (d_colidx) *d_colidx = ctx->c.d_colidx;
+  return 0;
+}
+
+void *gb_stream(gb_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr) {
+  if (!ctx || !d_vals || !a_msr) return fail("NULL argument");
+  return ctx->c.to_msr_host(d_vals, a_msr);
+}
+
+}  // extern "C"

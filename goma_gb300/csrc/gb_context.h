@@ -1,0 +1,47 @@
+// Per-problem state behind the gb_ctx handle of include/gb_newton.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "gb_device.h"
+#include "gb_layout.h"
+
+namespace gb {
+
+extern thread_local std::string g_err;
+int fail(const std::string &m);
+int cuda_fail(cudaError_t e, const char *where);
+
+struct Context {
+  gb_problem_desc desc{};
+  Layout L;
+  MaterialDev mat{};
+  bool carreau = false;
+  cudaStream_t stream = nullptr;
+  double *d_coords = nullptr;
+  int *d_conn = nullptr;
+  int *d_fu = nullptr;
+  uint8_t *d_dbc = nullptr;
+  double *d_dbc_val = nullptr;
+  int64_t *d_rowptr = nullptr;
+  int *d_colidx = nullptr;
+  int *d_nbr_ptr = nullptr, *d_nbr_off = nullptr, *d_nbr_offT = nullptr;
+  uint16_t *d_nslot = nullptr;
+  double *d_tab_phi = nullptr, *d_tab_dphi = nullptr, *d_tab_w = nullptr, *d_tab_pt = nullptr;
+  int *d_color_elems = nullptr;
+  double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
+  int *d_status = nullptr;
+  double *d_msr = nullptr;
+
+  ~Context();
+  int init(const gb_problem_desc *d);
+  AsmArgs args(const double *x, double *R, double *vals) const;
+  // zero R (and vals), then launch one kernel per colour on st
+  int assemble(const double *x, double *R, double *vals, cudaStream_t st);
+  int reset_status();
+  int check_status();
+  int to_msr_host(const double *vals, double *a_msr);
+};
+
+}  // namespace gb

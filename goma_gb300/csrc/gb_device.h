@@ -1,0 +1,45 @@
+// Device-side argument blocks shared by the kernels and the host driver.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/gb_problem.h"
+
+namespace gb {
+
+struct MaterialDev {
+  double density, viscosity, mu0, mu_inf, lambda, aexp, nexp;
+  double heat_capacity, conductivity;
+  int source_model;
+  double source[3];
+  double beta, Tref;
+};
+
+// Everything the assembly kernel reads or writes.  Device pointers.
+struct AsmArgs {
+  const double *coords;  // num_nodes * dim
+  const int *conn;       // num_elems * nn
+  const int *fu;         // num_nodes + 1
+  const uint8_t *dbc;    // N
+  const int64_t *rowptr; // N + 1
+  const int *nbr_ptr;
+  const int *nbr_off;
+  const int *nbr_offT;
+  const uint16_t *elem_nslot;  // num_elems * nn * nn
+  const double *tab_phi;       // nq * nn
+  const double *tab_dphi;      // nq * nn * dim
+  const double *tab_w;         // nq
+  const double *tab_pt;        // 3 Gauss abscissae (+pt, 0, -pt)
+  const double *x;             // N
+  double *R;                   // N
+  double *vals;                // nnz (CSR, diagonal in row); NULL: residual only
+  int *status;                 // [0] non-positive det J count, [1] first such element
+  MaterialDev mat;
+};
+
+cudaError_t launch_assemble(const AsmArgs &a, int dim, bool energy, bool carreau, bool jac,
+                            const int *elems, int nelem, cudaStream_t st);
+size_t assemble_smem_bytes(int dim, bool energy, bool carreau);
+
+}  // namespace gb

@@ -1,0 +1,234 @@
+// DOF map, sparsity and colouring of a Q2/P1 mesh.
+//
+// Unknown numbering restates Index_Solution (src/mm_unknown_map.c:5268):
+// node by node; per node the velocity components, then T when the energy
+// equation is on, and at an element's centroid node its dim+1 P1 pressure
+// unknowns.  The coupling graph restates build_node_node
+// (src/exo_conn.c:204) and find_MSR_problem_graph (src/mm_fill_util.c:3229):
+// an unknown couples with every unknown of every node that shares an
+// element with its node; a centroid node also couples with the centroid
+// nodes of its element's face neighbours (src/exo_conn.c:300-330); the
+// energy equation does not couple with pressure (set_interaction_masks,
+// src/mm_unknown_map.c:1125).  Rows keep the diagonal in place (CSR); the
+// reference's MSR form is the same order with the diagonal pulled out.
+#include "gb_layout.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace gb {
+
+int build_layout(const gb_problem_desc *d, Layout &L, std::string &err) {
+  if (!d || (d->dim != 2 && d->dim != 3)) {
+    err = "dim must be 2 (QUAD9) or 3 (HEX27)";
+    return -1;
+  }
+  if (d->num_nodes <= 0 || d->num_elems <= 0 || !d->coords || !d->conn) {
+    err = "empty mesh";
+    return -1;
+  }
+  L.dim = d->dim;
+  L.nn = d->dim == 2 ? 9 : 27;
+  L.centroid = d->dim == 2 ? 8 : 20;
+  L.energy = d->energy ? 1 : 0;
+  L.nvn = d->dim + L.energy;
+  L.npres = d->dim + 1;
+  L.nloc = L.nvn * L.nn + L.npres;
+  L.num_nodes = d->num_nodes;
+  L.num_elems = d->num_elems;
+  const int nn = L.nn, nnod = L.num_nodes, ne = L.num_elems;
+  for (int64_t i = 0; i < (int64_t)ne * nn; i++) {
+    if (d->conn[i] < 0 || d->conn[i] >= nnod) {
+      err = "connectivity references a node outside [0, num_nodes)";
+      return -1;
+    }
+  }
+  // centroid nodes
+  std::vector<int> cent_elem(nnod, -1);
+  for (int e = 0; e < ne; e++) {
+    int c = d->conn[(int64_t)e * nn + L.centroid];
+    if (cent_elem[c] != -1) {
+      err = "a centroid node is shared by two elements";
+      return -1;
+    }
+    cent_elem[c] = e;
+  }
+  L.fu.assign(nnod + 1, 0);
+  for (int n = 0; n < nnod; n++) L.fu[n + 1] = L.fu[n] + L.nvn + (cent_elem[n] >= 0 ? L.npres : 0);
+  if ((int64_t)L.fu[nnod] > 2000000000LL) {
+    err = "more than 2e9 unknowns";
+    return -1;
+  }
+  L.N = L.fu[nnod];
+  // node -> elements
+  std::vector<int> ne_ptr(nnod + 1, 0);
+  for (int64_t i = 0; i < (int64_t)ne * nn; i++) ne_ptr[d->conn[i] + 1]++;
+  for (int n = 0; n < nnod; n++) ne_ptr[n + 1] += ne_ptr[n];
+  std::vector<int> ne_list(ne_ptr[nnod]);
+  {
+    std::vector<int> fill(nnod, 0);
+    for (int e = 0; e < ne; e++)
+      for (int k = 0; k < nn; k++) {
+        int n = d->conn[(int64_t)e * nn + k];
+        ne_list[ne_ptr[n] + fill[n]++] = e;
+      }
+  }
+  const int side0 = d->dim == 2 ? 4 : 21, side1 = d->dim == 2 ? 8 : 27;
+  // node graph
+  L.nbr_ptr.assign(nnod + 1, 0);
+  std::vector<std::vector<int>> nbrs(nnod);
+  std::vector<int> tmp;
+  for (int n = 0; n < nnod; n++) {
+    tmp.clear();
+    for (int q = ne_ptr[n]; q < ne_ptr[n + 1]; q++) {
+      const int *c = d->conn + (int64_t)ne_list[q] * nn;
+      tmp.insert(tmp.end(), c, c + nn);
+    }
+    if (cent_elem[n] >= 0 && ne_ptr[n + 1] - ne_ptr[n] == 1) {
+      int e = cent_elem[n];
+      for (int k = side0; k < side1; k++) {
+        int m = d->conn[(int64_t)e * nn + k];
+        for (int q = ne_ptr[m]; q < ne_ptr[m + 1]; q++) {
+          int f = ne_list[q];
+          if (f != e) tmp.push_back(d->conn[(int64_t)f * nn + L.centroid]);
+        }
+      }
+    }
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    if (tmp.size() > 65535) {
+      err = "node with more than 65535 neighbours";
+      return -1;
+    }
+    nbrs[n] = tmp;
+    L.nbr_ptr[n + 1] = L.nbr_ptr[n] + (int)tmp.size();
+  }
+  L.nbr_node.resize(L.nbr_ptr[nnod]);
+  L.nbr_off.resize(L.nbr_ptr[nnod]);
+  L.nbr_offT.resize(L.nbr_ptr[nnod]);
+  std::vector<int64_t> len_all(nnod), len_T(nnod);
+  for (int n = 0; n < nnod; n++) {
+    int off = 0, offT = 0;
+    for (size_t s = 0; s < nbrs[n].size(); s++) {
+      int m = nbrs[n][s], q = L.nbr_ptr[n] + (int)s;
+      L.nbr_node[q] = m;
+      L.nbr_off[q] = off;
+      L.nbr_offT[q] = offT;
+      off += L.fu[m + 1] - L.fu[m];
+      offT += L.nvn;
+    }
+    len_all[n] = off;
+    len_T[n] = offT;
+  }
+  // CSR
+  L.rowptr.assign((size_t)L.N + 1, 0);
+  for (int n = 0; n < nnod; n++)
+    for (int i = L.fu[n]; i < L.fu[n + 1]; i++) {
+      bool rowT = L.energy && (i - L.fu[n]) == L.dim;
+      L.rowptr[i + 1] = rowT ? len_T[n] : len_all[n];
+    }
+  for (int i = 0; i < L.N; i++) L.rowptr[i + 1] += L.rowptr[i];
+  L.nnz = L.rowptr[L.N];
+  L.colidx.resize((size_t)L.nnz);
+  for (int n = 0; n < nnod; n++)
+    for (int i = L.fu[n]; i < L.fu[n + 1]; i++) {
+      bool rowT = L.energy && (i - L.fu[n]) == L.dim;
+      int64_t pos = L.rowptr[i];
+      for (int m : nbrs[n])
+        for (int j = L.fu[m]; j < L.fu[m + 1]; j++) {
+          if (rowT && j - L.fu[m] >= L.nvn) continue;
+          L.colidx[pos++] = j;
+        }
+    }
+  // element -> neighbour slots
+  L.elem_nslot.resize((size_t)ne * nn * nn);
+  for (int e = 0; e < ne; e++) {
+    const int *c = d->conn + (int64_t)e * nn;
+    for (int k = 0; k < nn; k++) {
+      const std::vector<int> &nb = nbrs[c[k]];
+      for (int l = 0; l < nn; l++) {
+        auto it = std::lower_bound(nb.begin(), nb.end(), c[l]);
+        L.elem_nslot[((size_t)e * nn + k) * nn + l] = (uint16_t)(it - nb.begin());
+      }
+    }
+  }
+  // Dirichlet cards in order, later cards win (src/mm_bc.c:132)
+  L.dbc.assign(L.N, 0);
+  L.dbc_val.assign(L.N, 0.0);
+  for (int c = 0; c < d->num_bc; c++) {
+    int var = d->bc_var[c], off;
+    if (var >= GB_VAR_U1 && var < GB_VAR_U1 + d->dim)
+      off = var;
+    else if (var == GB_VAR_T && L.energy)
+      off = d->dim;
+    else if (var == GB_VAR_T)
+      continue;
+    else {
+      err = "Dirichlet card on an unsupported variable";
+      return -1;
+    }
+    for (int q = d->bc_ptr[c]; q < d->bc_ptr[c + 1]; q++) {
+      int n = d->bc_nodes[q];
+      if (n < 0 || n >= nnod) {
+        err = "Dirichlet node outside the mesh";
+        return -1;
+      }
+      L.dbc[L.fu[n] + off] = 1;
+      L.dbc_val[L.fu[n] + off] = d->bc_value[c];
+    }
+  }
+  // PRESSURE DATUM: first pressure unknown of the element (src/mm_bc.c:418)
+  if (d->pressure_datum_elem >= 0) {
+    if (d->pressure_datum_elem >= ne) {
+      err = "pressure datum element out of range";
+      return -1;
+    }
+    int c = d->conn[(int64_t)d->pressure_datum_elem * nn + L.centroid];
+    L.dbc[L.fu[c] + L.nvn] = 1;
+    L.dbc_val[L.fu[c] + L.nvn] = d->pressure_datum_value;
+  }
+  // greedy colouring: elements sharing a node get different colours, so a
+  // colour's elements write disjoint CSR rows
+  std::vector<int> color(ne, -1);
+  int ncol = 0;
+  for (int e = 0; e < ne; e++) {
+    uint64_t used = 0;
+    const int *c = d->conn + (int64_t)e * nn;
+    for (int k = 0; k < nn; k++)
+      for (int q = ne_ptr[c[k]]; q < ne_ptr[c[k] + 1]; q++) {
+        int f = ne_list[q];
+        if (color[f] >= 0 && color[f] < 64) used |= 1ull << color[f];
+      }
+    int col = 0;
+    while (col < 64 && (used >> col & 1ull)) col++;
+    if (col >= 64) {
+      err = "element colouring needs more than 64 colours";
+      return -1;
+    }
+    color[e] = col;
+    ncol = std::max(ncol, col + 1);
+  }
+  L.color_ptr.assign(ncol + 1, 0);
+  for (int e = 0; e < ne; e++) L.color_ptr[color[e] + 1]++;
+  for (int k = 0; k < ncol; k++) L.color_ptr[k + 1] += L.color_ptr[k];
+  L.color_elems.resize(ne);
+  {
+    std::vector<int> fill(ncol, 0);
+    for (int e = 0; e < ne; e++) L.color_elems[L.color_ptr[color[e]] + fill[color[e]]++] = e;
+  }
+  return 0;
+}
+
+int64_t layout_msr_length(const Layout &L) { return (int64_t)L.N + 1 + (L.nnz - L.N); }
+
+void layout_msr_pattern(const Layout &L, int *ija) {
+  int64_t pos = (int64_t)L.N + 1;
+  for (int i = 0; i < L.N; i++) {
+    ija[i] = (int)pos;
+    for (int64_t k = L.rowptr[i]; k < L.rowptr[i + 1]; k++)
+      if (L.colidx[k] != i) ija[pos++] = L.colidx[k];
+  }
+  ija[L.N] = (int)pos;
+}
+
+}  // namespace gb

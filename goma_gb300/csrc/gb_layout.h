@@ -1,0 +1,39 @@
+// Host-side layout of one Q2/P1 problem: DOF map, CSR sparsity, the
+// node-neighbour offsets the assembly kernels use to find CSR slots, the
+// Dirichlet marks and the element colouring.  Built once per problem.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gb_problem.h"
+
+namespace gb {
+
+struct Layout {
+  int dim = 0, nn = 0, centroid = 0, nvn = 0, npres = 0, nloc = 0, energy = 0;
+  int num_nodes = 0, num_elems = 0, N = 0;
+  int64_t nnz = 0;              // CSR entries, diagonal included
+  std::vector<int> fu;          // first unknown per node (num_nodes + 1)
+  std::vector<int64_t> rowptr;  // N + 1
+  std::vector<int> colidx;      // nnz, ascending per row
+  // Node graph: neighbours of node n are nbr_node[nbr_ptr[n] .. nbr_ptr[n+1]),
+  // ascending.  nbr_off / nbr_offT give the offset, within any row of node n,
+  // of neighbour s's first unknown (nbr_offT for the energy row, which skips
+  // pressure columns).
+  std::vector<int> nbr_ptr, nbr_node, nbr_off, nbr_offT;
+  // For element e and local nodes k, l: index s of node conn[e][l] in the
+  // neighbour list of node conn[e][k].
+  std::vector<uint16_t> elem_nslot;
+  std::vector<uint8_t> dbc;     // 1 on Dirichlet / pressure-datum unknowns
+  std::vector<double> dbc_val;  // their values (later cards win)
+  std::vector<int> color_ptr, color_elems;
+};
+
+// Returns 0 on success, -1 with a message in err.
+int build_layout(const gb_problem_desc *d, Layout &L, std::string &err);
+// MSR pattern of the reference (diagonal first, off-diagonals ascending).
+void layout_msr_pattern(const Layout &L, int *ija);
+int64_t layout_msr_length(const Layout &L);
+
+}  // namespace gb

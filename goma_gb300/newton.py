@@ -1,0 +1,106 @@
+"""Host-side mirror of the reference interface for the Newton path.
+
+``GomaNewton`` wraps one problem context of libgbnewton.so and exposes the
+calls a Goma maintainer would bind: the MSR pattern of
+alloc_MSR_sparse_arrays, matrix_fill_full, and (in later layers) the linear
+solve and solve_nonlinear_problem.  Host arrays are numpy; device arrays
+are raw pointers (e.g. ``torch.Tensor.data_ptr()``).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .problem import make_desc
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def msr_pattern_host(problem):
+    """The reference's MSR ija for a problem, computed on the host only."""
+    L = _lib.load()
+    desc, keep = make_desc(problem)
+    n = ctypes.c_longlong()
+    _lib.check(L.gb_msr_pattern_host(ctypes.byref(desc), None, ctypes.byref(n)))
+    ija = np.empty(n.value, np.int32)
+    _lib.check(L.gb_msr_pattern_host(ctypes.byref(desc), ija.ctypes.data_as(
+        ctypes.POINTER(ctypes.c_int)), ctypes.byref(n)))
+    del keep
+    return ija
+
+
+class GomaNewton:
+    """One Q2/P1 problem resident on the GPU."""
+
+    def __init__(self, problem):
+        self.problem = problem
+        self._L = _lib.load()
+        desc, keep = make_desc(problem)
+        h = ctypes.c_void_p()
+        _lib.check(self._L.gb_create(ctypes.byref(desc), ctypes.byref(h)))
+        self.h = h
+        del keep
+        self.N = self._L.gb_num_unknowns(self.h)
+        self.msr_len = self._L.gb_msr_length(self.h)
+        self.nnz = self._L.gb_csr_nnz(self.h)
+        self.num_colors = self._L.gb_num_colors(self.h)
+        x, R, v, rp, ci = (ctypes.c_void_p() for _ in range(5))
+        _lib.check(self._L.gb_device_buffers(self.h, ctypes.byref(x), ctypes.byref(R),
+                                             ctypes.byref(v), ctypes.byref(rp), ctypes.byref(ci)))
+        self.d_x, self.d_R, self.d_vals = x.value, R.value, v.value
+        self.d_rowptr, self.d_colidx = rp.value, ci.value
+        self.stream = self._L.gb_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self._L.gb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- setup queries
+    def msr_pattern(self):
+        ija = np.empty(self.msr_len, np.int32)
+        _lib.check(self._L.gb_msr_pattern(self.h, ija.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int))))
+        return ija
+
+    def csr_pattern(self):
+        rp = np.empty(self.N + 1, np.int64)
+        ci = np.empty(self.nnz, np.int32)
+        _lib.check(self._L.gb_csr_pattern(self.h, rp.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_longlong)), ci.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return rp, ci
+
+    def dirichlet_init(self, x):
+        x = np.ascontiguousarray(x, np.float64).copy()
+        _lib.check(self._L.gb_dirichlet_init(self.h, _dp(x)))
+        return x
+
+    # --- matrix_fill_full
+    def matrix_fill_full(self, x, jacobian=True):
+        """Host arrays in and out: returns (R, a_msr or None)."""
+        x = np.ascontiguousarray(x, np.float64)
+        R = np.empty(self.N)
+        a = np.empty(self.msr_len) if jacobian else None
+        _lib.check(self._L.gb_matrix_fill_full(self.h, _dp(x), _dp(R),
+                                               _dp(a) if a is not None else None))
+        return R, a
+
+    def matrix_fill_full_device(self, d_x, d_R, d_vals, stream=None):
+        """Device pointers; enqueued on ``stream`` (default: library stream)."""
+        _lib.check(self._L.gb_matrix_fill_full_device(self.h, d_x, d_R, d_vals, stream))
+
+    def status(self):
+        _lib.check(self._L.gb_status(self.h))
+
+    def csr_to_msr(self, d_vals):
+        a = np.empty(self.msr_len)
+        _lib.check(self._L.gb_csr_to_msr_host(self.h, d_vals, _dp(a)))
+        return a

@@ -1,0 +1,95 @@
+/* GB300 Newton hot path for Q2/P1 Navier-Stokes (+ energy): the C ABI of
+ * libgbnewton.so.
+ *
+ * This is the drop-in boundary for the reference's Newton path.  A Goma
+ * build links the library and calls these entry points where it calls the
+ * functions named beside each declaration.  Plain pointers and sizes only;
+ * every entry point returns 0 (GOMA_SUCCESS, include/mm_eh.h:34) or -1
+ * (GOMA_ERROR) and leaves a message for gb_last_error().  Nothing calls
+ * exit() or aborts.
+ *
+ * Host/device convention: functions without a _device suffix take HOST
+ * arrays and copy them in and out; _device variants take device pointers
+ * (allocated by the caller or obtained from gb_device_buffers) and a CUDA
+ * stream (NULL = the library's stream) and never synchronise the host.
+ */
+#ifndef GB_NEWTON_H
+#define GB_NEWTON_H
+
+#include "gb_problem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_ctx gb_ctx;
+
+/* Builds the DOF map, the CSR/MSR sparsity, the element colouring and the
+ * device copies of one problem; the state the reference builds in
+ * setup_problem (src/rf_setup_problem.c:194) and alloc_MSR_sparse_arrays
+ * (src/mm_fill_util.c:2865, called from src/rf_solve.c:769). */
+int gb_create(const gb_problem_desc *desc, gb_ctx **out);
+void gb_destroy(gb_ctx *ctx);
+/* Message of the last failed call on this thread ("" if none). */
+const char *gb_last_error(void);
+
+/* Sizes: unknowns N (NumUnknowns), MSR length ija[N] (the reference's
+ * "Number of matrix nonzeroes" + 1), CSR nonzeros (diagonal in row). */
+int gb_num_unknowns(const gb_ctx *ctx);
+long long gb_msr_length(const gb_ctx *ctx);
+long long gb_csr_nnz(const gb_ctx *ctx);
+int gb_num_colors(const gb_ctx *ctx);
+
+/* The reference's MSR pattern, bit for bit: ija[0..N] row pointers into
+ * the off-diagonal part (which starts at N+1), then the off-diagonal
+ * columns in ascending order (src/mm_fill_util.c:3229
+ * find_MSR_problem_graph).  ija holds gb_msr_length() ints. */
+int gb_msr_pattern(const gb_ctx *ctx, int *ija);
+/* Host-only form of the same query, without a GPU or a context: fills ija
+ * (may be NULL) and its length, as alloc_MSR_sparse_arrays does
+ * (src/mm_fill_util.c:2865). */
+int gb_msr_pattern_host(const gb_problem_desc *desc, int *ija, long long *msr_length);
+/* CSR pattern used on the device: rowptr (N+1, int64), colidx (nnz). */
+int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx);
+/* First unknown of every node (num_nodes + 1 ints), as
+ * Nodes[i]->First_Unknown (src/mm_unknown_map.c:758). */
+int gb_first_unknown(const gb_ctx *ctx, int *fu);
+/* Writes the Dirichlet values (later cards win) and the pressure datum into
+ * the host vector x, as find_and_set_Dirichlet does (src/mm_bc.c:132). */
+int gb_dirichlet_init(const gb_ctx *ctx, double *x);
+
+/* Drop-in for matrix_fill_full (src/mm_fill.c:158): residual R and, when
+ * a_msr is not NULL, the analytic Jacobian in the reference's MSR layout
+ * (a_msr holds gb_msr_length() doubles; entry N is unused and written 0).
+ * Host arrays; R and a_msr are overwritten (the reference's caller zeroes
+ * them before the call, src/mm_sol_nonlinear.c:1114-1120, so the result is
+ * the same).  Returns -1 when an element has a non-positive Jacobian
+ * determinant, as matrix_fill_full does (src/mm_fill.c:217-312). */
+int gb_matrix_fill_full(gb_ctx *ctx, const double *x, double *resid_vector, double *a_msr);
+
+/* Device form: d_x (N), d_R (N) and d_vals (CSR values, gb_csr_nnz()) are
+ * device pointers; d_vals NULL assembles the residual only
+ * (af->Assemble_Jacobian = FALSE).  Enqueued on stream; the determinant
+ * status is checked at the next gb_status() call. */
+int gb_matrix_fill_full_device(gb_ctx *ctx, const double *d_x, double *d_R, double *d_vals,
+                               void *stream);
+/* Synchronises the library stream and reports the determinant status of
+ * all assemblies since the previous call: returns -1 (with the first bad
+ * element in the message) or 0. */
+int gb_status(gb_ctx *ctx);
+
+/* Library-owned device buffers: x (N), R (N), CSR values (nnz), and the
+ * CSR pattern (rowptr N+1 int64, colidx nnz int32). */
+int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
+                      const long long **d_rowptr, const int **d_colidx);
+/* The library's CUDA stream (a cudaStream_t). */
+void *gb_stream(gb_ctx *ctx);
+
+/* Converts device CSR values (same ctx) to the MSR layout in host memory
+ * (gb_msr_length() doubles). */
+int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,56 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry
+point declared in include/*.h, and its host-side layout reproduces the
+reference's MSR pattern bit for bit."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from goma_gb300 import _lib
+from goma_gb300.newton import msr_pattern_host
+from tests import golden_cases as gc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from goma_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) > 10
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("name", gc.names())
+def test_host_msr_pattern_matches_reference(lib, name):
+    g, case = gc.load(name)
+    ija = msr_pattern_host(gc.problem_from_case(case))
+    assert np.array_equal(ija, g["ija"])
+
+
+def test_host_layout_rejects_bad_connectivity(lib):
+    from goma_gb300 import problem as pb
+    prob = pb.lid_cavity_2d(2)
+    prob.mesh.conn = prob.mesh.conn.copy()
+    prob.mesh.conn[1, 3] = prob.mesh.num_nodes + 5
+    with pytest.raises(_lib.GbError, match="outside"):
+        msr_pattern_host(prob)
