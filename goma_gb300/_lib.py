@@ -12,6 +12,24 @@ LIB_PATH = os.path.join(HERE, "libgbnewton.so")
 _lib = None
 
 
+class NewtonOpts(ctypes.Structure):
+    """gb_newton_opts (include/gb_newton.h)."""
+    _fields_ = [("max_newton", ctypes.c_int), ("residual_tol", ctypes.c_double),
+                ("damping", ctypes.c_double), ("krylov_dim", ctypes.c_int),
+                ("max_linear_its", ctypes.c_int), ("linear_tol", ctypes.c_double),
+                ("linear_precision", ctypes.c_int), ("inner_tol", ctypes.c_double),
+                ("max_refinements", ctypes.c_int), ("verbose", ctypes.c_int)]
+
+
+class NewtonStats(ctypes.Structure):
+    """gb_newton_stats (include/gb_newton.h)."""
+    _fields_ = [("newton_its", ctypes.c_int), ("linear_its", ctypes.c_int),
+                ("refinements", ctypes.c_int), ("residual_l2", ctypes.c_double * 64),
+                ("residual_loo", ctypes.c_double), ("assemble_ms", ctypes.c_double),
+                ("scale_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
+                ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+
 class GbError(RuntimeError):
     pass
 
@@ -47,6 +65,15 @@ def load():
                                              ctypes.POINTER(vp)]),
         "gb_stream": (vp, [vp]),
         "gb_csr_to_msr_host": (ctypes.c_int, [vp, vp, dp]),
+        "gb_newton_opts_default": (None, [ctypes.POINTER(NewtonOpts)]),
+        "gb_solve_nonlinear_problem": (ctypes.c_int, [vp, dp, ctypes.POINTER(NewtonOpts), ip,
+                                                      ctypes.POINTER(NewtonStats)]),
+        "gb_solve_nonlinear_problem_device": (ctypes.c_int, [vp, vp, ctypes.POINTER(NewtonOpts),
+                                                             ip, ctypes.POINTER(NewtonStats)]),
+        "gb_row_sum_scale_device": (ctypes.c_int, [vp, vp, vp, vp]),
+        "gb_linear_solve_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(NewtonOpts), ip,
+                                                  dp]),
+        "gb_linear_solve": (ctypes.c_int, [vp, dp, dp, dp, ctypes.POINTER(NewtonOpts), ip, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

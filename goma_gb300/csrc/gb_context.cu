@@ -244,9 +244,6 @@ using gb::Context;
 using gb::fail;
 using gb::cuda_fail;
 
-struct gb_ctx {
-  Context c;
-};
 
 extern "C" {
 

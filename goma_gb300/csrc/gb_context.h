@@ -6,6 +6,9 @@
 
 #include "gb_device.h"
 #include "gb_layout.h"
+#include "gb_solve.h"
+
+#include <memory>
 
 namespace gb {
 
@@ -33,6 +36,7 @@ struct Context {
   double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
   int *d_status = nullptr;
   double *d_msr = nullptr;
+  std::unique_ptr<Solver> solver;
 
   ~Context();
   int init(const gb_problem_desc *d);
@@ -45,3 +49,8 @@ struct Context {
 };
 
 }  // namespace gb
+
+// the opaque handle of the C ABI
+struct gb_ctx {
+  gb::Context c;
+};

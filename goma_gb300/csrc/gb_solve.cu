@@ -1,0 +1,678 @@
+// Newton linear algebra on the device:
+//   row_sum_scale   restates row_sum_scale_MSR (src/sl_matrix_util.c:506)
+//   norms           L2_norm / L1_norm / Loo_norm (src/mm_sol_nonlinear.c:3177-3530)
+//   SpMV            MV_MSR semantics (src/sl_auxutil.c:373) on the CSR copy
+//   ILU(0)          the preconditioner AztecOO builds for "Preconditioner =
+//                   ilu" (dom_decomp + subdomain ILU(0), src/sl_util.c:556),
+//                   same ordering and pattern; factorised and applied by
+//                   node levels (one warp per node, unknowns of a node in
+//                   order), the level sequence replayed as a CUDA graph
+//   GMRES(m)        right-preconditioned restarted GMRES with classical
+//                   Gram-Schmidt + reorthogonalisation (the reference's
+//                   "Solution Algorithm = gmres", Krylov size 30,
+//                   src/sl_util.c:417) in FP64, or in FP32 inside FP64
+//                   iterative refinement
+// Reductions use a fixed grid and a fixed combination order, so every
+// result is bitwise reproducible run to run.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "gb_context.h"
+#include "gb_solve.h"
+
+namespace gb {
+
+static constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+static constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ------------------------------------------------------------ scaling
+
+__global__ void row_sum_scale_kernel(int N, const int64_t *__restrict__ rowptr,
+                                     const int64_t *__restrict__ diag, double *__restrict__ vals,
+                                     double *__restrict__ R, double *__restrict__ scale,
+                                     int *__restrict__ zero_rows) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= N) return;
+  const int64_t r0 = rowptr[i], r1 = rowptr[i + 1];
+  double s = 0.0;
+  for (int64_t k = r0 + lane; k < r1; k += 32) s += fabs(vals[k]);
+  s = warp_sum(s);
+  const double d = vals[diag[i]];
+  if (fabs(d) > 1.0e-200 && d < 0.0) s = -s;
+  if (s == 0.0) {
+    if (lane == 0) atomicAdd(zero_rows, 1);
+    s = 1.0;
+  }
+  for (int64_t k = r0 + lane; k < r1; k += 32) vals[k] = vals[k] / s;
+  if (lane == 0) {
+    scale[i] = s;
+    R[i] = R[i] / s;
+  }
+}
+
+// ------------------------------------------------------------ reductions
+
+template <class T>
+__global__ void norms_partial_kernel(int N, const T *__restrict__ x, double *__restrict__ part) {
+  __shared__ double sh[3][kRedThreads];
+  double s2 = 0.0, s1 = 0.0, mx = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double v = (double)x[i];
+    s2 = fma(v, v, s2);
+    s1 += fabs(v);
+    mx = fmax(mx, fabs(v));
+  }
+  sh[0][threadIdx.x] = s2;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+      sh[2][threadIdx.x] = fmax(sh[2][threadIdx.x], sh[2][threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 3 + 0] = sh[0][0];
+    part[blockIdx.x * 3 + 1] = sh[1][0];
+    part[blockIdx.x * 3 + 2] = sh[2][0];
+  }
+}
+
+__global__ void norms_final_kernel(int nblocks, const double *__restrict__ part,
+                                   double *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double s2 = 0.0, s1 = 0.0, mx = 0.0;
+  for (int b = 0; b < nblocks; b++) {
+    s2 += part[b * 3 + 0];
+    s1 += part[b * 3 + 1];
+    mx = fmax(mx, part[b * 3 + 2]);
+  }
+  out[0] = sqrt(s2);
+  out[1] = s1;
+  out[2] = mx;
+}
+
+// partial dots of w with the k columns V[0..k) (column stride ld)
+template <class T>
+__global__ void multidot_partial_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
+                                        const T *__restrict__ w, double *__restrict__ part) {
+  __shared__ double sh[kRedThreads];
+  for (int j = 0; j < k; j++) {
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+      s = fma((double)V[j * ld + i], (double)w[i], s);
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = sh[0];
+    __syncthreads();
+  }
+}
+
+__global__ void multidot_final_kernel(int k, int nblocks, const double *__restrict__ part,
+                                      double *__restrict__ out) {
+  const int j = threadIdx.x;
+  if (j >= k) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; b++) s += part[j * nblocks + b];
+  out[j] = s;
+}
+
+// w -= sum_j h[j] V[:, j]
+template <class T>
+__global__ void gemv_sub_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
+                                const double *__restrict__ h, T *__restrict__ w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double s = (double)w[i];
+    for (int j = 0; j < k; j++) s = fma(-h[j], (double)V[j * ld + i], s);
+    w[i] = (T)s;
+  }
+}
+
+// y = sum_j c[j] V[:, j]  (c on device)
+template <class T>
+__global__ void gemv_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
+                            const double *__restrict__ c, T *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < k; j++) s = fma(c[j], (double)V[j * ld + i], s);
+    y[i] = (T)s;
+  }
+}
+
+template <class T>
+__global__ void scale_copy_kernel(int N, const T *x, const double *__restrict__ alpha_inv, T *y) {
+  const double a = 1.0 / alpha_inv[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    y[i] = (T)((double)x[i] * a);
+}
+
+__global__ void axpy_kernel(int N, double a, const double *__restrict__ x, double *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    y[i] = fma(a, x[i], y[i]);
+}
+
+__global__ void axpy_f32_kernel(int N, double a, const float *__restrict__ x,
+                                double *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    y[i] = fma(a, (double)x[i], y[i]);
+}
+
+// x += t
+template <class T>
+__global__ void add_kernel(int N, const T *__restrict__ t, T *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    x[i] = (T)((double)x[i] + (double)t[i]);
+}
+
+// r = b - r   (r holds A x on entry)
+template <class T>
+__global__ void sub_from_kernel(int N, const T *__restrict__ b, T *__restrict__ r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    r[i] = (T)((double)b[i] - (double)r[i]);
+}
+
+// r = b - r   (r holds A x on entry)
+__global__ void residual_kernel(int N, const double *__restrict__ b, double *__restrict__ r) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    r[i] = b[i] - r[i];
+}
+
+// y32 = x / s  (normalised down-conversion)
+__global__ void to_f32_scaled_kernel(int N, const double *__restrict__ x, double s,
+                                     float *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    y[i] = (float)(x[i] / s);
+}
+
+__global__ void to_f32_kernel(int64_t n, const double *__restrict__ x, float *__restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+// ------------------------------------------------------------ SpMV
+
+// y = A x, LPR lanes per row (LPR divides 32)
+template <class T, int LPR>
+__global__ void spmv_kernel(int N, const int64_t *__restrict__ rowptr,
+                            const int *__restrict__ colidx, const T *__restrict__ vals,
+                            const T *__restrict__ x, T *__restrict__ y) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) / LPR;
+  const int l = threadIdx.x % LPR;
+  if (g >= N) return;
+  const int64_t r0 = rowptr[g], r1 = rowptr[g + 1];
+  double s = 0.0;
+  for (int64_t k = r0 + l; k < r1; k += LPR) s = fma((double)vals[k], (double)__ldg(x + colidx[k]), s);
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+  if (l == 0) y[g] = (T)s;
+}
+
+// ------------------------------------------------------------ ILU(0)
+
+// first position in [lo, hi) of a sorted column list holding c, or -1
+__device__ __forceinline__ int64_t find_col(const int *__restrict__ colidx, int64_t lo, int64_t hi,
+                                            int c) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (colidx[mid] < c)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// ILU(0) of the rows of the nodes of one level (IKJ order inside a row; the
+// rows of a node in increasing order), one warp per node.
+__global__ void ilu0_level_kernel(const int *__restrict__ nodes, int count,
+                                  const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
+                                  const int *__restrict__ colidx, const int64_t *__restrict__ diag,
+                                  double *__restrict__ lu) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= count) return;
+  const int n = nodes[w];
+  for (int i = fu[n]; i < fu[n + 1]; i++) {
+    const int64_t r0 = rowptr[i], r1 = rowptr[i + 1], di = diag[i];
+    for (int64_t p = r0; p < di; p++) {
+      const int k = colidx[p];
+      const double lik = lu[p] / lu[diag[k]];
+      __syncwarp();
+      if (lane == 0) lu[p] = lik;
+      const int64_t k1 = rowptr[k + 1];
+      for (int64_t q = diag[k] + 1 + lane; q < k1; q += 32) {
+        const int j = colidx[q];
+        const int64_t pos = find_col(colidx, p + 1, r1, j);
+        if (pos < r1 && colidx[pos] == j) lu[pos] = fma(-lik, lu[q], lu[pos]);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// forward solve with the unit lower factor, in place on z
+template <class T>
+__global__ void lsolve_level_kernel(const int *__restrict__ nodes, int count,
+                                    const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
+                                    const int *__restrict__ colidx,
+                                    const int64_t *__restrict__ diag, const T *__restrict__ lu,
+                                    T *__restrict__ z) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= count) return;
+  const int n = nodes[w];
+  for (int i = fu[n]; i < fu[n + 1]; i++) {
+    const int64_t r0 = rowptr[i], di = diag[i];
+    double s = 0.0;
+    for (int64_t p = r0 + lane; p < di; p += 32) s = fma((double)lu[p], (double)z[colidx[p]], s);
+    s = warp_sum(s);
+    if (lane == 0) z[i] = (T)((double)z[i] - s);
+    __syncwarp();
+  }
+}
+
+// backward solve with the upper factor, in place on z
+template <class T>
+__global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
+                                    const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
+                                    const int *__restrict__ colidx,
+                                    const int64_t *__restrict__ diag, const T *__restrict__ lu,
+                                    T *__restrict__ z) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= count) return;
+  const int n = nodes[w];
+  for (int i = fu[n + 1] - 1; i >= fu[n]; i--) {
+    const int64_t r1 = rowptr[i + 1], di = diag[i];
+    double s = 0.0;
+    for (int64_t p = di + 1 + lane; p < r1; p += 32) s = fma((double)lu[p], (double)z[colidx[p]], s);
+    s = warp_sum(s);
+    if (lane == 0) z[i] = (T)(((double)z[i] - s) / (double)lu[di]);
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------ schedule
+
+void build_ilu_schedule(const Layout &L, IluSchedule &S) {
+  const int nn = L.num_nodes;
+  std::vector<int> lev(nn, 0);
+  int maxl = 0;
+  for (int n = 0; n < nn; n++) {
+    int l = 0;
+    for (int q = L.nbr_ptr[n]; q < L.nbr_ptr[n + 1]; q++) {
+      const int m = L.nbr_node[q];
+      if (m < n) l = std::max(l, lev[m] + 1);
+    }
+    lev[n] = l;
+    maxl = std::max(maxl, l);
+  }
+  S.lo_ptr.assign(maxl + 2, 0);
+  for (int n = 0; n < nn; n++) S.lo_ptr[lev[n] + 1]++;
+  for (int l = 0; l <= maxl; l++) S.lo_ptr[l + 1] += S.lo_ptr[l];
+  S.lo_nodes.resize(nn);
+  {
+    std::vector<int> fill(maxl + 1, 0);
+    for (int n = 0; n < nn; n++) S.lo_nodes[S.lo_ptr[lev[n]] + fill[lev[n]]++] = n;
+  }
+  std::vector<int> levu(nn, 0);
+  int maxu = 0;
+  for (int n = nn - 1; n >= 0; n--) {
+    int l = 0;
+    for (int q = L.nbr_ptr[n]; q < L.nbr_ptr[n + 1]; q++) {
+      const int m = L.nbr_node[q];
+      if (m > n) l = std::max(l, levu[m] + 1);
+    }
+    levu[n] = l;
+    maxu = std::max(maxu, l);
+  }
+  S.up_ptr.assign(maxu + 2, 0);
+  for (int n = 0; n < nn; n++) S.up_ptr[levu[n] + 1]++;
+  for (int l = 0; l <= maxu; l++) S.up_ptr[l + 1] += S.up_ptr[l];
+  S.up_nodes.resize(nn);
+  {
+    std::vector<int> fill(maxu + 1, 0);
+    for (int n = 0; n < nn; n++) S.up_nodes[S.up_ptr[levu[n]] + fill[levu[n]]++] = n;
+  }
+}
+
+// ------------------------------------------------------------ Solver
+
+Solver::~Solver() {
+  if (prec64) cudaGraphExecDestroy(prec64);
+  if (prec32) cudaGraphExecDestroy(prec32);
+  void *p[] = {d_lu, d_lu32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work,
+               d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
+  for (void *q : p)
+    if (q) cudaFree(q);
+  if (h_work) cudaFreeHost(h_work);
+}
+
+#define GB_CU(call, what)                          \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+int Solver::init(Context *c, int krylov) {
+  C = c;
+  N = c->L.N;
+  nnz = c->L.nnz;
+  max_krylov = krylov;
+  const Layout &L = c->L;
+  std::vector<int64_t> diag(N);
+  for (int i = 0; i < N; i++) {
+    auto b = L.colidx.begin() + L.rowptr[i], e = L.colidx.begin() + L.rowptr[i + 1];
+    auto it = std::lower_bound(b, e, i);
+    diag[i] = (int64_t)(it - L.colidx.begin());
+  }
+  IluSchedule S;
+  build_ilu_schedule(L, S);
+  lo_ptr = S.lo_ptr;
+  up_ptr = S.up_ptr;
+  GB_CU(cudaMalloc(&d_diag, sizeof(int64_t) * N), "diag");
+  GB_CU(cudaMemcpy(d_diag, diag.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice), "diag");
+  GB_CU(cudaMalloc(&d_lo_nodes, sizeof(int) * S.lo_nodes.size()), "sched");
+  GB_CU(cudaMemcpy(d_lo_nodes, S.lo_nodes.data(), sizeof(int) * S.lo_nodes.size(),
+                   cudaMemcpyHostToDevice), "sched");
+  GB_CU(cudaMalloc(&d_up_nodes, sizeof(int) * S.up_nodes.size()), "sched");
+  GB_CU(cudaMemcpy(d_up_nodes, S.up_nodes.data(), sizeof(int) * S.up_nodes.size(),
+                   cudaMemcpyHostToDevice), "sched");
+  d_fu = c->d_fu;
+  GB_CU(cudaMalloc(&d_lu, sizeof(double) * nnz), "ILU factors");
+  GB_CU(cudaMalloc(&d_scale, sizeof(double) * N), "scale");
+  const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kRedBlocks + 4 * (krylov + 2) + 64);
+  GB_CU(cudaMalloc(&d_work, sizeof(double) * wk), "work");
+  GB_CU(cudaMallocHost(&h_work, sizeof(double) * 4 * (krylov + 2) + 64 * sizeof(double)), "host");
+  GB_CU(cudaMalloc(&d_V, sizeof(double) * (size_t)(krylov + 1) * N), "Krylov basis");
+  GB_CU(cudaMalloc(&d_t, sizeof(double) * N), "t");
+  GB_CU(cudaMalloc(&d_w, sizeof(double) * N), "w");
+  GB_CU(cudaMalloc(&d_r, sizeof(double) * N), "r");
+  GB_CU(cudaMalloc(&d_xs, sizeof(double) * N), "xs");
+  return 0;
+}
+
+static int lanes_per_row(const Layout &L) {
+  const double avg = (double)L.nnz / std::max(1, L.N);
+  return avg >= 192 ? 32 : (avg >= 48 ? 16 : 8);
+}
+
+template <class T>
+static cudaError_t spmv(const Context *C, int lpr, const T *vals, const T *x, T *y, cudaStream_t st) {
+  const int N = C->L.N, threads = 256;
+  const int blocks = (int)(((int64_t)N * lpr + threads - 1) / threads);
+  switch (lpr) {
+  case 32: spmv_kernel<T, 32><<<blocks, threads, 0, st>>>(N, C->d_rowptr, C->d_colidx, vals, x, y); break;
+  case 16: spmv_kernel<T, 16><<<blocks, threads, 0, st>>>(N, C->d_rowptr, C->d_colidx, vals, x, y); break;
+  default: spmv_kernel<T, 8><<<blocks, threads, 0, st>>>(N, C->d_rowptr, C->d_colidx, vals, x, y);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, cudaGraphExec_t *out) {
+  const Context *C = S->C;
+  cudaGraph_t g;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  for (size_t l = 0; l + 1 < S->lo_ptr.size(); l++) {
+    const int cnt = S->lo_ptr[l + 1] - S->lo_ptr[l];
+    lsolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
+        S->d_lo_nodes + S->lo_ptr[l], cnt, C->d_fu, C->d_rowptr, C->d_colidx, S->d_diag, lu, z);
+  }
+  for (size_t l = 0; l + 1 < S->up_ptr.size(); l++) {
+    const int cnt = S->up_ptr[l + 1] - S->up_ptr[l];
+    usolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
+        S->d_up_nodes + S->up_ptr[l], cnt, C->d_fu, C->d_rowptr, C->d_colidx, S->d_diag, lu, z);
+  }
+  e = cudaStreamEndCapture(st, &g);
+  if (e != cudaSuccess) return e;
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
+  d_A = vals;
+  GB_CU(cudaMemcpyAsync(d_lu, vals, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st), "lu copy");
+  for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
+    const int cnt = lo_ptr[l + 1] - lo_ptr[l];
+    ilu0_level_kernel<<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
+        d_lo_nodes + lo_ptr[l], cnt, d_fu, C->d_rowptr, C->d_colidx, d_diag, d_lu);
+  }
+  GB_CU(cudaGetLastError(), "ILU(0) factorisation");
+  if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");
+  if (fp32) {
+    if (!d_lu32) {
+      GB_CU(cudaMalloc(&d_lu32, sizeof(float) * nnz), "ILU32");
+      GB_CU(cudaMalloc(&d_a32, sizeof(float) * nnz), "A32");
+      GB_CU(cudaMalloc(&d_V32, sizeof(float) * (size_t)(max_krylov + 1) * N), "V32");
+      GB_CU(cudaMalloc(&d_t32, sizeof(float) * N), "t32");
+      GB_CU(cudaMalloc(&d_w32, sizeof(float) * N), "w32");
+    }
+    to_f32_kernel<<<1216, 256, 0, st>>>(nnz, d_lu, d_lu32);
+    to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
+    GB_CU(cudaGetLastError(), "FP32 copies");
+    if (!prec32) GB_CU(capture_prec<float>(this, d_lu32, d_t32, st, &prec32), "ILU32 graph");
+  }
+  return 0;
+}
+
+int Solver::apply_prec64(cudaStream_t st) {
+  GB_CU(cudaGraphLaunch(prec64, st), "ILU apply");
+  return 0;
+}
+int Solver::apply_prec32(cudaStream_t st) {
+  GB_CU(cudaGraphLaunch(prec32, st), "ILU32 apply");
+  return 0;
+}
+
+// ------------------------------------------------------------ helpers
+
+int device_norms(Context *C, const double *x, int n, double out3[3], cudaStream_t st) {
+  Solver &S = *C->solver;
+  norms_partial_kernel<double><<<kRedBlocks, kRedThreads, 0, st>>>(n, x, S.d_work);
+  norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, S.d_work, S.d_work + kRedBlocks * 3);
+  GB_CU(cudaGetLastError(), "norms");
+  GB_CU(cudaMemcpyAsync(S.h_work, S.d_work + kRedBlocks * 3, 3 * sizeof(double),
+                        cudaMemcpyDeviceToHost, st), "norms copy");
+  GB_CU(cudaStreamSynchronize(st), "norms sync");
+  memcpy(out3, S.h_work, 3 * sizeof(double));
+  return 0;
+}
+
+int row_sum_scale(Context *C, double *vals, double *R, cudaStream_t st) {
+  Solver &S = *C->solver;
+  const int N = C->L.N;
+  int *zr = (int *)(S.d_work + kRedBlocks * 3 + 8);
+  GB_CU(cudaMemsetAsync(zr, 0, sizeof(int), st), "scale");
+  row_sum_scale_kernel<<<(int)(((int64_t)N * 32 + 255) / 256), 256, 0, st>>>(
+      N, C->d_rowptr, S.d_diag, vals, R, S.d_scale, zr);
+  GB_CU(cudaGetLastError(), "row sum scaling");
+  return 0;
+}
+
+// GMRES(m), right preconditioned.  T = double: FP64 throughout; T = float:
+// FP32 matrix, factors and vectors (sums in FP64).  Solves A x = b with b,
+// x of type T on the device, x = 0 on entry; stops when the preconditioned
+// system's true residual <= tol * ||b|| or after maxit iterations.
+template <class T>
+static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int *its,
+                 double *relres, cudaStream_t st) {
+  Solver &S = *C->solver;
+  const Layout &L = C->L;
+  const int N = L.N, lpr = lanes_per_row(L);
+  const bool f32 = sizeof(T) == 4;
+  T *V = f32 ? (T *)S.d_V32 : (T *)S.d_V;
+  T *t = f32 ? (T *)S.d_t32 : (T *)S.d_t;
+  T *w = f32 ? (T *)S.d_w32 : (T *)S.d_w;
+  const T *A = f32 ? (const T *)S.d_a32 : (const T *)S.d_A;
+  const int64_t ld = N;
+  double *dred = S.d_work;                           // partials
+  double *dh = S.d_work + kRedBlocks * 3 + 16;       // (m+2) results
+  double *dpart = dh + (m + 2) * 2;                  // (m+2) * kRedBlocks
+  double *hh = S.h_work;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
+  auto norm = [&](const T *v, double *out) -> int {
+    norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, v, dred);
+    norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, dred, dh);
+    GB_CU(cudaMemcpyAsync(hh, dh, sizeof(double), cudaMemcpyDeviceToHost, st), "norm");
+    GB_CU(cudaStreamSynchronize(st), "norm sync");
+    *out = hh[0];
+    return 0;
+  };
+  GB_CU(cudaMemsetAsync(x, 0, sizeof(T) * N, st), "x0");
+  double bnorm;
+  if (norm(b, &bnorm)) return -1;
+  *its = 0;
+  *relres = 0.0;
+  if (bnorm == 0.0) return 0;
+  // r = b (x = 0)
+  GB_CU(cudaMemcpyAsync(V, b, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "r0");
+  double beta = bnorm;
+  int total = 0;
+  while (true) {
+    // V0 = r / beta (dh[0] = beta)
+    hh[0] = beta;
+    GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double), cudaMemcpyHostToDevice, st), "beta");
+    scale_copy_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, V, dh, V);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    bool done = false;
+    for (; j < m && total < maxit; j++) {
+      GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
+      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      GB_CU(spmv<T>(C, lpr, A, t, w, st), "spmv");
+      // CGS2
+      std::vector<double> hcol(j + 2, 0.0);
+      for (int pass = 0; pass < 2; pass++) {
+        multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
+        multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh);
+        gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh, w);
+        GB_CU(cudaMemcpyAsync(hh, dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, st), "h");
+        GB_CU(cudaStreamSynchronize(st), "h sync");
+        for (int i = 0; i <= j; i++) hcol[i] += hh[i];
+      }
+      double hn;
+      if (norm(w, &hn)) return -1;
+      hcol[j + 1] = hn;
+      total++;
+      if (hn > 0.0) {
+        hh[0] = hn;
+        GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double), cudaMemcpyHostToDevice, st), "hn");
+        scale_copy_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dh, V + (j + 1) * ld);
+      }
+      // Givens
+      for (int i = 0; i < j; i++) {
+        const double a = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+        hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+        hcol[i] = a;
+      }
+      const double den = std::hypot(hcol[j], hcol[j + 1]);
+      cs[j] = den == 0.0 ? 1.0 : hcol[j] / den;
+      sn[j] = den == 0.0 ? 0.0 : hcol[j + 1] / den;
+      hcol[j] = den;
+      hcol[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = hcol[i];
+      if (std::fabs(g[j + 1]) <= tol * bnorm || hn == 0.0) {
+        j++;
+        done = true;
+        break;
+      }
+    }
+    // y = H^-1 g, x += M^-1 V y
+    for (int i = j - 1; i >= 0; i--) {
+      double sum = g[i];
+      for (int k = i + 1; k < j; k++) sum -= H[(size_t)i * m + k] * y[k];
+      y[i] = H[(size_t)i * m + i] != 0.0 ? sum / H[(size_t)i * m + i] : 0.0;
+    }
+    memcpy(hh, y.data(), sizeof(double) * j);
+    GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double) * j, cudaMemcpyHostToDevice, st), "y");
+    gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, V, ld, dh, t);
+    if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+    add_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, t, x);
+    // true residual r = b - A x into V0
+    GB_CU(spmv<T>(C, lpr, A, x, V, st), "spmv");
+    sub_from_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, b, V);
+    if (norm(V, &beta)) return -1;
+    *its = total;
+    *relres = beta / bnorm;
+    if (beta <= tol * bnorm || total >= maxit || (done && beta <= 10 * tol * bnorm)) break;
+  }
+  return 0;
+}
+
+// Solves the scaled system A dx = R (both on the device, A = d_vals_scaled
+// after factorisation).  FP64: GMRES in FP64.  FP32 refined: FP32 GMRES on
+// the normalised residual inside FP64 iterative refinement.
+int linear_solve(Context *C, const double *R, double *dx, const LinearOpts &o, LinearStats *s,
+                 cudaStream_t st) {
+  Solver &S = *C->solver;
+  const int N = C->L.N;
+  s->iterations = 0;
+  s->refinements = 0;
+  if (!o.fp32_inner) {
+    int its;
+    double rr;
+    if (gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st)) return -1;
+    s->iterations = its;
+    s->relres = rr;
+    return 0;
+  }
+  // iterative refinement: dx = 0, r = R
+  const int lpr = lanes_per_row(C->L);
+  GB_CU(cudaMemsetAsync(dx, 0, sizeof(double) * N, st), "dx0");
+  GB_CU(cudaMemcpyAsync(S.d_r, R, sizeof(double) * N, cudaMemcpyDeviceToDevice, st), "r0");
+  double n3[3];
+  if (device_norms(C, R, N, n3, st)) return -1;
+  const double bnorm = n3[0];
+  s->relres = 0.0;
+  if (bnorm == 0.0) return 0;
+  double rn = bnorm;
+  // scratch: d_xs (N doubles) holds the FP32 right-hand side and solution
+  float *r32 = (float *)S.d_xs;
+  for (int it = 0; it < o.max_refinements; it++) {
+    to_f32_scaled_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, S.d_r, rn, r32);
+    int its;
+    double rr;
+    float *sol32 = (float *)S.d_xs + N;
+    if (gmres<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr, st)) return -1;
+    s->iterations += its;
+    s->refinements++;
+    axpy_f32_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, rn, sol32, dx);
+    // r = R - A dx (FP64)
+    GB_CU(spmv<double>(C, lpr, S.d_A, dx, S.d_r, st), "spmv64");
+    residual_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, R, S.d_r);
+    if (device_norms(C, S.d_r, N, n3, st)) return -1;
+    rn = n3[0];
+    s->relres = rn / bnorm;
+    if (rn <= o.tol * bnorm) break;
+  }
+  return 0;
+}
+
+}  // namespace gb

@@ -1,0 +1,72 @@
+// Krylov solve on the device: row-sum scaling, norms, CSR SpMV, ILU(0)
+// (node-level schedule), GMRES(m) in FP64 or FP32-inside-FP64-refinement.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "gb_layout.h"
+
+namespace gb {
+
+struct Context;
+
+// Host-built schedule of the ILU(0) factorisation and triangular solves:
+// nodes grouped by level; all unknowns of one node are handled by one warp
+// in order, so a level only waits for the levels before it.
+struct IluSchedule {
+  std::vector<int> lo_nodes, lo_ptr;  // forward (L) levels
+  std::vector<int> up_nodes, up_ptr;  // backward (U) levels
+};
+void build_ilu_schedule(const Layout &L, IluSchedule &S);
+
+struct Solver {
+  Context *C = nullptr;
+  int N = 0;
+  int64_t nnz = 0;
+  // ILU(0) factors (same pattern as A): FP64 and FP32 copies
+  double *d_lu = nullptr;
+  float *d_lu32 = nullptr;
+  float *d_a32 = nullptr;       // FP32 copy of the scaled matrix
+  int64_t *d_diag = nullptr;    // position of the diagonal in every row
+  int *d_fu = nullptr;          // first unknown per node (shared with C)
+  int *d_lo_nodes = nullptr, *d_up_nodes = nullptr;
+  std::vector<int> lo_ptr, up_ptr;
+  const double *d_A = nullptr;  // scaled FP64 matrix the factors were built from
+  double *d_scale = nullptr;
+  double *d_work = nullptr;     // reduction scratch
+  double *h_work = nullptr;     // pinned host mirror
+  int max_krylov = 0;
+  double *d_V = nullptr;        // (m+1) x N Krylov basis (FP64)
+  float *d_V32 = nullptr;       // (m+1) x N Krylov basis (FP32)
+  double *d_t = nullptr, *d_w = nullptr, *d_r = nullptr, *d_xs = nullptr;
+  float *d_t32 = nullptr, *d_w32 = nullptr;
+  cudaGraphExec_t prec64 = nullptr, prec32 = nullptr;  // captured ILU solves on d_t / d_t32
+  ~Solver();
+  int init(Context *c, int krylov);
+  int factor(const double *vals, bool fp32, cudaStream_t st);
+  int apply_prec64(cudaStream_t st);  // in place on d_t
+  int apply_prec32(cudaStream_t st);  // in place on d_t32
+};
+
+struct LinearOpts {
+  int krylov = 30;          // "Size of Krylov subspace"
+  int maxit = 500;          // "Maximum Linear Solve Iterations"
+  double tol = 1e-6;        // "Linear Solver Tolerance" (relative residual)
+  bool fp32_inner = false;  // FP32 GMRES inside FP64 iterative refinement
+  double inner_tol = 1e-3;  // FP32 inner relative tolerance
+  int max_refinements = 20;
+};
+struct LinearStats {
+  int iterations = 0;
+  int refinements = 0;
+  double relres = 0.0;
+};
+
+int device_norms(Context *C, const double *x, int n, double out3[3], cudaStream_t st);
+int row_sum_scale(Context *C, double *vals, double *R, cudaStream_t st);
+int linear_solve(Context *C, const double *R, double *dx, const LinearOpts &o, LinearStats *s,
+                 cudaStream_t st);
+
+}  // namespace gb

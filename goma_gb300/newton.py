@@ -100,7 +100,60 @@ class GomaNewton:
     def status(self):
         _lib.check(self._L.gb_status(self.h))
 
+    # --- solve_nonlinear_problem
+    def newton_opts(self, **kw):
+        o = _lib.NewtonOpts()
+        self._L.gb_newton_opts_default(ctypes.byref(o))
+        for k, v in kw.items():
+            if k == "fp32_inner":
+                o.linear_precision = 1 if v else 0
+            else:
+                setattr(o, k, v)
+        return o
+
+    def solve_nonlinear_problem(self, x0=None, **opts):
+        """Newton from x0 (host; Dirichlet values applied if x0 is None) to
+        the scaled-residual tolerance.  Returns (x, converged, stats dict)."""
+        x = self.dirichlet_init(np.zeros(self.N)) if x0 is None else np.ascontiguousarray(
+            x0, np.float64).copy()
+        o = self.newton_opts(**opts)
+        conv = ctypes.c_int()
+        st = _lib.NewtonStats()
+        _lib.check(self._L.gb_solve_nonlinear_problem(self.h, _dp(x), ctypes.byref(o),
+                                                      ctypes.byref(conv), ctypes.byref(st)))
+        return x, bool(conv.value), _stats_dict(st)
+
+    def solve_nonlinear_problem_device(self, d_x, **opts):
+        o = self.newton_opts(**opts)
+        conv = ctypes.c_int()
+        st = _lib.NewtonStats()
+        _lib.check(self._L.gb_solve_nonlinear_problem_device(self.h, d_x, ctypes.byref(o),
+                                                             ctypes.byref(conv),
+                                                             ctypes.byref(st)))
+        return bool(conv.value), _stats_dict(st)
+
+    def linear_solve(self, a_msr, rhs, **opts):
+        """Host MSR (row-scaled) matrix and right-hand side -> dx."""
+        a_msr = np.ascontiguousarray(a_msr, np.float64)
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        dx = np.empty(self.N)
+        o = self.newton_opts(**opts)
+        its = ctypes.c_int()
+        rr = ctypes.c_double()
+        _lib.check(self._L.gb_linear_solve(self.h, _dp(a_msr), _dp(rhs), _dp(dx), ctypes.byref(o),
+                                           ctypes.byref(its), ctypes.byref(rr)))
+        return dx, its.value, rr.value
+
     def csr_to_msr(self, d_vals):
         a = np.empty(self.msr_len)
         _lib.check(self._L.gb_csr_to_msr_host(self.h, d_vals, _dp(a)))
         return a
+
+
+def _stats_dict(st):
+    n = st.newton_its
+    return {"newton_its": n, "linear_its": st.linear_its, "refinements": st.refinements,
+            "residual_l2": [st.residual_l2[i] for i in range(min(n + 1, 64))],
+            "residual_loo": st.residual_loo, "assemble_ms": st.assemble_ms,
+            "scale_ms": st.scale_ms, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
+            "total_ms": st.total_ms}

@@ -89,6 +89,68 @@ void *gb_stream(gb_ctx *ctx);
  * (gb_msr_length() doubles). */
 int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
 
+/* ---------------------------------------------------------- Newton solve */
+
+#define GB_LINEAR_FP64 0
+#define GB_LINEAR_FP32_REFINED 1
+
+/* Solver cards of the input deck (src/mm_input.c rd_solver_specs). */
+typedef struct gb_newton_opts {
+  int max_newton;          /* "Number of Newton Iterations" */
+  double residual_tol;     /* "Normalized Residual Tolerance" (Epsilon[0]) */
+  double damping;          /* "Newton correction factor" */
+  int krylov_dim;          /* "Size of Krylov subspace" (AztecOO default 30) */
+  int max_linear_its;      /* "Maximum Linear Solve Iterations" */
+  double linear_tol;       /* "Linear Solver Tolerance" (relative residual) */
+  int linear_precision;    /* GB_LINEAR_FP64 or GB_LINEAR_FP32_REFINED */
+  double inner_tol;        /* FP32 inner GMRES tolerance (refined mode) */
+  int max_refinements;     /* FP64 refinement steps (refined mode) */
+  int verbose;             /* 1: one line per Newton step on stdout */
+} gb_newton_opts;
+
+typedef struct gb_newton_stats {
+  int newton_its;          /* Newton steps taken (assemblies - 1 on convergence) */
+  int linear_its;          /* Krylov iterations, all steps */
+  int refinements;         /* FP64 refinement steps, all steps */
+  double residual_l2[64];  /* scaled-residual L2 norm per Newton step */
+  double residual_loo;     /* final scaled-residual L-infinity norm */
+  double assemble_ms, scale_ms, factor_ms, solve_ms, total_ms;
+} gb_newton_stats;
+
+void gb_newton_opts_default(gb_newton_opts *o);
+
+/* Drop-in for solve_nonlinear_problem (src/mm_sol_nonlinear.c:596), steady
+ * case: Newton from x (host, N doubles, Dirichlet values already set as
+ * find_and_set_Dirichlet leaves them) until the row-sum-scaled residual
+ * has L2 and L-infinity norms below residual_tol after at least one update
+ * (:1482-1486).  Each step: matrix_fill_full, row_sum_scaling_scale
+ * (src/sl_matrix_util.c:441), ILU(0)-GMRES (the AztecOO case, :1805),
+ * x -= damping * dx (:2553).  x is overwritten with the last iterate;
+ * *converged is 1 or 0.  Returns -1 on a non-positive Jacobian
+ * determinant, a non-finite residual, or a CUDA error. */
+int gb_solve_nonlinear_problem(gb_ctx *ctx, double *x, const gb_newton_opts *opts,
+                               int *converged, gb_newton_stats *stats);
+/* Same with x in device memory (N doubles); the iterate stays there. */
+int gb_solve_nonlinear_problem_device(gb_ctx *ctx, double *d_x, const gb_newton_opts *opts,
+                                      int *converged, gb_newton_stats *stats);
+
+/* row_sum_scaling_scale (src/sl_matrix_util.c:441) on device CSR values
+ * and residual of this context: scale[i] = sign(a_ii) sum_j |a_ij|, A and R
+ * divided by it.  d_scale (N doubles) may be NULL. */
+int gb_row_sum_scale_device(gb_ctx *ctx, double *d_vals, double *d_R, double *d_scale);
+
+/* The Krylov solve of one Newton step (the Linear_Solver switch,
+ * src/mm_sol_nonlinear.c:1624): factor ILU(0) of the scaled matrix
+ * d_vals (device CSR values) and solve A dx = rhs by GMRES.  Device arrays. */
+int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rhs, double *d_dx,
+                           const gb_newton_opts *opts, int *iterations, double *relres);
+/* Host form taking the reference's MSR values (gb_msr_length() doubles,
+ * already row-scaled as the reference does before AZ_solve) and host
+ * vectors; the drop-in for aztecoo_solve_epetra
+ * (src/sl_aztecoo_interface.cpp:56). */
+int gb_linear_solve(gb_ctx *ctx, const double *a_msr, const double *rhs, double *dx,
+                    const gb_newton_opts *opts, int *iterations, double *relres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,58 @@
+"""GPU Newton (assembly + row-sum scaling + ILU(0)-GMRES, FP64 and FP32
+refined) against the reference's converged solutions: fields within 1e-8
+relative of the reference's FP64 Newton solution."""
+import numpy as np
+import pytest
+
+import oracle
+from goma_gb300 import problem as pb
+from goma_gb300.newton import GomaNewton
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+TOL_X = 1e-8
+
+
+@pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
+@pytest.mark.parametrize("name", gc.names("solve"))
+def test_gpu_newton_matches_reference_solution(name, fp32_inner):
+    g, case = gc.load(name)
+    gn = GomaNewton(gc.problem_from_case(case))
+    x, conv, st = gn.solve_nonlinear_problem(residual_tol=1e-11, linear_tol=1e-10,
+                                             fp32_inner=fp32_inner, max_newton=30)
+    assert conv, st
+    xc = g["x_converged"]
+    assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
+
+
+def test_gpu_linear_solve_drop_in():
+    """gb_linear_solve on the reference-scaled MSR system matches a direct
+    solve of the same system (oracle band LU via one Newton correction)."""
+    prob = pb.lid_cavity_2d(6, 100.0)
+    o = oracle.Oracle(prob)
+    gn = GomaNewton(prob)
+    x = o.dirichlet_init(np.random.default_rng(0).uniform(-0.5, 0.5, o.N))
+    R, a, _ = o.matrix_fill(x)
+    a_s, R_s, _ = o.row_sum_scale(a, R)
+    dx, its, rr = gn.linear_solve(a_s, R_s, linear_tol=1e-12, max_linear_its=2000)
+    assert rr <= 1e-12
+    # residual of the scaled system
+    ija = o.ija()
+    N = o.N
+    Ax = a_s[:N] * dx
+    for i in range(N):
+        Ax[i] += np.dot(a_s[ija[i]:ija[i + 1]], dx[ija[ija[i]:ija[i + 1]]])
+    assert np.abs(Ax - R_s).max() <= 1e-9 * np.abs(R_s).max()
+
+
+def test_gpu_newton_larger_cavity_against_oracle():
+    prob = pb.lid_cavity_2d(16, 100.0)
+    o = oracle.Oracle(prob)
+    xo, it, _ = o.newton(o.dirichlet_init(np.zeros(o.N)), 30, 1e-11)
+    assert it > 0
+    gn = GomaNewton(prob)
+    for fp32 in (False, True):
+        x, conv, st = gn.solve_nonlinear_problem(residual_tol=1e-11, linear_tol=1e-10,
+                                                 fp32_inner=fp32)
+        assert conv
+        assert np.abs(x - xo).max() <= TOL_X * np.abs(xo).max()
