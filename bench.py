@@ -1,0 +1,310 @@
+"""Benchmark of the Q2/P1 Newton hot path on one GB300.
+
+Workload: 3-D Boussinesq natural convection in a unit cube, 32^3 HEX27
+elements, Q2 velocity + temperature / P1 pressure (1,229,572 unknowns,
+300,429,328 CSR nonzeros), the configuration the headline metric is quoted
+on.  A step is one full residual + analytic-Jacobian assembly
+(matrix_fill_full): zeroing, the element kernels and the coloured CSR
+scatter, at a seeded synthetic state.
+
+  value  elements/s with x, R and the matrix resident in HBM
+  e2e    elements/s through the C ABI with host buffers: x copied in, R and
+         the Jacobian (reference MSR layout) copied out, every step
+  roofline  the element kernel: algorithmic FP64 flops per launch
+         (2 Q n_loc^2 (d+1) per element) / measured kernel time, against
+         this GPU's FP64 tensor-pipe (DMMA) throughput measured in-process;
+         HBM view of the same launch alongside
+  cpu_baseline  the CPU oracle (a restatement of the reference's
+         matrix_fill) on an 8^3-element block of the same problem
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Q2/P1 elem/s (R+J); time-to-solve @1e-8, plain vs learned+FP32 GMRES, 1 GB300"
+UNIT = "elements/s"
+NEL = 32
+RA, PR = 1e5, 0.71
+
+
+def workload_config(nel):
+    return {"workload": "3-D Boussinesq cube %d^3 HEX27 Q2/P1 NS+energy, Ra=1e5 Pr=0.71" % nel,
+            "elements": nel ** 3, "element": "HEX27", "fields": "u,v,w,T (Q2), P (P1)",
+            "state": "seeded uniform(-1,1) unknowns", "assembly": "R + analytic J, FP64",
+            "l2": "inputs larger than L2 (CSR values 2.4 GB)"}
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            p = [s.strip() for s in line.split(",")]
+            if len(p) == 7:
+                self.rows.append(p)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
+    """The CPU oracle's matrix_fill on an nel_block^3 block of the same
+    problem; elements/s over `threads` threads (disjoint element ranges,
+    private output arrays)."""
+    import concurrent.futures
+
+    import oracle
+    from goma_gb300 import problem as pb
+    prob = pb.boussinesq_cube_3d(nel_block, RA, PR)
+    o = oracle.Oracle(prob)
+    x = np.random.default_rng(7).uniform(-1, 1, o.N)
+    ne = prob.mesh.num_elems
+    # time one element first to size the sample to the budget
+    t = time.perf_counter()
+    o.matrix_fill(x, True, 0, 1)
+    per = max(time.perf_counter() - t, 1e-6)
+    n = int(min(ne, max(threads, budget_s / per)))
+    chunks = np.array_split(np.arange(n), threads)
+
+    def work(c):
+        R = np.zeros(o.N)
+        a = np.zeros(o.msr_len)
+        lib = oracle.lib()
+        P = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        lib.orc_matrix_fill(o.h, P(x), P(R), P(a), int(c[0]), int(c[-1]) + 1)
+        return len(c)
+
+    t = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
+        done = sum(ex.map(work, [c for c in chunks if len(c)]))
+    dt = time.perf_counter() - t
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "CPU oracle matrix_fill (restatement of the reference's), %d elements of an "
+                      "%d^3-element block of the same HEX27 Boussinesq problem, %.1f s"
+                      % (done, nel_block, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path.  The reference C compiles
+    only where its source tree is (oracle/_ref, not on the GPU machine), so
+    the oracle port stands in, on all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(8, threads, budget_s=2.0)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(8, threads, budget_s=max(60.0 / max(args.steps, 1), 5.0)))
+    v = float(np.median([c["value"] for c in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * NEL ** 3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(NEL), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--nel", type=int, default=NEL)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from goma_gb300 import _lib
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    warm = max(args.warmup, 3)
+    nel = args.nel
+
+    prob = pb.boussinesq_cube_3d(nel, RA, PR)
+    gn = GomaNewton(prob)
+    L = gn._L
+    N, nnz, msr_len = gn.N, gn.nnz, gn.msr_len
+    x_host = gn.dirichlet_init(np.random.default_rng(11).uniform(-1.0, 1.0, N))
+    dx = torch.tensor(x_host, dtype=torch.float64, device="cuda")
+    dR = torch.empty(N, dtype=torch.float64, device="cuda")
+    dv = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        gn.matrix_fill_full_device(dx.data_ptr(), dR.data_ptr(), dv.data_ptr(), sp)
+
+    for _ in range(warm):
+        step()
+    torch.cuda.synchronize()
+    gn.status()
+
+    # ---- value: device-resident
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler() as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    gn.status()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    elems = prob.mesh.num_elems
+    value = world * elems / (ms * 1e-3)
+
+    # ---- e2e: host buffers through the C ABI (x in, R + MSR Jacobian out)
+    xh = torch.from_numpy(x_host).pin_memory()
+    Rh = torch.empty(N, dtype=torch.float64).pin_memory()
+    ah = torch.empty(msr_len, dtype=torch.float64).pin_memory()
+    P = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_double))  # noqa: E731
+
+    def e2e_step():
+        _lib.check(L.gb_matrix_fill_full(gn.h, P(xh), P(Rh), P(ah)))
+
+    for _ in range(2):
+        e2e_step()
+    ke = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(ke):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t) * 1e3 / ke
+    e2e = {"value": world * elems / (e2e_ms * 1e-3), "unit": UNIT,
+           "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N + 8 * msr_len,
+           "ms_per_step": e2e_ms,
+           "path": "gb_matrix_fill_full: x host->device, R and MSR Jacobian device->host"}
+
+    # ---- roofline of the element kernel
+    kms = ctypes.c_double()
+    kl = ctypes.c_longlong()
+    _lib.check(L.gb_kernel_timing(gn.h, 1, None, None))
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    _lib.check(L.gb_kernel_timing(gn.h, 0, ctypes.byref(kms), ctypes.byref(kl)))
+    per_launch_ms = kms.value / max(kl.value, 1)
+    elems_per_launch = elems / gn.num_colors
+    nloc = 4 * 27 + 4
+    flop_el = 2.0 * 27 * nloc * nloc * 4
+    achieved_tf = flop_el * elems_per_launch / (per_launch_ms * 1e-3) / 1e12
+    dmma = ctypes.c_double()
+    fma = ctypes.c_double()
+    _lib.check(L.gb_probe_fp64_peaks(ctypes.byref(dmma), ctypes.byref(fma)))
+    peaks = read_peaks()
+    # algorithmic bytes of one launch: its share of the matrix values written,
+    # R, x, connectivity and coordinates
+    nodes = prob.mesh.num_nodes
+    bytes_asm = 8 * nnz + 8 * N + 8 * N + 4 * elems * 27 + 8 * 3 * nodes
+    bytes_launch = bytes_asm / gn.num_colors
+    hbm_gbs = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+    roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": dmma.value,
+                "unit": "TFLOP/s", "frac": achieved_tf / dmma.value,
+                "traffic": None,
+                "kernel": "assemble_kernel<3,energy> (one colour, %d elements)" % elems_per_launch,
+                "launch_ms": per_launch_ms,
+                "flop_per_element": flop_el,
+                "peak_source": "FP64 mma.sync m8n8k4 (DMMA) throughput measured in-process on "
+                               "this GPU (MEASURED_PEAKS.json has HBM and bf16 only)",
+                "fp64_fma_peak_tflops": fma.value,
+                "hbm_view": {"achieved_gbs": hbm_gbs, "peak_gbs": peaks.get("hbm_gbs"),
+                             "frac": hbm_gbs / peaks.get("hbm_gbs", 6800.0),
+                             "bytes_per_launch": bytes_launch}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(workload_config(nel), unknowns=N, csr_nnz=nnz,
+                           colors=gn.num_colors, parallelism="replicas"),
+            "clocks": clk.summary(), "e2e": e2e, "roofline": roofline,
+            "gpu_launches": int(gn.num_colors * args.steps)}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(8, 1, budget_s=15.0)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -73,6 +73,8 @@ def load():
         "gb_row_sum_scale_device": (ctypes.c_int, [vp, vp, vp, vp]),
         "gb_linear_solve_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(NewtonOpts), ip,
                                                   dp]),
+        "gb_probe_fp64_peaks": (ctypes.c_int, [dp, dp]),
+        "gb_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int, dp, llp]),
         "gb_linear_solve": (ctypes.c_int, [vp, dp, dp, dp, ctypes.POINTER(NewtonOpts), ip, dp]),
     }
     for name, (res, args) in sig.items():

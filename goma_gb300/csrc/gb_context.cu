@@ -110,6 +110,8 @@ Context::~Context() {
                   d_tab_pt, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (ev_k0) cudaEventDestroy(ev_k0);
+  if (ev_k1) cudaEventDestroy(ev_k1);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -198,11 +200,20 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   if (e != cudaSuccess) return cuda_fail(e, "assembly zeroing");
   AsmArgs a = args(x, R, vals);
   const int ncol = (int)L.color_ptr.size() - 1;
+  if (timing) cudaEventRecord(ev_k0, st);
   for (int c = 0; c < ncol; c++) {
     const int n = L.color_ptr[c + 1] - L.color_ptr[c];
     e = launch_assemble(a, L.dim, L.energy != 0, carreau, vals != nullptr,
                         d_color_elems + L.color_ptr[c], n, st);
     if (e != cudaSuccess) return cuda_fail(e, "assembly launch");
+  }
+  if (timing) {
+    cudaEventRecord(ev_k1, st);
+    cudaEventSynchronize(ev_k1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev_k0, ev_k1);
+    kernel_ms += ms;
+    kernel_launches += ncol;
   }
   return 0;
 }
@@ -342,6 +353,21 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
   if (d_vals) *d_vals = ctx->c.d_vals;
   if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
   if (d_colidx) *d_colidx = ctx->c.d_colidx;
+  return 0;
+}
+
+int gb_kernel_timing(gb_ctx *ctx, int enable, double *kernel_ms, long long *launches) {
+  if (!ctx) return fail("NULL argument");
+  Context &c = ctx->c;
+  if (kernel_ms) *kernel_ms = c.kernel_ms;
+  if (launches) *launches = c.kernel_launches;
+  if (enable && !c.ev_k0) {
+    cudaEventCreate(&c.ev_k0);
+    cudaEventCreate(&c.ev_k1);
+  }
+  c.timing = enable != 0;
+  c.kernel_ms = 0.0;
+  c.kernel_launches = 0;
   return 0;
 }
 

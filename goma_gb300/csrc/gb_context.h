@@ -37,6 +37,11 @@ struct Context {
   int *d_status = nullptr;
   double *d_msr = nullptr;
   std::unique_ptr<Solver> solver;
+  // optional kernel timing of the element kernels (events on the launch stream)
+  bool timing = false;
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
+  double kernel_ms = 0.0;
+  long kernel_launches = 0;
 
   ~Context();
   int init(const gb_problem_desc *d);

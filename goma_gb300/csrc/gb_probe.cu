@@ -1,0 +1,84 @@
+// FP64 throughput probe: the roofline denominators for the FP64 element
+// kernels (the measured peaks cover HBM and bf16 only).  Two short
+// kernels of independent FP64 work: scalar FMA chains and mma.sync
+// m8n8k4 f64 (DMMA) chains, timed with CUDA events.
+#include <cuda_runtime.h>
+
+#include "../../include/gb_newton.h"
+#include "gb_context.h"
+
+namespace gb {
+
+static constexpr int kProbeIters = 2048;
+
+__global__ void probe_fma64(double *out, double s) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4,
+         a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  for (int i = 0; i < kProbeIters; i++) {
+    a0 = fma(a0, s, 0.5);
+    a1 = fma(a1, s, 0.5);
+    a2 = fma(a2, s, 0.5);
+    a3 = fma(a3, s, 0.5);
+    a4 = fma(a4, s, 0.5);
+    a5 = fma(a5, s, 0.5);
+    a6 = fma(a6, s, 0.5);
+    a7 = fma(a7, s, 0.5);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+__global__ void probe_dmma(double *out, double s) {
+  double a = threadIdx.x * 1e-3, b = s;
+  double c0 = 0, c1 = 0, d0 = 0, d1 = 0, e0 = 0, e1 = 0, f0 = 0, f1 = 0;
+  for (int i = 0; i < kProbeIters / 4; i++) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(c0), "+d"(c1) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(d0), "+d"(d1) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(e0), "+d"(e1) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(f0), "+d"(f1) : "d"(a), "d"(b));
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + d0 + d1 + e0 + e1 + f0 + f1;
+}
+
+}  // namespace gb
+
+extern "C" int gb_probe_fp64_peaks(double *dmma_tflops, double *fma_tflops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256;
+  double *out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double) * blocks * threads);
+  if (e != cudaSuccess) return gb::cuda_fail(e, "probe buffer");
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  float best_f = 1e30f, best_d = 1e30f, ms;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(t0);
+    gb::probe_fma64<<<blocks, threads>>>(out, 0.999);
+    cudaEventRecord(t1);
+    cudaEventSynchronize(t1);
+    cudaEventElapsedTime(&ms, t0, t1);
+    best_f = ms < best_f ? ms : best_f;
+    cudaEventRecord(t0);
+    gb::probe_dmma<<<blocks, threads>>>(out, 0.999);
+    cudaEventRecord(t1);
+    cudaEventSynchronize(t1);
+    cudaEventElapsedTime(&ms, t0, t1);
+    best_d = ms < best_d ? ms : best_d;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(out);
+  if (e != cudaSuccess) return gb::cuda_fail(e, "probe");
+  const double fma_flops = 2.0 * 8 * gb::kProbeIters * (double)blocks * threads;
+  const double mma_flops = 512.0 * gb::kProbeIters * (double)blocks * (threads / 32);
+  if (fma_tflops) *fma_tflops = fma_flops / (best_f * 1e-3) / 1e12;
+  if (dmma_tflops) *dmma_tflops = mma_flops / (best_d * 1e-3) / 1e12;
+  return 0;
+}

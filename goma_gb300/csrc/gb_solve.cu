@@ -247,11 +247,15 @@ __device__ __forceinline__ int64_t find_col(const int *__restrict__ colidx, int6
 }
 
 // ILU(0) of the rows of the nodes of one level (IKJ order inside a row; the
-// rows of a node in increasing order), one warp per node.
+// rows of a node in increasing order), one warp per node.  A pivot smaller
+// than tau in magnitude (the row-scaled matrix has unit row sums) is
+// replaced by +-tau: in the reference's node-major order an element without
+// a pressure datum whose earlier velocity unknowns are all Dirichlet rows
+// leaves an exactly singular pressure pivot.
 __global__ void ilu0_level_kernel(const int *__restrict__ nodes, int count,
                                   const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
                                   const int *__restrict__ colidx, const int64_t *__restrict__ diag,
-                                  double *__restrict__ lu) {
+                                  double *__restrict__ lu, double tau, int *__restrict__ nfix) {
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= count) return;
   const int n = nodes[w];
@@ -270,6 +274,14 @@ __global__ void ilu0_level_kernel(const int *__restrict__ nodes, int count,
       }
       __syncwarp();
     }
+    if (lane == 0) {
+      const double d = lu[di];
+      if (fabs(d) < tau) {
+        lu[di] = d < 0.0 ? -tau : tau;
+        atomicAdd(nfix, 1);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -455,11 +467,13 @@ static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, c
 
 int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   d_A = vals;
+  GB_CU(cudaMemsetAsync(d_work + kRedBlocks * 3 + 10, 0, sizeof(int), st), "pivot count");
   GB_CU(cudaMemcpyAsync(d_lu, vals, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st), "lu copy");
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
     ilu0_level_kernel<<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        d_lo_nodes + lo_ptr[l], cnt, d_fu, C->d_rowptr, C->d_colidx, d_diag, d_lu);
+        d_lo_nodes + lo_ptr[l], cnt, d_fu, C->d_rowptr, C->d_colidx, d_diag, d_lu, pivot_tau,
+        (int *)(d_work + kRedBlocks * 3 + 10));
   }
   GB_CU(cudaGetLastError(), "ILU(0) factorisation");
   if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");

@@ -85,6 +85,12 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
+/* Instrumentation: with enable = 1, every following assembly records CUDA
+ * events around its element-kernel launches (on the launch stream, then
+ * synchronises); a call returns the accumulated kernel time and launch
+ * count since the previous call and sets the new state. */
+int gb_kernel_timing(gb_ctx *ctx, int enable, double *kernel_ms, long long *launches);
+
 /* Converts device CSR values (same ctx) to the MSR layout in host memory
  * (gb_msr_length() doubles). */
 int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
@@ -150,6 +156,11 @@ int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rh
  * (src/sl_aztecoo_interface.cpp:56). */
 int gb_linear_solve(gb_ctx *ctx, const double *a_msr, const double *rhs, double *dx,
                     const gb_newton_opts *opts, int *iterations, double *relres);
+
+/* Measures this GPU's FP64 throughput (TFLOP/s) with two short kernels:
+ * mma.sync m8n8k4 f64 (tensor pipe) and scalar FMA.  The FP64 roofline
+ * denominators of the element kernels. */
+int gb_probe_fp64_peaks(double *dmma_tflops, double *fma_tflops);
 
 #ifdef __cplusplus
 }
