@@ -198,8 +198,12 @@ def main():
     dx = torch.tensor(x_host, dtype=torch.float64, device="cuda")
     dR = torch.empty(N, dtype=torch.float64, device="cuda")
     dv = torch.empty(nnz, dtype=torch.float64, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the library treats a NULL stream as
+    # its own stream, so the timing events and the kernels must share this one
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = stream.cuda_stream
+    assert sp != 0
 
     def step():
         gn.matrix_fill_full_device(dx.data_ptr(), dR.data_ptr(), dv.data_ptr(), sp)
