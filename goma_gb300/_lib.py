@@ -44,6 +44,7 @@ def load():
     L = ctypes.CDLL(LIB_PATH)
     vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
     llp = ctypes.POINTER(ctypes.c_longlong)
+    fp = ctypes.POINTER(ctypes.c_float)
     sig = {
         "gb_create": (ctypes.c_int, [vp, ctypes.POINTER(vp)]),
         "gb_destroy": (None, [vp]),
@@ -74,6 +75,21 @@ def load():
         "gb_linear_solve_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(NewtonOpts), ip,
                                                   dp]),
         "gb_probe_fp64_peaks": (ctypes.c_int, [dp, dp]),
+        "gb_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_ulonglong, ctypes.POINTER(vp)]),
+        "gb_mlp_destroy": (None, [vp]),
+        "gb_mlp_num_params": (ctypes.c_int, [vp]),
+        "gb_mlp_get_params": (ctypes.c_int, [vp, fp]),
+        "gb_mlp_set_params": (ctypes.c_int, [vp, fp]),
+        "gb_mlp_get_grads": (ctypes.c_int, [vp, fp]),
+        "gb_mlp_forward_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+        "gb_mlp_loss_grad_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, fp]),
+        "gb_mlp_adam_step": (ctypes.c_int, [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_float]),
+        "gb_mlp_train_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong,
+                                               fp]),
+        "gb_set_material": (ctypes.c_int, [vp, vp]),
         "gb_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int, dp, llp]),
         "gb_linear_solve": (ctypes.c_int, [vp, dp, dp, dp, ctypes.POINTER(NewtonOpts), ip, dp]),
     }

@@ -106,7 +106,7 @@ __global__ void csr_to_msr_kernel(int N, const int64_t *__restrict__ rowptr,
 
 Context::~Context() {
   void *ptrs[] = {d_coords, d_conn,   d_fu,     d_dbc,     d_dbc_val, d_rowptr, d_colidx,
-                  d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
+                  d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nbr_node, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
                   d_tab_pt, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -115,10 +115,7 @@ Context::~Context() {
   if (stream) cudaStreamDestroy(stream);
 }
 
-int Context::init(const gb_problem_desc *d) {
-  desc = *d;
-  if (build_layout(d, L, g_err) != 0) return -1;
-  const gb_material &m = d->mat;
+int Context::set_material(const gb_material &m) {
   if (m.viscosity_model != GB_VISC_NEWTONIAN && m.viscosity_model != GB_VISC_CARREAU)
     return fail("unsupported viscosity model");
   if (m.momentum_source_model != GB_SOURCE_CONSTANT &&
@@ -138,6 +135,14 @@ int Context::init(const gb_problem_desc *d) {
   mat.beta = m.volume_expansion;
   mat.Tref = m.reference_temperature;
   carreau = m.viscosity_model == GB_VISC_CARREAU;
+  desc.mat = m;
+  return 0;
+}
+
+int Context::init(const gb_problem_desc *d) {
+  desc = *d;
+  if (build_layout(d, L, g_err) != 0) return -1;
+  if (set_material(d->mat)) return -1;
 
   cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
@@ -151,6 +156,7 @@ int Context::init(const gb_problem_desc *d) {
       upload(&d_dbc_val, L.dbc_val, "dbc_val") || upload(&d_rowptr, L.rowptr, "rowptr") ||
       upload(&d_colidx, L.colidx, "colidx") || upload(&d_nbr_ptr, L.nbr_ptr, "nbr_ptr") ||
       upload(&d_nbr_off, L.nbr_off, "nbr_off") || upload(&d_nbr_offT, L.nbr_offT, "nbr_offT") ||
+      upload(&d_nbr_node, L.nbr_node, "nbr_node") ||
       upload(&d_nslot, L.elem_nslot, "elem_nslot") || upload(&d_tab_phi, tphi, "tab") ||
       upload(&d_tab_dphi, tdphi, "tab") || upload(&d_tab_w, tw, "tab") ||
       upload(&d_tab_pt, tpt, "tab") || upload(&d_color_elems, L.color_elems, "colors"))
@@ -354,6 +360,11 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
   if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
   if (d_colidx) *d_colidx = ctx->c.d_colidx;
   return 0;
+}
+
+int gb_set_material(gb_ctx *ctx, const gb_material *mat) {
+  if (!ctx || !mat) return fail("NULL argument");
+  return ctx->c.set_material(*mat);
 }
 
 int gb_kernel_timing(gb_ctx *ctx, int enable, double *kernel_ms, long long *launches) {

@@ -29,7 +29,7 @@ struct Context {
   double *d_dbc_val = nullptr;
   int64_t *d_rowptr = nullptr;
   int *d_colidx = nullptr;
-  int *d_nbr_ptr = nullptr, *d_nbr_off = nullptr, *d_nbr_offT = nullptr;
+  int *d_nbr_ptr = nullptr, *d_nbr_off = nullptr, *d_nbr_offT = nullptr, *d_nbr_node = nullptr;
   uint16_t *d_nslot = nullptr;
   double *d_tab_phi = nullptr, *d_tab_dphi = nullptr, *d_tab_w = nullptr, *d_tab_pt = nullptr;
   int *d_color_elems = nullptr;
@@ -45,6 +45,7 @@ struct Context {
 
   ~Context();
   int init(const gb_problem_desc *d);
+  int set_material(const gb_material &m);
   AsmArgs args(const double *x, double *R, double *vals) const;
   // zero R (and vals), then launch one kernel per colour on st
   int assemble(const double *x, double *R, double *vals, cudaStream_t st);

@@ -246,42 +246,201 @@ __device__ __forceinline__ int64_t find_col(const int *__restrict__ colidx, int6
   return lo;
 }
 
-// ILU(0) of the rows of the nodes of one level (IKJ order inside a row; the
-// rows of a node in increasing order), one warp per node.  A pivot smaller
-// than tau in magnitude (the row-scaled matrix has unit row sums) is
-// replaced by +-tau: in the reference's node-major order an element without
-// a pressure datum whose earlier velocity unknowns are all Dirichlet rows
-// leaves an exactly singular pressure pivot.
-__global__ void ilu0_level_kernel(const int *__restrict__ nodes, int count,
-                                  const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
-                                  const int *__restrict__ colidx, const int64_t *__restrict__ diag,
-                                  double *__restrict__ lu, double tau, int *__restrict__ nfix) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= count) return;
-  const int n = nodes[w];
-  for (int i = fu[n]; i < fu[n + 1]; i++) {
-    const int64_t r0 = rowptr[i], r1 = rowptr[i + 1], di = diag[i];
-    for (int64_t p = r0; p < di; p++) {
-      const int k = colidx[p];
-      const double lik = lu[p] / lu[diag[k]];
-      __syncwarp();
-      if (lane == 0) lu[p] = lik;
-      const int64_t k1 = rowptr[k + 1];
-      for (int64_t q = diag[k] + 1 + lane; q < k1; q += 32) {
-        const int j = colidx[q];
-        const int64_t pos = find_col(colidx, p + 1, r1, j);
-        if (pos < r1 && colidx[pos] == j) lu[pos] = fma(-lik, lu[q], lu[pos]);
-      }
-      __syncwarp();
+// ILU(0) of the rows of one node per CTA, all nodes of one level at once.
+//
+// The pattern is dense in node blocks (every unknown of a node couples with
+// every unknown of every neighbour node; the energy row alone skips pressure
+// columns), so the reference's scalar ILU(0) in node-major order is, block
+// by block: for each lower neighbour node m (ascending)
+//     L_nm   = A_nm U_mm^-1                 (triangular, <= 8 x 8)
+//     A_nq  -= L_nm U_mq   for every q > m neighbouring both n and m
+// then the dense elimination of the node's own diagonal block and the rest
+// of its row.  Fill outside the pattern (energy row x pressure column) is
+// dropped, as in ILU(0).  The node's block row lives in shared memory; the
+// factored rows of lower nodes are read from global memory (earlier levels).
+// A pivot smaller than tau in magnitude (the row-scaled matrix has unit row
+// sums) becomes +-tau: in the reference's node-major order an element
+// without a pressure datum whose earlier velocity unknowns are all Dirichlet
+// rows leaves an exactly singular pressure pivot.
+struct IluArgs {
+  const int *fu;
+  const int64_t *rowptr;
+  const int *nbr_ptr, *nbr_node, *nbr_off, *nbr_offT;
+  int dim, nvn, energy;
+  int maxnb, lmax, maxnr;
+  double tau;
+  int *nfix;
+};
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    ilu0_block_kernel(const int *__restrict__ nodes, IluArgs g, const double *__restrict__ A,
+                      T *__restrict__ lu) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *blk = reinterpret_cast<T *>(sm_raw);                      // [maxnr][lmax]
+  T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [8][8]
+  int *snb = reinterpret_cast<int *>(lnm + 64);                  // [maxnb]
+  int *soff = snb + g.maxnb;
+  int *sndof = soff + g.maxnb;
+  int *tmap = sndof + g.maxnb;                                   // [maxnb]
+  const int n = nodes[blockIdx.x];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int base = g.nbr_ptr[n], nb = g.nbr_ptr[n + 1] - base;
+  const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+  const int Tr = g.energy ? g.dim : -1;  // local index of the energy row
+  for (int s2 = tid; s2 < nb; s2 += nt) {
+    const int q = g.nbr_node[base + s2];
+    snb[s2] = q;
+    soff[s2] = g.nbr_off[base + s2];
+    sndof[s2] = g.fu[q + 1] - g.fu[q];
+  }
+  __syncthreads();
+  const int L = soff[nb - 1] + sndof[nb - 1];
+  // load the block row (full layout; energy-row pressure columns held at 0)
+  for (int c = tid; c < L; c += nt) {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (soff[mid] <= c) lo = mid; else hi = mid - 1;
     }
-    if (lane == 0) {
-      const double d = lu[di];
-      if (fabs(d) < tau) {
-        lu[di] = d < 0.0 ? -tau : tau;
-        atomicAdd(nfix, 1);
+    const int d = c - soff[lo];
+    for (int r = 0; r < nr; r++) {
+      if (r == Tr) {
+        blk[r * g.lmax + c] = d >= g.nvn ? (T)0 : (T)A[g.rowptr[f0 + r] + g.nbr_offT[base + lo] + d];
+      } else {
+        blk[r * g.lmax + c] = (T)A[g.rowptr[f0 + r] + c];
       }
     }
-    __syncwarp();
+  }
+  int self = 0;
+  {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (snb[mid] < n) lo = mid + 1; else hi = mid;
+    }
+    self = lo;
+  }
+  __syncthreads();
+  for (int sm = 0; sm < self; sm++) {
+    const int m = snb[sm], mb = g.nbr_ptr[m], mnb = g.nbr_ptr[m + 1] - mb;
+    const int fm = g.fu[m], nm = sndof[sm], cm = soff[sm];
+    // neighbours q > m of m that are also neighbours of n
+    for (int t = tid; t < mnb; t += nt) {
+      const int q = g.nbr_node[mb + t];
+      int slot = -1;
+      if (q > m) {
+        int lo = 0, hi = nb - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (snb[mid] < q) lo = mid + 1; else hi = mid;
+        }
+        if (snb[lo] == q) slot = lo;
+      }
+      tmap[t] = slot;
+    }
+    // self slot of m in its own list (for U_mm)
+    int mself = 0;
+    {
+      int lo = 0, hi = mnb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (g.nbr_node[mb + mid] < m) lo = mid + 1; else hi = mid;
+      }
+      mself = lo;
+    }
+    // step 1: L_nm = A_nm U_mm^-1, one thread per row
+    if (tid < nr) {
+      const int r = tid;
+      for (int dk = 0; dk < nm; dk++) {
+        const bool rowkT = dk == Tr;
+        if (r == Tr && dk >= g.nvn) {
+          lnm[r * 8 + dk] = (T)0;
+          continue;
+        }
+        const int64_t rk = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + mself] : g.nbr_off[mb + mself]);
+        const T l = blk[r * g.lmax + cm + dk] / (T)lu[rk + dk];
+        blk[r * g.lmax + cm + dk] = l;
+        lnm[r * 8 + dk] = l;
+        for (int d2 = dk + 1; d2 < nm; d2++) {
+          if (r == Tr && d2 >= g.nvn) continue;
+          if (rowkT && d2 >= g.nvn) continue;
+          blk[r * g.lmax + cm + d2] -= l * (T)lu[rk + d2];
+        }
+      }
+    }
+    __syncthreads();
+    // step 2: A_nq -= L_nm U_mq
+    for (int t = 0; t < mnb; t++) {
+      const int slot = tmap[t];
+      if (slot < 0) continue;
+      const int nq = sndof[slot], cq = soff[slot];
+      for (int w = tid; w < nq * nr; w += nt) {
+        const int d = w / nr, r = w - d * nr;
+        if (r == Tr && d >= g.nvn) continue;
+        T acc = (T)0;
+        for (int dk = 0; dk < nm; dk++) {
+          const bool rowkT = dk == Tr;
+          if (rowkT && d >= g.nvn) continue;
+          const int64_t pos = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + t] : g.nbr_off[mb + t]) + d;
+          acc += lnm[r * 8 + dk] * (T)lu[pos];
+        }
+        blk[r * g.lmax + cq + d] -= acc;
+      }
+    }
+    __syncthreads();
+  }
+  // own diagonal block and the rest of the row
+  const int cs = soff[self];
+  for (int dk = 0; dk < nr; dk++) {
+    if (tid == 0) {
+      const T p = blk[dk * g.lmax + cs + dk];
+      if (fabs((double)p) < g.tau) {
+        blk[dk * g.lmax + cs + dk] = p < (T)0 ? (T)-g.tau : (T)g.tau;
+        atomicAdd(g.nfix, 1);
+      }
+    }
+    __syncthreads();
+    const T piv = blk[dk * g.lmax + cs + dk];
+    const int c0 = cs + dk + 1;
+    for (int r = dk + 1; r < nr; r++) {
+      if (r == Tr && dk >= g.nvn) continue;
+      const T l = blk[r * g.lmax + cs + dk] / piv;
+      for (int c = c0 + tid; c < L; c += nt) {
+        const T u = blk[dk * g.lmax + c];
+        if (u == (T)0) continue;
+        if (r == Tr) {
+          // energy row: pressure columns are outside the pattern
+          int lo = 0, hi = nb - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (soff[mid] <= c) lo = mid; else hi = mid - 1;
+          }
+          if (c - soff[lo] >= g.nvn) continue;
+        }
+        blk[r * g.lmax + c] -= l * u;
+      }
+    }
+    __syncthreads();
+    if (tid < nr && tid > dk && !(tid == Tr && dk >= g.nvn))
+      blk[tid * g.lmax + cs + dk] = blk[tid * g.lmax + cs + dk] / piv;
+    __syncthreads();
+  }
+  // write back
+  for (int c = tid; c < L; c += nt) {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (soff[mid] <= c) lo = mid; else hi = mid - 1;
+    }
+    const int d = c - soff[lo];
+    for (int r = 0; r < nr; r++) {
+      if (r == Tr) {
+        if (d < g.nvn) lu[g.rowptr[f0 + r] + g.nbr_offT[base + lo] + d] = blk[r * g.lmax + c];
+      } else {
+        lu[g.rowptr[f0 + r] + c] = blk[r * g.lmax + c];
+      }
+    }
   }
 }
 
@@ -412,6 +571,25 @@ int Solver::init(Context *c, int krylov) {
   GB_CU(cudaMemcpy(d_up_nodes, S.up_nodes.data(), sizeof(int) * S.up_nodes.size(),
                    cudaMemcpyHostToDevice), "sched");
   d_fu = c->d_fu;
+  if (L.nvn + L.npres > 8) return fail("ILU(0) supports at most 8 unknowns per node");
+  maxnb = 0;
+  lmax = 0;
+  for (int n = 0; n < L.num_nodes; n++) {
+    const int nb = L.nbr_ptr[n + 1] - L.nbr_ptr[n];
+    maxnb = std::max(maxnb, nb);
+    const int q = L.nbr_node[L.nbr_ptr[n + 1] - 1];
+    lmax = std::max(lmax, L.nbr_off[L.nbr_ptr[n + 1] - 1] + L.fu[q + 1] - L.fu[q]);
+  }
+  {
+    const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
+    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + 64) + ints;
+    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + 64) + ints;
+    if (sm64 > 200 * 1024) return fail("ILU(0) block row does not fit in shared memory");
+    GB_CU(cudaFuncSetAttribute(ilu0_block_kernel<double>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64), "smem");
+    GB_CU(cudaFuncSetAttribute(ilu0_block_kernel<float>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32), "smem");
+  }
   GB_CU(cudaMalloc(&d_lu, sizeof(double) * nnz), "ILU factors");
   GB_CU(cudaMalloc(&d_scale, sizeof(double) * N), "scale");
   const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kRedBlocks + 4 * (krylov + 2) + 64);
@@ -467,28 +645,49 @@ static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, c
 
 int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   d_A = vals;
-  GB_CU(cudaMemsetAsync(d_work + kRedBlocks * 3 + 10, 0, sizeof(int), st), "pivot count");
-  GB_CU(cudaMemcpyAsync(d_lu, vals, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, st), "lu copy");
+  int *nfix = (int *)(d_work + kRedBlocks * 3 + 10);
+  GB_CU(cudaMemsetAsync(nfix, 0, sizeof(int), st), "pivot count");
+  const Layout &L = C->L;
+  IluArgs g;
+  g.fu = d_fu;
+  g.rowptr = C->d_rowptr;
+  g.nbr_ptr = C->d_nbr_ptr;
+  g.nbr_node = C->d_nbr_node;
+  g.nbr_off = C->d_nbr_off;
+  g.nbr_offT = C->d_nbr_offT;
+  g.dim = L.dim;
+  g.nvn = L.nvn;
+  g.energy = L.energy;
+  g.maxnb = maxnb;
+  g.lmax = lmax;
+  g.maxnr = L.nvn + L.npres;
+  g.tau = pivot_tau;
+  g.nfix = nfix;
+  if (fp32 && !d_lu32) {
+    GB_CU(cudaMalloc(&d_lu32, sizeof(float) * nnz), "ILU32");
+    GB_CU(cudaMalloc(&d_a32, sizeof(float) * nnz), "A32");
+    GB_CU(cudaMalloc(&d_V32, sizeof(float) * (size_t)(max_krylov + 1) * N), "V32");
+    GB_CU(cudaMalloc(&d_t32, sizeof(float) * N), "t32");
+    GB_CU(cudaMalloc(&d_w32, sizeof(float) * N), "w32");
+  }
+  const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
-    ilu0_level_kernel<<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        d_lo_nodes + lo_ptr[l], cnt, d_fu, C->d_rowptr, C->d_colidx, d_diag, d_lu, pivot_tau,
-        (int *)(d_work + kRedBlocks * 3 + 10));
+    if (fp32) {
+      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + 64) + ints;
+      ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu32);
+    } else {
+      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + 64) + ints;
+      ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu);
+    }
   }
   GB_CU(cudaGetLastError(), "ILU(0) factorisation");
-  if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");
   if (fp32) {
-    if (!d_lu32) {
-      GB_CU(cudaMalloc(&d_lu32, sizeof(float) * nnz), "ILU32");
-      GB_CU(cudaMalloc(&d_a32, sizeof(float) * nnz), "A32");
-      GB_CU(cudaMalloc(&d_V32, sizeof(float) * (size_t)(max_krylov + 1) * N), "V32");
-      GB_CU(cudaMalloc(&d_t32, sizeof(float) * N), "t32");
-      GB_CU(cudaMalloc(&d_w32, sizeof(float) * N), "w32");
-    }
-    to_f32_kernel<<<1216, 256, 0, st>>>(nnz, d_lu, d_lu32);
     to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
-    GB_CU(cudaGetLastError(), "FP32 copies");
+    GB_CU(cudaGetLastError(), "FP32 matrix copy");
     if (!prec32) GB_CU(capture_prec<float>(this, d_lu32, d_t32, st, &prec32), "ILU32 graph");
+  } else {
+    if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");
   }
   return 0;
 }

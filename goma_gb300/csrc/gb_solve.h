@@ -35,6 +35,7 @@ struct Solver {
   std::vector<int> lo_ptr, up_ptr;
   const double *d_A = nullptr;  // scaled FP64 matrix the factors were built from
   double pivot_tau = 1e-4;      // ILU(0) pivot floor on the row-scaled matrix
+  int maxnb = 0, lmax = 0;      // largest node neighbourhood / block-row length
   double *d_scale = nullptr;
   double *d_work = nullptr;     // reduction scratch
   double *h_work = nullptr;     // pinned host mirror

@@ -1,0 +1,73 @@
+"""Host-side handle of the GPU network (gb_mlp in include/gb_newton.h)."""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class GpuMLP:
+    """n_in -> width x hidden_layers (tanh) -> n_out, FP32 on the GPU."""
+
+    def __init__(self, n_in, width, hidden_layers, n_out, seed=0):
+        self._L = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._L.gb_mlp_create(n_in, width, hidden_layers, n_out, seed,
+                                         ctypes.byref(h)))
+        self.h = h
+        self.widths = [n_in] + [width] * hidden_layers + [n_out]
+        self.nparam = self._L.gb_mlp_num_params(self.h)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self._L.gb_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.empty(self.nparam, np.float32)
+        _lib.check(self._L.gb_mlp_get_params(self.h, _fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _lib.check(self._L.gb_mlp_set_params(self.h, _fp(p)))
+
+    def grads(self):
+        g = np.empty(self.nparam, np.float32)
+        _lib.check(self._L.gb_mlp_get_grads(self.h, _fp(g)))
+        return g
+
+    # device tensors (torch) in, device tensors out
+    def forward(self, x):
+        import torch
+        x = x.contiguous().float()
+        y = torch.empty((x.shape[0], self.widths[-1]), dtype=torch.float32, device=x.device)
+        _lib.check(self._L.gb_mlp_forward_device(self.h, x.data_ptr(), x.shape[0], y.data_ptr()))
+        return y
+
+    def loss_grad(self, x, t, mask):
+        loss = ctypes.c_float()
+        _lib.check(self._L.gb_mlp_loss_grad_device(self.h, x.data_ptr(), t.data_ptr(),
+                                                   mask.data_ptr(), x.shape[0],
+                                                   ctypes.byref(loss)))
+        return loss.value
+
+    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        _lib.check(self._L.gb_mlp_adam_step(self.h, lr, b1, b2, eps))
+
+    def train(self, x, t, mask, steps, batch=4096, lr=1e-3, seed=0):
+        loss = ctypes.c_float()
+        _lib.check(self._L.gb_mlp_train_device(self.h, x.data_ptr(), t.data_ptr(), mask.data_ptr(),
+                                               x.shape[0], steps, batch, lr, seed,
+                                               ctypes.byref(loss)))
+        return loss.value

@@ -100,6 +100,26 @@ class GomaNewton:
     def status(self):
         _lib.check(self._L.gb_status(self.h))
 
+    def set_material(self, material):
+        """update_parameterC analogue: new material, same mesh and pattern."""
+        from .problem import make_desc
+        self.problem.material = material
+        desc, keep = make_desc(self.problem)
+        _lib.check(self._L.gb_set_material(self.h, ctypes.byref(desc.mat)))
+        del keep
+
+    def scale_device(self, d_vals, d_R, d_scale=None):
+        """row_sum_scaling_scale on device arrays (in place)."""
+        _lib.check(self._L.gb_row_sum_scale_device(self.h, d_vals, d_R, d_scale))
+
+    def linear_solve_device(self, d_vals, d_rhs, d_dx, **opts):
+        o = self.newton_opts(**opts)
+        its = ctypes.c_int()
+        rr = ctypes.c_double()
+        _lib.check(self._L.gb_linear_solve_device(self.h, d_vals, d_rhs, d_dx, ctypes.byref(o),
+                                                  ctypes.byref(its), ctypes.byref(rr)))
+        return its.value, rr.value
+
     # --- solve_nonlinear_problem
     def newton_opts(self, **kw):
         o = _lib.NewtonOpts()

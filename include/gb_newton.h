@@ -85,6 +85,11 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
+/* Replaces the material of a context (same mesh, DOF map and pattern), as
+ * update_parameterC does during continuation (src/ac_conti.c:755,
+ * src/ac_update_parameter.c). */
+int gb_set_material(gb_ctx *ctx, const gb_material *mat);
+
 /* Instrumentation: with enable = 1, every following assembly records CUDA
  * events around its element-kernel launches (on the launch stream, then
  * synchronises); a call returns the accumulated kernel time and launch
@@ -156,6 +161,35 @@ int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rh
  * (src/sl_aztecoo_interface.cpp:56). */
 int gb_linear_solve(gb_ctx *ctx, const double *a_msr, const double *rhs, double *dx,
                     const gb_newton_opts *opts, int *iterations, double *relres);
+
+/* ---------------------------------------------- learned continuation guess */
+
+/* A fully connected FP32 network, hidden layers tanh, trained on the GPU by
+ * the library's own forward / backward / Adam kernels.  It predicts the next
+ * Newton initial guess of a parameter continuation from (node coordinates,
+ * parameter); the reference has no counterpart -- its predictor
+ * (src/ac_conti.c:759-784, ALC_ZEROTH / ALC_FIRST) stays the fallback. */
+typedef struct gb_mlp gb_mlp;
+int gb_mlp_create(int n_in, int width, int hidden_layers, int n_out, unsigned long long seed,
+                  gb_mlp **out);
+void gb_mlp_destroy(gb_mlp *m);
+int gb_mlp_num_params(const gb_mlp *m);
+/* flat parameter / gradient buffers: per layer W[out][in] then b[out] */
+int gb_mlp_get_params(const gb_mlp *m, float *host);
+int gb_mlp_set_params(gb_mlp *m, const float *host);
+int gb_mlp_get_grads(const gb_mlp *m, float *host);
+/* y[B][n_out] = net(x[B][n_in]); device arrays */
+int gb_mlp_forward_device(gb_mlp *m, const float *d_x, int B, float *d_y);
+/* loss = sum mask (net(x) - t)^2 / sum mask, gradients kept inside (read
+ * with gb_mlp_get_grads); device arrays, *loss on the host */
+int gb_mlp_loss_grad_device(gb_mlp *m, const float *d_x, const float *d_t, const float *d_mask,
+                            int B, float *loss);
+int gb_mlp_adam_step(gb_mlp *m, float lr, float beta1, float beta2, float eps);
+/* steps Adam steps on minibatches of `batch` points drawn from n_points
+ * (fixed integer-hash sampling from seed) */
+int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const float *d_mask,
+                        int n_points, int steps, int batch, float lr, unsigned long long seed,
+                        float *final_loss);
 
 /* Measures this GPU's FP64 throughput (TFLOP/s) with two short kernels:
  * mma.sync m8n8k4 f64 (tensor pipe) and scalar FMA.  The FP64 roofline
