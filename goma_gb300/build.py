@@ -31,7 +31,7 @@ def sources():
 
 def _compile(src, nvcc):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
+    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps += [os.path.join(HERE, "..", "include", h)
              for h in os.listdir(os.path.join(HERE, "..", "include"))]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):

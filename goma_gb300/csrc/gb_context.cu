@@ -207,10 +207,21 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   AsmArgs a = args(x, R, vals);
   const int ncol = (int)L.color_ptr.size() - 1;
   if (timing) cudaEventRecord(ev_k0, st);
+  const bool tc = L.dim == 3 && vals != nullptr && path == 0;
+  if (tc && tc_grid == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    tc_grid = 2 * sms;
+  }
   for (int c = 0; c < ncol; c++) {
     const int n = L.color_ptr[c + 1] - L.color_ptr[c];
-    e = launch_assemble(a, L.dim, L.energy != 0, carreau, vals != nullptr,
-                        d_color_elems + L.color_ptr[c], n, st);
+    if (tc)
+      e = launch_assemble_tc(a, L.energy != 0, carreau, d_color_elems + L.color_ptr[c], n,
+                             tc_grid, st);
+    else
+      e = launch_assemble(a, L.dim, L.energy != 0, carreau, vals != nullptr,
+                          d_color_elems + L.color_ptr[c], n, st);
     if (e != cudaSuccess) return cuda_fail(e, "assembly launch");
   }
   if (timing) {
@@ -359,6 +370,12 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
   if (d_vals) *d_vals = ctx->c.d_vals;
   if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
   if (d_colidx) *d_colidx = ctx->c.d_colidx;
+  return 0;
+}
+
+int gb_set_assembly_path(gb_ctx *ctx, int path) {
+  if (!ctx || path < 0 || path > 1) return fail("path must be 0 (auto) or 1 (scalar FP64)");
+  ctx->c.path = path;
   return 0;
 }
 

@@ -21,6 +21,8 @@ struct Context {
   Layout L;
   MaterialDev mat{};
   bool carreau = false;
+  int path = 0;        // element kernel: 0 auto (DMMA in 3-D), 1 scalar FP64
+  int tc_grid = 0;     // persistent grid of the DMMA kernel
   cudaStream_t stream = nullptr;
   double *d_coords = nullptr;
   int *d_conn = nullptr;

@@ -41,5 +41,8 @@ struct AsmArgs {
 cudaError_t launch_assemble(const AsmArgs &a, int dim, bool energy, bool carreau, bool jac,
                             const int *elems, int nelem, cudaStream_t st);
 size_t assemble_smem_bytes(int dim, bool energy, bool carreau);
+// 3-D Jacobian contractions on the FP64 tensor pipe (gb_assemble_tc.cu)
+cudaError_t launch_assemble_tc(const AsmArgs &a, bool energy, bool carreau, const int *elems,
+                               int nelem, int grid_cap, cudaStream_t st);
 
 }  // namespace gb

@@ -108,6 +108,10 @@ class GomaNewton:
         _lib.check(self._L.gb_set_material(self.h, ctypes.byref(desc.mat)))
         del keep
 
+    def set_assembly_path(self, path):
+        """0: automatic (DMMA element Jacobians in 3-D), 1: scalar FP64."""
+        _lib.check(self._L.gb_set_assembly_path(self.h, int(path)))
+
     def scale_device(self, d_vals, d_R, d_scale=None):
         """row_sum_scaling_scale on device arrays (in place)."""
         _lib.check(self._L.gb_row_sum_scale_device(self.h, d_vals, d_R, d_scale))

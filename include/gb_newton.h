@@ -85,6 +85,11 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
+/* Element-kernel path of later assemblies: 0 = automatic (3-D Jacobians on
+ * the FP64 tensor pipe, DMMA), 1 = scalar FP64 everywhere.  Both give the
+ * same matrix to rounding. */
+int gb_set_assembly_path(gb_ctx *ctx, int path);
+
 /* Replaces the material of a context (same mesh, DOF map and pattern), as
  * update_parameterC does during continuation (src/ac_conti.c:755,
  * src/ac_update_parameter.c). */
