@@ -41,16 +41,17 @@ constexpr int TAB = QP_PAD * LD;
 enum { T_PHI = 0, T_G0, T_G1, T_G2, T_CK, T_GM0, T_GM1, T_GM2 };
 // coefficient ids (per quadrature point)
 enum {
-  C_AB = 0,  // 9: -rho dA gv[b][a], index a*3+b
-  C_NMU = 9,
-  C_NK,
-  C_TV,        // 3: -rho Cp dA gT[b]
-  C_VT = 13,   // 3: dA dfT[a]
-  C_CP = 16,
-  C_NCMU,
-  C_ONE,
-  NCOEF
+  C_AB = 0,        // 9: -rho dA gv[b][a], index a*3+b
+  C_NMU = 9,       // -mu dA
+  C_NK = 10,       // -k dA
+  C_TV = 11,       // 3: -rho Cp dA gT[b]
+  C_VT = 14,       // 3: dA dfT[a]
+  C_CP = 17,       // Cp
+  C_NCMU = 18,     // -cmu dA
+  C_ONE = 19,      // 1
+  NCOEF = 20
 };
+static_assert(C_VT == C_TV + 3 && C_CP == C_VT + 3, "coefficient ids overlap");
 
 struct Smem {
   double X[NN][3], U[NN][3], Tn[NN], Pn[NP];
@@ -319,7 +320,9 @@ __global__ void __launch_bounds__(256, 1)
       atomicMin(A.status + 1, e);
     }
 
-    // tensor-pipe part
+    // tensor-pipe part: mma.sync.aligned needs the whole warp converged, and
+    // the residual owners above diverge inside warps
+    __syncwarp();
     double acc0[16][2], acc1[16][2];
     if (blk0 >= 0) run_block<CARREAU>(acc0, blk0, S, lane);
     if (blk1 >= 0) run_block<CARREAU>(acc1, blk1, S, lane);
