@@ -30,6 +30,9 @@ class NewtonStats(ctypes.Structure):
                 ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
 
 
+MLP_NOALLOC_MAX_ACT = 1 << 20  # GB_MLP_NOALLOC_MAX_ACT of include/gb_newton.h
+
+
 class GbError(RuntimeError):
     pass
 
@@ -83,6 +86,7 @@ def load():
         "gb_mlp_set_params": (ctypes.c_int, [vp, fp]),
         "gb_mlp_get_grads": (ctypes.c_int, [vp, fp]),
         "gb_mlp_forward_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+        "gb_mlp_forward_noalloc": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
         "gb_mlp_loss_grad_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, fp]),
         "gb_mlp_adam_step": (ctypes.c_int, [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_float]),

@@ -17,7 +17,9 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/gb_newton.h"
@@ -499,3 +501,73 @@ int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const flo
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- allocation-free inference
+//
+// gb_mlp_forward_device keeps its hidden activations in buffers it
+// allocates (and grows) on demand.  gb_mlp_forward_noalloc runs the same
+// kernels with the activations in the fixed array below instead, for callers
+// that cannot allocate device memory at that point.
+
+namespace gb {
+
+// Two ping-pong activation buffers of GB_MLP_NOALLOC_MAX_ACT floats each.
+// Every GPU that loads the library holds this array until the process ends.
+static __device__ __align__(256) float g_mlp_noalloc_scratch[2 * (size_t)GB_MLP_NOALLOC_MAX_ACT];
+
+constexpr int kNoallocMaxDevices = 64;
+static float *g_noalloc_addr[kNoallocMaxDevices];  // device address, per device
+static std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device.  Host code only
+// sees a host-side stand-in under the array's name, so the address is
+// looked up once per device, with that device current.
+static int noalloc_scratch(float **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoallocMaxDevices) return fail("device index beyond the scratch table");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_mlp_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+    g_noalloc_addr[dev] = static_cast<float *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return 0;
+}
+
+}  // namespace gb
+
+extern "C" int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y) {
+  if (!m || !d_x || !d_y) return gb::fail("NULL argument");
+  if (B <= 0) return gb::fail("batch size must be positive");
+  gb::Mlp &M = m->m;
+  int widest = 0;
+  for (int l = 1; l + 1 < (int)M.width.size(); l++) widest = M.width[l] > widest ? M.width[l] : widest;
+  if ((long long)B * widest > (long long)GB_MLP_NOALLOC_MAX_ACT) {
+    char msg[200];
+    snprintf(msg, sizeof msg,
+             "batch %d x hidden width %d exceeds the static scratch of %d floats per activation "
+             "buffer; split the batch",
+             B, widest, (int)GB_MLP_NOALLOC_MAX_ACT);
+    return gb::fail(msg);
+  }
+  float *base = nullptr;
+  if (gb::noalloc_scratch(&base)) return -1;
+  float *buf[2] = {base, base + (size_t)GB_MLP_NOALLOC_MAX_ACT};
+  const float *in = d_x;
+  const int L = M.layers();
+  for (int l = 0; l < L; l++) {
+    const int K = M.width[l], N = M.width[l + 1];
+    float *out = l + 1 == L ? d_y : buf[l & 1];
+    dim3 grid((N + gb::TN - 1) / gb::TN, (B + gb::TM - 1) / gb::TM);
+    gb::gemm_xwT_kernel<<<grid, 256, 0, M.st>>>(B, N, K, in, M.d_w + M.woff[l], M.d_w + M.boff[l],
+                                                out, l + 1 < L ? 1 : 0);
+    in = out;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(M.st);
+  return e == cudaSuccess ? 0 : gb::cuda_fail(e, "MLP forward (no allocation)");
+}

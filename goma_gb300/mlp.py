@@ -55,6 +55,13 @@ class GpuMLP:
         _lib.check(self._L.gb_mlp_forward_device(self.h, x.data_ptr(), x.shape[0], y.data_ptr()))
         return y
 
+    def forward_noalloc(self, x, y):
+        """Forward pass into the caller's y without any device allocation
+        (gb_mlp_forward_noalloc): x [B, n_in] and y [B, n_out] are FP32 device
+        tensors the caller owns; B x hidden width <= MLP_NOALLOC_MAX_ACT."""
+        _lib.check(self._L.gb_mlp_forward_noalloc(self.h, x.data_ptr(), x.shape[0], y.data_ptr()))
+        return y
+
     def loss_grad(self, x, t, mask):
         loss = ctypes.c_float()
         _lib.check(self._L.gb_mlp_loss_grad_device(self.h, x.data_ptr(), t.data_ptr(),

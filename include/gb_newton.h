@@ -190,6 +190,24 @@ int gb_mlp_forward_device(gb_mlp *m, const float *d_x, int B, float *d_y);
 int gb_mlp_loss_grad_device(gb_mlp *m, const float *d_x, const float *d_t, const float *d_mask,
                             int B, float *loss);
 int gb_mlp_adam_step(gb_mlp *m, float lr, float beta1, float beta2, float eps);
+/* Same forward pass without allocating device memory.  This entry point has
+ * no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc when they ask for a prediction: a continuation driver whose
+ * device memory is all held by another allocator (a framework's caching
+ * allocator that has reserved the GPU), or a solver loop that must not take
+ * cudaMalloc's implicit device-wide synchronisation between Newton steps.
+ * The caller still passes x and y; the hidden activations go to a fixed
+ * array compiled into the library: two buffers of GB_MLP_NOALLOC_MAX_ACT
+ * floats, so B times the hidden width may not exceed GB_MLP_NOALLOC_MAX_ACT
+ * (larger batches are rejected with an error; split them).  Every GPU that
+ * loads the library holds that 8 MB until the process exits.  The first call
+ * on a device looks the array's device address up (once per device); make
+ * that first call before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU (other threads, other streams) race; it
+ * keeps the last call's activations, and nothing in it needs to start at
+ * zero because every activation is written before it is read. */
+#define GB_MLP_NOALLOC_MAX_ACT (1 << 20)
+int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y);
 /* steps Adam steps on minibatches of `batch` points drawn from n_points
  * (fixed integer-hash sampling from seed) */
 int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const float *d_mask,
