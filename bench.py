@@ -137,6 +137,49 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
                       % (done, nel_block, dt)}
 
 
+def time_to_solve(nel, ra_path=(1e4, 3e4, 1e5), tol=1e-10):
+    """Wall-clock time to the converged Boussinesq cube at Ra = ra_path[-1],
+    by Ra continuation from rest: plain FP64 Newton (ILU(0)-GMRES in FP64,
+    zeroth-order predictor, the reference's ALC_ZEROTH) against the learned
+    predictor + FP32-inner GMRES with FP64 refinement.  Returns a dict with
+    both times, Newton/Krylov counts and the relative difference of the two
+    converged solutions."""
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.continuation import continuation
+    from goma_gb300.newton import GomaNewton
+
+    def set_ra(gn, ra):
+        m = gn.problem.material
+        m.momentum_source = (0.0, 0.0, -ra * PR)
+        gn.set_material(m)
+
+    out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra continuation %s, Pr=%g, scaled |R| < %g"
+           % (nel, list(ra_path), PR, tol)}
+    sols = {}
+    for mode in ("plain_fp64", "learned_fp32"):
+        prob = pb.boussinesq_cube_3d(nel, ra_path[0], PR)
+        gn = GomaNewton(prob)
+        opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
+                    fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        recs, x = continuation(gn, ra_path[0], ra_path[-1], len(ra_path) - 1,
+                               predictor="learned" if mode == "learned_fp32" else "zeroth",
+                               set_param=set_ra, newton_opts=opts,
+                               learned_opts=dict(steps=300, batch=4096, lr=2e-3))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        sols[mode] = x
+        out[mode] = {"seconds": dt, "newton_its": sum(r["newton_its"] for r in recs),
+                     "guesses": [r["guess"] for r in recs[1:]]}
+        del gn
+    a, b = sols["plain_fp64"], sols["learned_fp32"]
+    out["solution_rel_diff"] = float(np.abs(a - b).max() / np.abs(a).max())
+    out["speedup"] = out["plain_fp64"]["seconds"] / out["learned_fp32"]["seconds"]
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path.  The reference C compiles
     only where its source tree is (oracle/_ref, not on the GPU machine), so
@@ -171,6 +214,8 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--solve-nel", type=int, default=8,
+                    help="cube size of the time-to-solve leg (0 skips it)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -303,6 +348,14 @@ def main():
             "gpu_launches": int(gn.num_colors * args.steps)}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(8, 1, budget_s=15.0)
+    if rank == 0 and args.solve_nel > 0:
+        del dv, dx, dR, xh, Rh, ah
+        gn.close()
+        torch.cuda.empty_cache()
+        try:
+            line["time_to_solve"] = time_to_solve(args.solve_nel)
+        except RuntimeError as exc:   # a continuation step that did not converge
+            line["time_to_solve"] = {"error": str(exc)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

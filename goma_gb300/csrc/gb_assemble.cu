@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(256)
     assemble_kernel(AsmArgs A, const int *__restrict__ elems, int nelem) {
   using C = Q2<DIM>;
   constexpr int NN = C::NN, NQ = C::NQ, NP = C::NP, TPE = C::TPE, EPB = C::EPB, PPT = C::PPT;
-  constexpr int NVN = DIM + (ENERGY ? 1 : 0);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using Elem = ElemSmem<DIM, CARREAU>;
   Elem *S = reinterpret_cast<Elem *>(smem_raw);
@@ -93,7 +92,7 @@ __global__ void __launch_bounds__(256)
     }
     if (ENERGY) E.Tn[k] = A.x[f0 + DIM];
     if (k == C::CENT)
-      for (int l = 0; l < NP; l++) E.Pn[l] = A.x[f0 + NVN + l];
+      for (int l = 0; l < NP; l++) E.Pn[l] = A.x[f0 + A.pofs + l];
   }
   __syncthreads();
 
@@ -275,8 +274,8 @@ __global__ void __launch_bounds__(256)
     } else {
       k = C::CENT;
       node = nodes[C::CENT];
-      gr = A.fu[node] + NVN + rc;
-      rowvar = NVN + rc;
+      gr = A.fu[node] + A.pofs + rc;
+      rowvar = A.pofs + rc;
     }
     const bool dir = A.dbc[gr] != 0;
     if (!dir) A.R[gr] += Racc;
@@ -291,7 +290,7 @@ __global__ void __launch_bounds__(256)
       } else if (own_m) {
         // J_m_P: row (a, i), columns P_l at the centroid node
         const int s = nslot[k * NN + C::CENT];
-        const int64_t base = rb + A.nbr_off[nb0 + s] + NVN;
+        const int64_t base = rb + A.nbr_off[nb0 + s] + A.pofs;
 #pragma unroll
         for (int l = 0; l < NP; l++) A.vals[base + l] += JmP[l];
       }
@@ -305,7 +304,7 @@ __global__ void __launch_bounds__(256)
     const int off = A.nbr_off[nb0 + s] + ra;
 #pragma unroll
     for (int l = 0; l < NP; l++) {
-      const int gr = A.fu[nc] + NVN + l;
+      const int gr = A.fu[nc] + A.pofs + l;
       if (A.dbc[gr]) continue;
       A.vals[A.rowptr[gr] + off] += JmP[l];
     }

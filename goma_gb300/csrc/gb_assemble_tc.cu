@@ -169,7 +169,7 @@ template <bool ENERGY, bool CARREAU>
 __global__ void __launch_bounds__(256, 1)
     assemble_tc_kernel(AsmArgs A, const int *__restrict__ elems, int nelem) {
   using namespace tc;
-  constexpr int DIM = 3, NVN = DIM + (ENERGY ? 1 : 0);
+  constexpr int DIM = 3;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem &S = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256, 1)
       }
       S.Tn[k] = ENERGY ? A.x[f0 + DIM] : 0.0;
       if (k == CENT)
-        for (int l = 0; l < NP; l++) S.Pn[l] = A.x[f0 + NVN + l];
+        for (int l = 0; l < NP; l++) S.Pn[l] = A.x[f0 + A.pofs + l];
     }
     if (tid == 0) S.e = e;
     __syncthreads();
@@ -344,8 +344,8 @@ __global__ void __launch_bounds__(256, 1)
       } else {
         k = CENT;
         node = S.nodes[CENT];
-        gr = A.fu[node] + NVN + rc;
-        rowvar = NVN + rc;
+        gr = A.fu[node] + A.pofs + rc;
+        rowvar = A.pofs + rc;
       }
       const bool dir = A.dbc[gr] != 0;
       if (!dir) A.R[gr] += Racc;
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(256, 1)
         A.vals[rb + off + rowvar] += 1.0;
       } else if (own_m) {
         const int s = nslot[k * NN + CENT];
-        const int64_t base = rb + A.nbr_off[nb0 + s] + NVN;
+        const int64_t base = rb + A.nbr_off[nb0 + s] + A.pofs;
 #pragma unroll
         for (int l = 0; l < NP; l++) A.vals[base + l] += JmP[l];
       }
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(256, 1)
       const int off = A.nbr_off[nb0 + s] + ra;
 #pragma unroll
       for (int l = 0; l < NP; l++) {
-        const int gr = A.fu[nc] + NVN + l;
+        const int gr = A.fu[nc] + A.pofs + l;
         if (A.dbc[gr]) continue;
         A.vals[A.rowptr[gr] + off] += JmP[l];
       }

@@ -134,6 +134,22 @@ int Context::set_material(const gb_material &m) {
   for (int a = 0; a < 3; a++) mat.source[a] = m.momentum_source[a];
   mat.beta = m.volume_expansion;
   mat.Tref = m.reference_temperature;
+  mat.nspec = L.nspec;
+  for (int w = 0; w < GB_MAX_SPECIES; w++) {
+    const bool on = w < L.nspec;
+    const int model = on ? m.species_source_model[w] : GB_SPECIES_SOURCE_NONE;
+    if (model != GB_SPECIES_SOURCE_NONE && model != GB_SPECIES_SOURCE_CONSTANT &&
+        model != GB_SPECIES_SOURCE_ARRHENIUS)
+      return fail("unsupported species source model");
+    if (model == GB_SPECIES_SOURCE_ARRHENIUS) {
+      const double src = m.species_source[w][3];
+      if (!L.energy || !(src >= 0.0 && src < L.nspec && src == (int)src))
+        return fail("an Arrhenius species source needs the energy equation and a valid species index");
+    }
+    mat.diff[w] = on ? m.diffusivity[w] : 0.0;
+    mat.ssm[w] = model;
+    for (int k = 0; k < 4; k++) mat.ssp[w][k] = on ? m.species_source[w][k] : 0.0;
+  }
   carreau = m.viscosity_model == GB_VISC_CARREAU;
   desc.mat = m;
   return 0;
@@ -195,6 +211,7 @@ AsmArgs Context::args(const double *x, double *R, double *vals) const {
   a.R = R;
   a.vals = vals;
   a.status = d_status;
+  a.pofs = L.nvn;
   a.mat = mat;
   return a;
 }
@@ -223,6 +240,11 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
       e = launch_assemble(a, L.dim, L.energy != 0, carreau, vals != nullptr,
                           d_color_elems + L.color_ptr[c], n, st);
     if (e != cudaSuccess) return cuda_fail(e, "assembly launch");
+    if (L.nspec > 0) {
+      e = launch_assemble_species(a, L.dim, L.energy != 0, vals != nullptr,
+                                  d_color_elems + L.color_ptr[c], n, st);
+      if (e != cudaSuccess) return cuda_fail(e, "species assembly launch");
+    }
   }
   if (timing) {
     cudaEventRecord(ev_k1, st);
@@ -230,7 +252,7 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev_k0, ev_k1);
     kernel_ms += ms;
-    kernel_launches += ncol;
+    kernel_launches += ncol * (L.nspec > 0 ? 2 : 1);
   }
   return 0;
 }
@@ -376,6 +398,12 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 int gb_set_assembly_path(gb_ctx *ctx, int path) {
   if (!ctx || path < 0 || path > 1) return fail("path must be 0 (auto) or 1 (scalar FP64)");
   ctx->c.path = path;
+  return 0;
+}
+
+int gb_set_triangular_solve(gb_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 1) return fail("mode must be 0 (sync-free) or 1 (level graph)");
+  ctx->c.trsv = mode;
   return 0;
 }
 

@@ -14,6 +14,12 @@ struct MaterialDev {
   int source_model;
   double source[3];
   double beta, Tref;
+  // species w < nspec: Fickian diffusivity and source (GB_SPECIES_SOURCE_*;
+  // CONSTANT ssp[w][0], ARRHENIUS k0, E, nu, s)
+  int nspec;
+  double diff[GB_MAX_SPECIES];
+  int ssm[GB_MAX_SPECIES];
+  double ssp[GB_MAX_SPECIES][4];
 };
 
 // Everything the assembly kernel reads or writes.  Device pointers.
@@ -35,12 +41,18 @@ struct AsmArgs {
   double *R;                   // N
   double *vals;                // nnz (CSR, diagonal in row); NULL: residual only
   int *status;                 // [0] non-positive det J count, [1] first such element
+  int pofs;                    // offset of the first P1 pressure at a centroid node
+                               // (= nodal fields per node: dim + energy + species)
   MaterialDev mat;
 };
 
 cudaError_t launch_assemble(const AsmArgs &a, int dim, bool energy, bool carreau, bool jac,
                             const int *elems, int nelem, cudaStream_t st);
 size_t assemble_smem_bytes(int dim, bool energy, bool carreau);
+// species rows (gb_assemble_species.cu); launched after the flow kernel of
+// the same colour
+cudaError_t launch_assemble_species(const AsmArgs &a, int dim, bool energy, bool jac,
+                                    const int *elems, int nelem, cudaStream_t st);
 // 3-D Jacobian contractions on the FP64 tensor pipe (gb_assemble_tc.cu)
 cudaError_t launch_assemble_tc(const AsmArgs &a, bool energy, bool carreau, const int *elems,
                                int nelem, int grid_cap, cudaStream_t st);

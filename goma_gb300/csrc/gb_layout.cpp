@@ -2,8 +2,9 @@
 //
 // Unknown numbering restates Index_Solution (src/mm_unknown_map.c:5268):
 // node by node; per node the velocity components, then T when the energy
-// equation is on, and at an element's centroid node its dim+1 P1 pressure
-// unknowns.  The coupling graph restates build_node_node
+// equation is on, then the species Y_0.., and at an element's centroid node
+// its dim+1 P1 pressure unknowns (variable types ascending,
+// include/rf_fem_const.h:174-200).  The coupling graph restates build_node_node
 // (src/exo_conn.c:204) and find_MSR_problem_graph (src/mm_fill_util.c:3229):
 // an unknown couples with every unknown of every node that shares an
 // element with its node; a centroid node also couples with the centroid
@@ -31,7 +32,27 @@ int build_layout(const gb_problem_desc *d, Layout &L, std::string &err) {
   L.nn = d->dim == 2 ? 9 : 27;
   L.centroid = d->dim == 2 ? 8 : 20;
   L.energy = d->energy ? 1 : 0;
-  L.nvn = d->dim + L.energy;
+  if (d->num_species < 0 || d->num_species > GB_MAX_SPECIES) {
+    err = "num_species must be in [0, GB_MAX_SPECIES]";
+    return -1;
+  }
+  L.nspec = d->num_species;
+  for (int w = 0; w < L.nspec; w++) {
+    const int m = d->mat.species_source_model[w];
+    if (m != GB_SPECIES_SOURCE_NONE && m != GB_SPECIES_SOURCE_CONSTANT &&
+        m != GB_SPECIES_SOURCE_ARRHENIUS) {
+      err = "unknown species source model";
+      return -1;
+    }
+    if (m == GB_SPECIES_SOURCE_ARRHENIUS) {
+      const double s = d->mat.species_source[w][3];
+      if (!L.energy || !(s >= 0.0 && s < L.nspec && s == (int)s)) {
+        err = "an Arrhenius species source needs the energy equation and a valid species index";
+        return -1;
+      }
+    }
+  }
+  L.nvn = d->dim + L.energy + L.nspec;
   L.npres = d->dim + 1;
   L.nloc = L.nvn * L.nn + L.npres;
   L.num_nodes = d->num_nodes;
@@ -163,7 +184,10 @@ int build_layout(const gb_problem_desc *d, Layout &L, std::string &err) {
       off = d->dim;
     else if (var == GB_VAR_T)
       continue;
-    else {
+    else if (var >= GB_VAR_Y(0) && var < GB_VAR_Y(0) + GB_MAX_SPECIES) {
+      if (var - GB_VAR_Y(0) >= L.nspec) continue;
+      off = d->dim + L.energy + (var - GB_VAR_Y(0));
+    } else {
       err = "Dirichlet card on an unsupported variable";
       return -1;
     }

@@ -12,6 +12,7 @@ namespace gb {
 
 struct Layout {
   int dim = 0, nn = 0, centroid = 0, nvn = 0, npres = 0, nloc = 0, energy = 0;
+  int nspec = 0;  // species; nodal fields are u..(w), T, Y_0..Y_{nspec-1}
   int num_nodes = 0, num_elems = 0, N = 0;
   int64_t nnz = 0;              // CSR entries, diagonal included
   std::vector<int> fu;          // first unknown per node (num_nodes + 1)

@@ -164,7 +164,7 @@ __global__ void gemv_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
 
 template <class T>
 __global__ void scale_copy_kernel(int N, const T *x, const double *__restrict__ alpha_inv, T *y) {
-  const double a = 1.0 / alpha_inv[0];
+  const double a = alpha_inv[0] != 0.0 ? 1.0 / alpha_inv[0] : 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
     y[i] = (T)((double)x[i] * a);
 }
@@ -252,7 +252,7 @@ __device__ __forceinline__ int64_t find_col(const int *__restrict__ colidx, int6
 // every unknown of every neighbour node; the energy row alone skips pressure
 // columns), so the reference's scalar ILU(0) in node-major order is, block
 // by block: for each lower neighbour node m (ascending)
-//     L_nm   = A_nm U_mm^-1                 (triangular, <= 8 x 8)
+//     L_nm   = A_nm U_mm^-1                 (triangular, <= 16 x 16)
 //     A_nq  -= L_nm U_mq   for every q > m neighbouring both n and m
 // then the dense elimination of the node's own diagonal block and the rest
 // of its row.  Fill outside the pattern (energy row x pressure column) is
@@ -262,6 +262,9 @@ __device__ __forceinline__ int64_t find_col(const int *__restrict__ colidx, int6
 // sums) becomes +-tau: in the reference's node-major order an element
 // without a pressure datum whose earlier velocity unknowns are all Dirichlet
 // rows leaves an exactly singular pressure pivot.
+// unknowns per node: nodal fields (<= 3 + 1 + GB_MAX_SPECIES) + P1 pressures
+static constexpr int kMaxNodeDofs = 16;
+
 struct IluArgs {
   const int *fu;
   const int64_t *rowptr;
@@ -278,8 +281,8 @@ __global__ void __launch_bounds__(256)
                       T *__restrict__ lu) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *blk = reinterpret_cast<T *>(sm_raw);                      // [maxnr][lmax]
-  T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [8][8]
-  int *snb = reinterpret_cast<int *>(lnm + 64);                  // [maxnb]
+  T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [16][16]
+  int *snb = reinterpret_cast<int *>(lnm + kMaxNodeDofs * kMaxNodeDofs);  // [maxnb]
   int *soff = snb + g.maxnb;
   int *sndof = soff + g.maxnb;
   int *tmap = sndof + g.maxnb;                                   // [maxnb]
@@ -355,13 +358,13 @@ __global__ void __launch_bounds__(256)
       for (int dk = 0; dk < nm; dk++) {
         const bool rowkT = dk == Tr;
         if (r == Tr && dk >= g.nvn) {
-          lnm[r * 8 + dk] = (T)0;
+          lnm[r * kMaxNodeDofs + dk] = (T)0;
           continue;
         }
         const int64_t rk = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + mself] : g.nbr_off[mb + mself]);
         const T l = blk[r * g.lmax + cm + dk] / (T)lu[rk + dk];
         blk[r * g.lmax + cm + dk] = l;
-        lnm[r * 8 + dk] = l;
+        lnm[r * kMaxNodeDofs + dk] = l;
         for (int d2 = dk + 1; d2 < nm; d2++) {
           if (r == Tr && d2 >= g.nvn) continue;
           if (rowkT && d2 >= g.nvn) continue;
@@ -383,7 +386,7 @@ __global__ void __launch_bounds__(256)
           const bool rowkT = dk == Tr;
           if (rowkT && d >= g.nvn) continue;
           const int64_t pos = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + t] : g.nbr_off[mb + t]) + d;
-          acc += lnm[r * 8 + dk] * (T)lu[pos];
+          acc += lnm[r * kMaxNodeDofs + dk] * (T)lu[pos];
         }
         blk[r * g.lmax + cq + d] -= acc;
       }
@@ -484,6 +487,92 @@ __global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
   }
 }
 
+// Sync-free triangular solves: one cooperative launch per sweep.  Warps take
+// nodes in elimination order from an atomic ticket (ascending for L,
+// descending for U), wait until every node they depend on (lower / higher
+// neighbours) has published this solve's epoch in its flag, solve their
+// node's unknowns in order, and publish.  Tickets are handed out in order,
+// so the node a warp waits on is always held by a warp that is already
+// running; the cooperative launch keeps every block resident as well.
+// Every wait is bounded: past kSpinLimit polls the warp records an error,
+// publishes anyway (so no other warp can wait forever), every later wait of
+// the sweep stops within 1024 polls, and the host reports the failure after
+// the sweep.  A legitimate wait lasts microseconds; the limit is ~0.3 s.
+static constexpr long long kSpinLimit = 1LL << 22;
+
+struct TrsvArgs {
+  const int *fu;
+  const int64_t *rowptr;
+  const int *colidx;
+  const int64_t *diag;
+  const int *nbr_ptr;
+  const int *nbr_node;
+  int num_nodes;
+  unsigned *flags;     // per node: epoch of the last sweep that finished it
+  unsigned *tickets;   // [0] L sweep, [1] U sweep (reset before each sweep)
+  int *error;          // set when a wait gave up
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <class T, bool LOWER>
+__global__ void __launch_bounds__(256) trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu,
+                                                             T *z, unsigned epoch) {
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(g.tickets + (LOWER ? 0 : 1), 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= (unsigned)g.num_nodes) return;
+    const int n = LOWER ? (int)t : g.num_nodes - 1 - (int)t;
+    // wait for the dependencies
+    bool gave_up = false;
+    for (int q = g.nbr_ptr[n] + lane; q < g.nbr_ptr[n + 1]; q += 32) {
+      const int m = g.nbr_node[q];
+      if (LOWER ? m >= n : m <= n) continue;
+      long long polls = 0;
+      while (ld_acquire(g.flags + m) != epoch) {
+        // past the limit, or once any warp of the sweep has given up
+        if (++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile int *)g.error)) {
+          gave_up = true;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (__any_sync(0xffffffffu, gave_up) && lane == 0) atomicExch(g.error, 1);
+    __syncwarp();
+    // solve the node's unknowns in order
+    const int f0 = g.fu[n], f1 = g.fu[n + 1];
+    for (int r = 0; r < f1 - f0; r++) {
+      const int i = LOWER ? f0 + r : f1 - 1 - r;
+      const int64_t di = g.diag[i];
+      const int64_t p0 = LOWER ? g.rowptr[i] : di + 1;
+      const int64_t p1 = LOWER ? di : g.rowptr[i + 1];
+      double sum = 0.0;
+      for (int64_t p = p0 + lane; p < p1; p += 32)
+        sum = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), sum);
+      sum = warp_sum(sum);
+      if (lane == 0) {
+        const double zi = (double)__ldcg(z + i);
+        const double v = LOWER ? zi - sum : (zi - sum) / (double)lu[di];
+        __stcg(z + i, (T)v);
+      }
+      __syncwarp();
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(g.flags + n, epoch);
+  }
+}
+
 // ------------------------------------------------------------ schedule
 
 void build_ilu_schedule(const Layout &L, IluSchedule &S) {
@@ -533,7 +622,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
 Solver::~Solver() {
   if (prec64) cudaGraphExecDestroy(prec64);
   if (prec32) cudaGraphExecDestroy(prec32);
-  void *p[] = {d_lu, d_lu32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work,
+  void *p[] = {d_lu, d_lu32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
                d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
@@ -571,7 +660,7 @@ int Solver::init(Context *c, int krylov) {
   GB_CU(cudaMemcpy(d_up_nodes, S.up_nodes.data(), sizeof(int) * S.up_nodes.size(),
                    cudaMemcpyHostToDevice), "sched");
   d_fu = c->d_fu;
-  if (L.nvn + L.npres > 8) return fail("ILU(0) supports at most 8 unknowns per node");
+  if (L.nvn + L.npres > kMaxNodeDofs) return fail("ILU(0) supports at most 16 unknowns per node");
   maxnb = 0;
   lmax = 0;
   for (int n = 0; n < L.num_nodes; n++) {
@@ -582,8 +671,8 @@ int Solver::init(Context *c, int krylov) {
   }
   {
     const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
-    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + 64) + ints;
-    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + 64) + ints;
+    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
+    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
     if (sm64 > 200 * 1024) return fail("ILU(0) block row does not fit in shared memory");
     GB_CU(cudaFuncSetAttribute(ilu0_block_kernel<double>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64), "smem");
@@ -592,7 +681,7 @@ int Solver::init(Context *c, int krylov) {
   }
   GB_CU(cudaMalloc(&d_lu, sizeof(double) * nnz), "ILU factors");
   GB_CU(cudaMalloc(&d_scale, sizeof(double) * N), "scale");
-  const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kRedBlocks + 4 * (krylov + 2) + 64);
+  const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kRedBlocks + 4 * (krylov + 2) + 96);
   GB_CU(cudaMalloc(&d_work, sizeof(double) * wk), "work");
   GB_CU(cudaMallocHost(&h_work, sizeof(double) * 4 * (krylov + 2) + 64 * sizeof(double)), "host");
   GB_CU(cudaMalloc(&d_V, sizeof(double) * (size_t)(krylov + 1) * N), "Krylov basis");
@@ -674,10 +763,10 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
     if (fp32) {
-      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + 64) + ints;
+      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
       ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu32);
     } else {
-      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + 64) + ints;
+      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
       ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu);
     }
   }
@@ -692,11 +781,69 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   return 0;
 }
 
+template <class T>
+static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
+  Context *C = S->C;
+  if (!S->d_flags) {
+    GB_CU(cudaMalloc(&S->d_flags, sizeof(unsigned) * C->L.num_nodes + 16 * sizeof(unsigned)),
+          "trsv flags");
+    GB_CU(cudaMemsetAsync(S->d_flags, 0, sizeof(unsigned) * C->L.num_nodes + 16 * sizeof(unsigned),
+                          st), "trsv flags");
+    int per_sm = 1 << 30, dev = 0, sms = 0;
+    const void *fns[4] = {(const void *)trsv_sync_free_kernel<double, true>,
+                          (const void *)trsv_sync_free_kernel<double, false>,
+                          (const void *)trsv_sync_free_kernel<float, true>,
+                          (const void *)trsv_sync_free_kernel<float, false>};
+    for (const void *f : fns) {
+      int b = 0;
+      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, 256, 0), "occupancy");
+      per_sm = std::min(per_sm, b);
+    }
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    S->trsv_grid = std::max(1, std::min(per_sm, 4)) * sms;
+  }
+  TrsvArgs g;
+  g.fu = C->d_fu;
+  g.rowptr = C->d_rowptr;
+  g.colidx = C->d_colidx;
+  g.diag = S->d_diag;
+  g.nbr_ptr = C->d_nbr_ptr;
+  g.nbr_node = C->d_nbr_node;
+  g.num_nodes = C->L.num_nodes;
+  g.flags = S->d_flags;
+  g.tickets = S->d_flags + C->L.num_nodes;
+  g.error = (int *)(S->d_flags + C->L.num_nodes + 4);
+  for (int pass = 0; pass < 2; pass++) {
+    const unsigned epoch = ++S->epoch;
+    GB_CU(cudaMemsetAsync(g.tickets, 0, 2 * sizeof(unsigned), st), "tickets");
+    void *args[] = {&g, (void *)&lu, &z, (void *)&epoch};
+    void *fn = pass == 0 ? (void *)trsv_sync_free_kernel<T, true>
+                         : (void *)trsv_sync_free_kernel<T, false>;
+    GB_CU(cudaLaunchCooperativeKernel(fn, dim3(S->trsv_grid), dim3(256), args, 0, st), "trsv");
+  }
+  return 0;
+}
+
+int Solver::check_trsv_error() {
+  if (!d_flags) return 0;
+  int h = 0;
+  GB_CU(cudaMemcpy(&h, d_flags + C->L.num_nodes + 4, sizeof(int), cudaMemcpyDeviceToHost),
+        "trsv error");
+  if (h) {
+    cudaMemset(d_flags + C->L.num_nodes + 4, 0, sizeof(int));
+    return fail("triangular solve: a dependency wait gave up");
+  }
+  return 0;
+}
+
 int Solver::apply_prec64(cudaStream_t st) {
+  if (C->trsv == 0) return sync_free_apply<double>(this, d_lu, d_t, st);
   GB_CU(cudaGraphLaunch(prec64, st), "ILU apply");
   return 0;
 }
 int Solver::apply_prec32(cudaStream_t st) {
+  if (C->trsv == 0) return sync_free_apply<float>(this, d_lu32, d_t32, st);
   GB_CU(cudaGraphLaunch(prec32, st), "ILU32 apply");
   return 0;
 }
@@ -744,7 +891,7 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
   const int64_t ld = N;
   double *dred = S.d_work;                           // partials
   double *dh = S.d_work + kRedBlocks * 3 + 16;       // (m+2) results
-  double *dpart = dh + (m + 2) * 2;                  // (m+2) * kRedBlocks
+  double *dpart = dh + (m + 2) * 2 + 8;              // (m+2) * kRedBlocks
   double *hh = S.h_work;
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
   auto norm = [&](const T *v, double *out) -> int {
@@ -778,25 +925,26 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
       GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
       if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
       GB_CU(spmv<T>(C, lpr, A, t, w, st), "spmv");
-      // CGS2
+      // CGS2 on the device; the host reads both passes and the norm in one copy
       std::vector<double> hcol(j + 2, 0.0);
-      for (int pass = 0; pass < 2; pass++) {
-        multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
-        multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh);
-        gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh, w);
-        GB_CU(cudaMemcpyAsync(hh, dh, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, st), "h");
-        GB_CU(cudaStreamSynchronize(st), "h sync");
-        for (int i = 0; i <= j; i++) hcol[i] += hh[i];
-      }
-      double hn;
-      if (norm(w, &hn)) return -1;
+      double *dh1 = dh, *dh2 = dh + (m + 2), *dnrm = dh + 2 * (m + 2);
+      multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
+      multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh1);
+      gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
+      multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
+      multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh2);
+      gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
+      norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dred);
+      norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, dred, dnrm);
+      scale_copy_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dnrm, V + (j + 1) * ld);
+      GB_CU(cudaGetLastError(), "Arnoldi step");
+      GB_CU(cudaMemcpyAsync(hh, dh, sizeof(double) * (2 * (m + 2) + 1), cudaMemcpyDeviceToHost,
+                            st), "h");
+      GB_CU(cudaStreamSynchronize(st), "h sync");
+      for (int i = 0; i <= j; i++) hcol[i] = hh[i] + hh[(m + 2) + i];
+      const double hn = hh[2 * (m + 2)];
       hcol[j + 1] = hn;
       total++;
-      if (hn > 0.0) {
-        hh[0] = hn;
-        GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double), cudaMemcpyHostToDevice, st), "hn");
-        scale_copy_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dh, V + (j + 1) * ld);
-      }
       // Givens
       for (int i = 0; i < j; i++) {
         const double a = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
@@ -842,8 +990,20 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
 // Solves the scaled system A dx = R (both on the device, A = d_vals_scaled
 // after factorisation).  FP64: GMRES in FP64.  FP32 refined: FP32 GMRES on
 // the normalised residual inside FP64 iterative refinement.
+static int linear_solve_impl(Context *C, const double *R, double *dx, const LinearOpts &o,
+                             LinearStats *s, cudaStream_t st);
+
 int linear_solve(Context *C, const double *R, double *dx, const LinearOpts &o, LinearStats *s,
                  cudaStream_t st) {
+  const int rc = linear_solve_impl(C, R, dx, o, s, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "linear solve");
+  if (C->solver->check_trsv_error()) return -1;
+  return rc;
+}
+
+static int linear_solve_impl(Context *C, const double *R, double *dx, const LinearOpts &o,
+                             LinearStats *s, cudaStream_t st) {
   Solver &S = *C->solver;
   const int N = C->L.N;
   s->iterations = 0;

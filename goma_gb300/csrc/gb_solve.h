@@ -45,6 +45,10 @@ struct Solver {
   double *d_t = nullptr, *d_w = nullptr, *d_r = nullptr, *d_xs = nullptr;
   float *d_t32 = nullptr, *d_w32 = nullptr;
   cudaGraphExec_t prec64 = nullptr, prec32 = nullptr;  // captured ILU solves on d_t / d_t32
+  unsigned *d_flags = nullptr;  // per-node epochs, tickets, error word
+  unsigned epoch = 0;
+  int trsv_grid = 0;
+  int check_trsv_error();
   ~Solver();
   int init(Context *c, int krylov);
   int factor(const double *vals, bool fp32, cudaStream_t st);

@@ -112,6 +112,10 @@ class GomaNewton:
         """0: automatic (DMMA element Jacobians in 3-D), 1: scalar FP64."""
         _lib.check(self._L.gb_set_assembly_path(self.h, int(path)))
 
+    def set_triangular_solve(self, mode):
+        """ILU(0) solves: 0 sync-free sweeps, 1 level-scheduled graph."""
+        _lib.check(self._L.gb_set_triangular_solve(self.h, int(mode)))
+
     def scale_device(self, d_vals, d_R, d_scale=None):
         """row_sum_scaling_scale on device arrays (in place)."""
         _lib.check(self._L.gb_row_sum_scale_device(self.h, d_vals, d_R, d_scale))

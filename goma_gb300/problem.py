@@ -15,6 +15,13 @@ import numpy as np
 VAR_U1, VAR_U2, VAR_U3, VAR_T, VAR_P = 0, 1, 2, 3, 9
 VISC_NEWTONIAN, VISC_CARREAU = 0, 1
 SOURCE_CONSTANT, SOURCE_BOUSSINESQ = 0, 1
+MAX_SPECIES = 4
+SPECIES_SOURCE_NONE, SPECIES_SOURCE_CONSTANT, SPECIES_SOURCE_ARRHENIUS = 0, 1, 2
+
+
+def VAR_Y(w):
+    """Variable id of species w (GB_VAR_Y in include/gb_problem.h)."""
+    return 100 + w
 
 # grid offsets (0..2) of the local nodes, Goma order
 QUAD9_LOCAL = np.array([[0, 0], [2, 0], [2, 2], [0, 2], [1, 0], [2, 1], [1, 2], [0, 1], [1, 1]])
@@ -144,6 +151,11 @@ class Material:
     momentum_source: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     volume_expansion: float = 0.0
     reference_temperature: float = 0.0
+    # species w: Fickian diffusivity and source; a source is (model, params),
+    # params (S,) for CONSTANT, (k0, E, nu, s) for ARRHENIUS:
+    # S_w = nu k0 exp(-E/T) Y_s
+    diffusivity: Tuple[float, ...] = ()
+    species_source: Tuple[Tuple[int, Tuple[float, ...]], ...] = ()
 
 
 @dataclass
@@ -154,6 +166,7 @@ class Problem:
     # Dirichlet cards in deck order: (variable, node set id (1-based), value)
     bcs: List[Tuple[int, int, float]] = field(default_factory=list)
     pressure_datum: Tuple[int, float] = (-1, 0.0)
+    num_species: int = 0
 
     @property
     def dim(self):
@@ -169,20 +182,37 @@ class CMaterial(ctypes.Structure):
                 ("momentum_source_model", ctypes.c_int),
                 ("momentum_source", ctypes.c_double * 3),
                 ("volume_expansion", ctypes.c_double),
-                ("reference_temperature", ctypes.c_double)]
+                ("reference_temperature", ctypes.c_double),
+                ("diffusivity", ctypes.c_double * MAX_SPECIES),
+                ("species_source_model", ctypes.c_int * MAX_SPECIES),
+                ("species_source", (ctypes.c_double * 4) * MAX_SPECIES)]
 
 
 class CProblemDesc(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int), ("num_nodes", ctypes.c_int), ("num_elems", ctypes.c_int),
                 ("coords", ctypes.POINTER(ctypes.c_double)),
                 ("conn", ctypes.POINTER(ctypes.c_int)), ("energy", ctypes.c_int),
-                ("mat", CMaterial), ("num_bc", ctypes.c_int),
+                ("num_species", ctypes.c_int), ("mat", CMaterial), ("num_bc", ctypes.c_int),
                 ("bc_var", ctypes.POINTER(ctypes.c_int)),
                 ("bc_value", ctypes.POINTER(ctypes.c_double)),
                 ("bc_ptr", ctypes.POINTER(ctypes.c_int)),
                 ("bc_nodes", ctypes.POINTER(ctypes.c_int)),
                 ("pressure_datum_elem", ctypes.c_int),
                 ("pressure_datum_value", ctypes.c_double)]
+
+
+def c_material(mt: Material):
+    cm = CMaterial(mt.density, mt.viscosity_model, mt.viscosity, mt.mu0, mt.mu_inf, mt.lam,
+                   mt.aexp, mt.nexp, mt.heat_capacity, mt.conductivity,
+                   mt.momentum_source_model, (ctypes.c_double * 3)(*mt.momentum_source),
+                   mt.volume_expansion, mt.reference_temperature)
+    for w, d in enumerate(mt.diffusivity):
+        cm.diffusivity[w] = d
+    for w, (model, params) in enumerate(mt.species_source):
+        cm.species_source_model[w] = model
+        for k, v in enumerate(params):
+            cm.species_source[w][k] = v
+    return cm
 
 
 def make_desc(prob: Problem):
@@ -200,14 +230,11 @@ def make_desc(prob: Problem):
     if bc_var.size == 0:
         bc_var = np.zeros(1, np.int32)
         bc_val = np.zeros(1, np.float64)
-    mt = prob.material
-    cm = CMaterial(mt.density, mt.viscosity_model, mt.viscosity, mt.mu0, mt.mu_inf, mt.lam,
-                   mt.aexp, mt.nexp, mt.heat_capacity, mt.conductivity,
-                   mt.momentum_source_model, (ctypes.c_double * 3)(*mt.momentum_source),
-                   mt.volume_expansion, mt.reference_temperature)
+    cm = c_material(prob.material)
     P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
     d = CProblemDesc(m.dim, m.num_nodes, m.num_elems, P(coords, ctypes.c_double),
-                     P(conn, ctypes.c_int), 1 if prob.energy else 0, cm, len(prob.bcs),
+                     P(conn, ctypes.c_int), 1 if prob.energy else 0, int(prob.num_species),
+                     cm, len(prob.bcs),
                      P(bc_var, ctypes.c_int), P(bc_val, ctypes.c_double), P(bc_ptr, ctypes.c_int),
                      P(bc_nodes, ctypes.c_int), int(prob.pressure_datum[0]),
                      float(prob.pressure_datum[1]))
@@ -222,6 +249,9 @@ BFS2D_BCS = [(VAR_U1, 1, 0.0), (VAR_U2, 1, 0.0), (VAR_U1, 3, 0.0), (VAR_U2, 3, 0
              (VAR_U1, 5, 0.0), (VAR_U2, 5, 0.0), (VAR_U1, 6, 1.0), (VAR_U2, 6, 0.0)]
 HEATED3D_BCS = ([(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in (VAR_U1, VAR_U2, VAR_U3)]
                 + [(VAR_T, 1, 1.0), (VAR_T, 2, 0.0)])
+# heated box fed with species 0 at x = 0; T in [1, 2] keeps exp(-E/T) finite
+SPECIES3D_BCS = ([(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in (VAR_U1, VAR_U2, VAR_U3)]
+                 + [(VAR_T, 1, 2.0), (VAR_T, 2, 1.0), (VAR_Y(0), 1, 1.0), (VAR_Y(1), 1, 0.0)])
 
 
 def lid_cavity_2d(n, re=100.0, mesh=None):

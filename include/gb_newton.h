@@ -90,6 +90,14 @@ void *gb_stream(gb_ctx *ctx);
  * same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
 
+/* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
+ * (one cooperative launch per factor; each node waits on flags of the
+ * nodes it depends on, bounded, then publishes), 1 = level-scheduled
+ * sweeps replayed as a CUDA graph.  Both give the same result to
+ * rounding.  No counterpart in the reference (AztecOO's ILU solves are
+ * sequential). */
+int gb_set_triangular_solve(gb_ctx *ctx, int mode);
+
 /* Replaces the material of a context (same mesh, DOF map and pattern), as
  * update_parameterC does during continuation (src/ac_conti.c:755,
  * src/ac_update_parameter.c). */

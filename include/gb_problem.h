@@ -7,11 +7,18 @@
  *   - mesh: coordinates and QUAD9/HEX27 connectivity in the Exodus/Goma local
  *     node order (src/rf_shape.c:361 BIQUAD_QUAD, :1105 TRIQUAD_HEX);
  *   - equations: momentum (Q2), continuity (P1 discontinuous pressure,
- *     basis {1,s,t[,u]} in reference coordinates), optional energy (Q2);
+ *     basis {1,s,t[,u]} in reference coordinates), optional energy (Q2),
+ *     optional dilute species (Q2, "EQ = species_bulk", FICKIAN flux with
+ *     constant diffusivity, SPECIES_UNDEFINED_FORM; assemble_mass_transport
+ *     src/mm_fill_species.c:194, fickian_flux :12414);
  *   - material: density, Newtonian or Carreau-Yasuda viscosity
  *     (src/mm_viscosity.c:981), heat capacity, Fourier conductivity,
  *     CONSTANT or BOUSSINESQ momentum source (src/mm_std_models.c:125);
- *   - "BC = U|V|W|T NS <id> <value>" cards in deck order
+ *   - species sources: CONSTANT, or the Arrhenius rate of a USER model
+ *     (usr_species_source, src/user_mp.c:598, called from
+ *     src/mm_fill_species.c:10146):  S_w = nu k0 exp(-E/T) Y_s;
+ *   - "BC = U|V|W|T NS <id> <value>" and "BC = Y NS <id> <w> <value>"
+ *     cards in deck order
  *     (src/mm_input_bc.c), hard-set Dirichlet (src/bc_dirich.c:44), and the
  *     PRESSURE DATUM card (src/mm_input_bc.c:3215, src/mm_bc.c:388).
  */
@@ -29,6 +36,14 @@ extern "C" {
 #define GB_VAR_U3 2
 #define GB_VAR_T 3
 #define GB_VAR_P 9
+/* species w (the reference's MASS_FRACTION variable, sub-variable w) */
+#define GB_VAR_Y(w) (100 + (w))
+
+#define GB_MAX_SPECIES 4
+
+#define GB_SPECIES_SOURCE_NONE 0
+#define GB_SPECIES_SOURCE_CONSTANT 1
+#define GB_SPECIES_SOURCE_ARRHENIUS 2
 
 #define GB_VISC_NEWTONIAN 0
 #define GB_VISC_CARREAU 1
@@ -51,6 +66,12 @@ typedef struct gb_material {
   double momentum_source[3];     /* constant force or gravity vector */
   double volume_expansion;       /* "Volume Expansion = CONSTANT" (beta) */
   double reference_temperature;  /* "Reference Temperature = CONSTANT" */
+  /* species w < num_species of the problem */
+  double diffusivity[GB_MAX_SPECIES];        /* "Diffusivity = CONSTANT w D" */
+  int species_source_model[GB_MAX_SPECIES];  /* GB_SPECIES_SOURCE_* ("Species Source") */
+  /* CONSTANT: [0] = S.  ARRHENIUS: k0, E, nu, s with S_w = nu k0 exp(-E/T) Y_s
+   * (needs the energy equation, T > 0). */
+  double species_source[GB_MAX_SPECIES][4];
 } gb_material;
 
 typedef struct gb_problem_desc {
@@ -60,10 +81,12 @@ typedef struct gb_problem_desc {
   const double *coords; /* num_nodes * dim, interleaved (x, y[, z]) */
   const int *conn;      /* num_elems * (9 | 27), 0-based node ids */
   int energy;           /* 1: solve the energy equation (variable T) */
+  int num_species;      /* "Number of bulk species" (dilute: one equation each) */
   gb_material mat;
   /* Dirichlet cards, applied in order (a later card wins on a shared
    * node): card c sets variable bc_var[c] to bc_value[c] on the nodes
-   * bc_nodes[bc_ptr[c] .. bc_ptr[c+1]-1]. */
+   * bc_nodes[bc_ptr[c] .. bc_ptr[c+1]-1].  bc_var: GB_VAR_U1..U3, GB_VAR_T
+   * or GB_VAR_Y(w). */
   int num_bc;
   const int *bc_var;
   const double *bc_value;

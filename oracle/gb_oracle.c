@@ -16,7 +16,8 @@ struct orc_problem {
   int *conn;
   int nn;       /* nodes per element: 9 or 27 */
   int centroid; /* local index of the centroid node: 8 or 20 */
-  int nvn;      /* nodal fields per node: dim + energy */
+  int nvn;      /* nodal fields per node: dim + energy + species */
+  int ns;       /* species */
   int npres;    /* P1 pressure unknowns per element: dim + 1 */
   int nloc;     /* nvn * nn + npres */
   int N;
@@ -97,8 +98,10 @@ static int cmp_int(const void *a, const void *b) {
 }
 
 /* DOF numbering (src/mm_unknown_map.c:758, Index_Solution :5268): node by
- * node in node order; at every node the velocity components, then T, and
- * at an element's centroid node its dim+1 P1 pressure unknowns.
+ * node in node order; at every node the velocity components, then T, then
+ * the species Y_0.., and at an element's centroid node its dim+1 P1
+ * pressure unknowns (variable types in ascending order,
+ * include/rf_fem_const.h:174-200).
  * Sparsity (src/exo_conn.c:204 build_node_node, src/mm_fill_util.c:3229
  * find_MSR_problem_graph): unknown i couples with every unknown of every
  * node sharing an element with its node; a centroid node also couples with
@@ -111,7 +114,8 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
   const int dim = desc->dim, nnod = desc->num_nodes, ne = desc->num_elems;
   p->nn = dim == 2 ? 9 : 27;
   p->centroid = dim == 2 ? 8 : 20;
-  p->nvn = dim + (desc->energy ? 1 : 0);
+  p->ns = desc->num_species > 0 ? desc->num_species : 0;
+  p->nvn = dim + (desc->energy ? 1 : 0) + p->ns;
   p->npres = dim + 1;
   p->nloc = p->nvn * p->nn + p->npres;
   p->coords = (double *)malloc(sizeof(double) * (size_t)nnod * dim);
@@ -194,7 +198,8 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
   }
   /* Interaction mask (src/mm_unknown_map.c:1125 set_interaction_masks):
    * every equation couples with every variable except energy with
-   * pressure.  An unknown's variable: offset < nvn is a nodal field
+   * pressure (:1692; momentum :1226, species :1761 and continuity :2276 list
+   * pressure).  An unknown's variable: offset < nvn is a nodal field
    * (offset == dim is T when energy is on), offset >= nvn is pressure. */
   long off = 0;
   for (int pass = 0; pass < 2; pass++) {
@@ -228,9 +233,16 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
   p->dbc_val = (double *)calloc((size_t)p->N, sizeof(double));
   for (int i = 0; i < p->N; i++) p->dbc[i] = -1;
   for (int c = 0; c < desc->num_bc; c++) {
-    int var = desc->bc_var[c];
-    int offv = var == GB_VAR_T ? dim : var;
-    if (var == GB_VAR_T && !desc->energy) continue;
+    int var = desc->bc_var[c], offv;
+    if (var == GB_VAR_T) {
+      if (!desc->energy) continue;
+      offv = dim;
+    } else if (var >= GB_VAR_Y(0)) {
+      if (var - GB_VAR_Y(0) >= p->ns) continue;
+      offv = dim + (desc->energy ? 1 : 0) + (var - GB_VAR_Y(0));
+    } else {
+      offv = var;
+    }
     for (int q = desc->bc_ptr[c]; q < desc->bc_ptr[c + 1]; q++) {
       int n = desc->bc_nodes[q];
       p->dbc[p->fu[n] + offv] = c;
@@ -291,6 +303,9 @@ void orc_element_dofs(const orc_problem *p, int e, int *g) {
     for (int k = 0; k < nn; k++) g[a * nn + k] = p->fu[cn[k]] + a;
   if (p->d.energy)
     for (int k = 0; k < nn; k++) g[dim * nn + k] = p->fu[cn[k]] + dim;
+  const int oy = dim + (p->d.energy ? 1 : 0);
+  for (int w = 0; w < p->ns; w++)
+    for (int k = 0; k < nn; k++) g[(oy + w) * nn + k] = p->fu[cn[k]] + oy + w;
   for (int l = 0; l < p->npres; l++) g[p->nvn * nn + l] = p->fu[cn[p->centroid]] + p->nvn + l;
 }
 
@@ -308,24 +323,30 @@ void orc_element_dofs(const orc_problem *p, int e, int *g) {
  *   continuity R, J_c_v                       src/mm_fill_continuity.c:430-700
  *   energy R, J_e_T, J_e_v (Fourier flux)     src/mm_fill_energy.c:315-560,
  *                                             heat_flux :1629
+ *   species R, J_s_c, J_s_v, J_s_T (Galerkin, steady, SPECIES_UNDEFINED_FORM
+ *   so coeff_rho = 1; Fickian flux -D grad Y; CONSTANT or Arrhenius source)
+ *                                             src/mm_fill_species.c:194-1710,
+ *                                             fickian_flux :12414, sources
+ *                                             :10100-10190
  * then the hard-set Dirichlet rows of put_dirichlet_in_matrix
  * (src/bc_dirich.c:44): row zeroed, diagonal DIRICHLET_PENALTY = 1,
  * residual 0. */
 int orc_element(const orc_problem *p, int e, const double *x, double *Re, double *Je,
                 int apply_bc) {
   const int nn = p->nn, dim = p->d.dim, nloc = p->nloc, nq = dim == 2 ? 9 : 27;
-  const int en = p->d.energy, npr = p->npres;
-  const int oT = dim * nn, oP = p->nvn * nn;
+  const int en = p->d.energy, npr = p->npres, ns = p->ns;
+  const int oT = dim * nn, oP = p->nvn * nn, oY = (dim + (en ? 1 : 0)) * nn;
   const gb_material *m = &p->d.mat;
   const int *cn = p->conn + (size_t)e * nn;
   int status = 0;
-  double X[27][3], U[27][3], Tn[27], Pn[4];
-  int g[27 * 4 + 4];
+  double X[27][3], U[27][3], Tn[27], Pn[4], Yn[GB_MAX_SPECIES][27];
+  int g[27 * (4 + GB_MAX_SPECIES) + 4];
   orc_element_dofs(p, e, g);
   for (int k = 0; k < nn; k++) {
     for (int j = 0; j < dim; j++) X[k][j] = p->coords[(size_t)cn[k] * dim + j];
     for (int a = 0; a < dim; a++) U[k][a] = x[g[a * nn + k]];
     Tn[k] = en ? x[g[oT + k]] : 0.0;
+    for (int w = 0; w < ns; w++) Yn[w][k] = x[g[oY + w * nn + k]];
   }
   for (int l = 0; l < npr; l++) Pn[l] = x[g[oP + l]];
   memset(Re, 0, sizeof(double) * (size_t)nloc);
@@ -391,6 +412,12 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
       }
     }
     for (int l = 0; l < npr; l++) P += Pn[l] * psi[l];
+    double Y[GB_MAX_SPECIES] = {0}, gY[GB_MAX_SPECIES][3] = {{0}};
+    for (int w = 0; w < ns; w++)
+      for (int k = 0; k < nn; k++) {
+        Y[w] += Yn[w][k] * phi[k];
+        for (int pp = 0; pp < dim; pp++) gY[w][pp] += Yn[w][k] * gphi[k][pp];
+      }
     double divv = 0.0;
     for (int a = 0; a < dim; a++) divv += gv[a][a];
     double gam[3][3];
@@ -506,6 +533,49 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         }
       }
     }
+    /* species: source S_w and its sensitivities (usr_species_source /
+     * CONSTANT, src/mm_fill_species.c:10117,:10146-10190) */
+    for (int w = 0; w < ns; w++) {
+      double S = 0.0, dSdT = 0.0, dSdY[GB_MAX_SPECIES] = {0};
+      const double *sp = m->species_source[w];
+      if (m->species_source_model[w] == GB_SPECIES_SOURCE_CONSTANT) {
+        S = sp[0];
+      } else if (m->species_source_model[w] == GB_SPECIES_SOURCE_ARRHENIUS) {
+        const int src = (int)sp[3];
+        const double r = sp[0] * exp(-sp[1] / T);
+        S = sp[2] * r * Y[src];
+        dSdT = S * sp[1] / (T * T);
+        dSdY[src] = sp[2] * r;
+      }
+      const double D = m->diffusivity[w];
+      double vgY = 0.0;
+      for (int pp = 0; pp < dim; pp++) vgY += v[pp] * gY[w][pp];
+      for (int i = 0; i < nn; i++) {
+        const int ri = oY + w * nn + i;
+        /* advection -phi_i (v . grad Y_w), diffusion grad phi_i . (-D grad Y_w),
+         * source phi_i S_w (:572-665) */
+        double dif = 0.0;
+        for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * (-D * gY[w][pp]);
+        Re[ri] += -vgY * phi[i] * dA + dif * dA + S * phi[i] * dA;
+        for (int j = 0; j < nn; j++) {
+          double vgj = 0.0, gij = 0.0;
+          for (int pp = 0; pp < dim; pp++) {
+            vgj += v[pp] * gphi[j][pp];
+            gij += gphi[i][pp] * gphi[j][pp];
+          }
+          const double pij = phi[i] * phi[j] * dA;
+          /* J_s_c (:760-904): advection and diffusion on the diagonal species,
+           * the source on every species it depends on */
+          JE(ri, oY + w * nn + j) += -phi[i] * vgj * dA - D * gij * dA;
+          for (int w1 = 0; w1 < ns; w1++)
+            if (dSdY[w1] != 0.0) JE(ri, oY + w1 * nn + j) += dSdY[w1] * pij;
+          /* J_s_v (:906-1000): d(v . grad Y_w)/d v_b = phi_j dY_w/dx_b */
+          for (int b = 0; b < dim; b++) JE(ri, b * nn + j) += -gY[w][b] * pij;
+          /* J_s_T: source only (constant diffusivity) */
+          if (en && dSdT != 0.0) JE(ri, oT + j) += dSdT * pij;
+        }
+      }
+    }
   }
   if (apply_bc) {
     for (int r = 0; r < nloc; r++) {
@@ -525,7 +595,7 @@ int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a,
   const int nloc = p->nloc;
   double *Re = (double *)malloc(sizeof(double) * (size_t)nloc);
   double *Je = (double *)malloc(sizeof(double) * (size_t)nloc * nloc);
-  int g[27 * 4 + 4];
+  int g[27 * (4 + GB_MAX_SPECIES) + 4];
   int status = 0;
   for (int e = e0; e < e1; e++) {
     if (orc_element(p, e, x, Re, Je, 1) != 0) status = -1;

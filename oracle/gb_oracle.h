@@ -5,7 +5,8 @@
  * src/exo_conn.c:204, src/mm_fill_util.c:3229), element residual and
  * analytic Jacobian (src/mm_fill.c:317 matrix_fill with assemble_momentum
  * src/mm_fill_momentum.c:100, assemble_continuity
- * src/mm_fill_continuity.c:119, assemble_energy src/mm_fill_energy.c:109),
+ * src/mm_fill_continuity.c:119, assemble_energy src/mm_fill_energy.c:109,
+ * assemble_mass_transport src/mm_fill_species.c:194),
  * hard-set Dirichlet rows (src/bc_dirich.c:44), the MSR scatter
  * (src/mm_fill.c:5175), row-sum scaling (src/sl_matrix_util.c:506) and the
  * Newton loop (src/mm_sol_nonlinear.c:1108).  It is pinned against golden
@@ -43,7 +44,8 @@ int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a,
 /* Element-level residual and Jacobian (before the Dirichlet rows are
  * applied when apply_bc == 0), in the oracle's local DOF order:
  * velocity component a of local node k at a*nn + k, temperature at
- * dim*nn + k, pressure mode l at (dim+energy)*nn + l. */
+ * dim*nn + k, species w at (dim+energy+w)*nn + k, pressure mode l at
+ * (dim+energy+species)*nn + l. */
 int orc_element(const orc_problem *p, int e, const double *x, double *Re, double *Je,
                 int apply_bc);
 int orc_local_size(const orc_problem *p);

@@ -4,7 +4,8 @@
  * reference's Newton loop (src/mm_sol_nonlinear.c:1279) makes to
  * matrix_fill_full (src/mm_fill.c:158) passes through here.  Environment:
  *   GB_REF_X_IN   raw little-endian float64 file; when set, x[] is replaced
- *                 by its contents before assembly (a seeded state)
+ *                 by its contents before the first assembly (a seeded state,
+ *                 or the initial guess of a Newton solve)
  *   GB_REF_DUMP   path prefix; the first assembly writes <prefix>.ija
  *                 (int32, MSR bindx), <prefix>.a (float64, MSR values),
  *                 <prefix>.R and <prefix>.x (float64, length N)
@@ -49,7 +50,7 @@ int __wrap_matrix_fill_full(struct GomaLinearSolverData *ams, double x[], double
                             dbl *estifm) {
   const int N = ams->npu;
   const char *xin = getenv("GB_REF_X_IN");
-  if (xin) {
+  if (xin && g_calls == 0) {
     FILE *f = fopen(xin, "rb");
     if (!f || fread(x, sizeof(double), (size_t)N, f) != (size_t)N) {
       fprintf(stderr, "harness: cannot read %d doubles from %s\n", N, xin);

@@ -46,7 +46,17 @@ CASES = {
                                   visc=("carreau", 2.0, 0.1, 0.5, 2.0, 0.6),
                                   bc="cube_heated", datum=True, mode="assemble", seed=6,
                                   ra_pr=500.0),
-    # converged Newton solutions from a zero initial guess
+    # energy + two dilute species with an Arrhenius source (configuration 5 physics)
+    "box3d_2x2x2_species": dict(mesh="hex27 2 2 2 1 1 1 0.1 13", phys="nsty", rho=1.0,
+                                visc=("newtonian", 0.71), bc="cube_species", datum=True,
+                                mode="assemble", seed=7, ra_pr=710.0, nspec=2,
+                                diff=(0.05, 0.02), arrhenius=(3.0, 1.5), T_range=(1.0, 2.0)),
+    # converged Newton solutions from a zero initial guess (T0: from that
+    # temperature instead of zero)
+    "box3d_2x2x2_species_solve": dict(mesh="hex27 2 2 2 1 1 1", phys="nsty", rho=1.0,
+                                      visc=("newtonian", 0.71), bc="cube_species", datum=True,
+                                      mode="solve", tol=1e-12, ra_pr=710.0, nspec=2,
+                                      diff=(0.05, 0.02), arrhenius=(3.0, 1.5), T0=1.5),
     "cav2d_4x4_solve": dict(mesh="quad9 4 4 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
                             bc="cavity2d", datum=True, mode="solve", tol=1e-12),
     "cav2d_8x8_solve": dict(mesh="quad9 8 8 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
@@ -67,6 +77,9 @@ BCS = {
               ("V", 5, 0.0), ("U", 6, 1.0), ("V", 6, 0.0)],
     "cube_heated": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
     + [("T", 1, 1.0), ("T", 2, 0.0)],
+    # heated box with two species fed at x = 0: T in [1, 2] keeps exp(-E/T) finite
+    "cube_species": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
+    + [("T", 1, 2.0), ("T", 2, 1.0), ("Y0", 1, 1.0), ("Y1", 1, 0.0)],
 }
 
 
@@ -102,7 +115,10 @@ def deck_text(case):
     for var, ns, val in BCS[case["bc"]]:
         if dim == 2 and var == "W":
             continue
-        lines.append("BC = %s NS %d %.17g" % (var, ns, val))
+        if var.startswith("Y"):      # species w: "BC = Y NS id w value"
+            lines.append("BC = Y NS %d %d %.17g" % (ns, int(var[1:]), val))
+        else:
+            lines.append("BC = %s NS %d %.17g" % (var, ns, val))
     lines.append("END OF BC")
     if case["datum"]:
         lines += ["", "PRESSURE DATUM = 0 0."]
@@ -114,13 +130,15 @@ def deck_text(case):
         "Coordinate System = CARTESIAN",
         "Element Mapping = isoparametric",
         "Mesh Motion = ARBITRARY",
-        "Number of bulk species = 0",
+        "Number of bulk species = %d" % case.get("nspec", 0),
         "Number of EQ = -1",
     ]
     for a in range(dim):
         lines.append("EQ = momentum%d Q2 U%d Q2 0. 1. 1. 1. 1. 0." % (a + 1, a + 1))
-    if case["phys"] == "nst":
+    if case["phys"] in ("nst", "nsty"):
         lines.append("EQ = energy Q2 T Q2 0. 1. 1. 1. 1.")
+    if case["phys"] == "nsty":
+        lines.append("EQ = species_bulk Q2 Y Q2 0. 1. 1. 1. 1.")
     lines += ["EQ = continuity P1 P P1 1. 0.", "END OF EQ", "END OF MAT", "",
               "Post Processing Specifications", ""]
     # the BC count line must match what was written
@@ -139,7 +157,7 @@ def mat_text(case):
               "Power Law Exponent = CONSTANT %.17g" % nexp,
               "High Rate Viscosity = CONSTANT %.17g" % muinf,
               "Time Constant = CONSTANT %.17g" % lam, "Aexp = CONSTANT %.17g" % aexp]
-    if case["phys"] == "nst":
+    if case["phys"] in ("nst", "nsty"):
         src = "Navier-Stokes Source = BOUSSINESQ 0. 0. %.17g" % (-case["ra_pr"])
     else:
         src = "Navier-Stokes Source = CONSTANT 0. 0. 0."
@@ -155,10 +173,45 @@ def mat_text(case):
         "---Electrical Properties", "Electrical Conductivity = CONSTANT 0.", "",
         "---Microstructure Properties", "Media Type = CONTINUOUS", "Porosity = CONSTANT 0.",
         "Permeability = CONSTANT 0.", "",
-        "---Species Properties", "Diffusion Constitutive Equation = NONE", "",
+        ] + species_props(case) + [
         "---Source Terms", src, "Solid Body Source = CONSTANT 0. 0. 0.",
-        "Mass Source = CONSTANT 0.", "Heat Source = CONSTANT 0.", "Current Source = CONSTANT 0.",
-        ""])
+        "Mass Source = CONSTANT 0.", "Heat Source = CONSTANT 0."] + species_sources(case) + [
+        "Current Source = CONSTANT 0.", ""])
+
+
+def species_props(case):
+    ns = case.get("nspec", 0)
+    if ns == 0:
+        return ["---Species Properties", "Diffusion Constitutive Equation = NONE", ""]
+    out = ["---Species Properties", "Diffusion Constitutive Equation = FICKIAN"]
+    # the reader takes one group of cards per species, in species order
+    for w in range(ns):
+        out.append("Diffusivity = CONSTANT %d %.17g" % (w, case["diff"][w]))
+        out += ["%s = CONSTANT %d 0." % (card, w)
+                for card in ("Latent Heat Vaporization", "Latent Heat Fusion", "Vapor Pressure",
+                             "Species Volume Expansion", "Reference Concentration")]
+    return out + [""]
+
+
+def species_sources(case):
+    """Arrhenius: S_w = nu_w k0 exp(-E/T) Y_0 (USER model, oracle/ref_shim/user_species.c)."""
+    ns = case.get("nspec", 0)
+    out = []
+    for w in range(ns):
+        k0, E = case["arrhenius"]
+        nu = -1.0 if w == 0 else 1.0
+        out.append("Species Source = USER %d %.17g %.17g %.17g 0" % (w, k0, E, nu))
+    return out
+
+
+def temperature_unknowns(case):
+    """Indices of the T unknowns (offset dim at every node, node-major DOF map)."""
+    sys.path.insert(0, REPO)
+    import oracle
+    from tests import golden_cases as gc
+    prob = gc.problem_from_case(case)
+    fu = oracle.Oracle(prob).first_unknown(prob.mesh.num_nodes)
+    return fu[:-1] + prob.dim
 
 
 def run_case(name, case, outdir):
@@ -178,6 +231,10 @@ def run_case(name, case, outdir):
             n = np.fromfile(os.path.join(tmp, "d.R")).size
             rng = np.random.default_rng(case["seed"])
             x = rng.uniform(-1.0, 1.0, n)
+            if "T_range" in case:
+                # temperatures inside a range (an Arrhenius rate needs T > 0)
+                lo, hi = case["T_range"]
+                x[temperature_unknowns(case)] = rng.uniform(lo, hi, len(temperature_unknowns(case)))
             x.astype("<f8").tofile(os.path.join(tmp, "xin.bin"))
             env2 = dict(env1, GB_REF_X_IN=os.path.join(tmp, "xin.bin"))
             subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env2, check=True,
@@ -185,6 +242,19 @@ def run_case(name, case, outdir):
             rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
             assert np.array_equal(rec["x"], x)
         else:
+            if "T0" in case:
+                # initial guess: Dirichlet values, T0 at the other temperatures
+                # (zero everywhere else), as the package builds it
+                sys.path.insert(0, REPO)
+                import oracle
+                from tests import golden_cases as gc
+                o = oracle.Oracle(gc.problem_from_case(case))
+                x0 = np.zeros(o.N)
+                x0[temperature_unknowns(case)] = case["T0"]
+                x0 = o.dirichlet_init(x0)
+                x0.astype("<f8").tofile(os.path.join(tmp, "x0.bin"))
+                env = dict(env, GB_REF_X_IN=os.path.join(tmp, "x0.bin"))
+                rec["x0"] = x0
             p = subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env, check=True,
                                stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
             if "converged SS!" not in p.stdout:

@@ -34,7 +34,7 @@ def problem_from_case(case):
     else:
         mat = pb.Material(density=case["rho"], viscosity_model=pb.VISC_CARREAU, mu0=v[1],
                           mu_inf=v[2], lam=v[3], aexp=v[4], nexp=v[5])
-    energy = case["phys"] == "nst"
+    energy = case["phys"] in ("nst", "nsty")
     if energy:
         mat.momentum_source_model = pb.SOURCE_BOUSSINESQ
         mat.momentum_source = (0.0, 0.0, -case["ra_pr"])
@@ -42,9 +42,17 @@ def problem_from_case(case):
         mat.reference_temperature = 0.5
         mat.heat_capacity = 1.0
         mat.conductivity = 1.0
+    ns = case.get("nspec", 0)
+    if ns:
+        # Arrhenius S_w = nu_w k0 exp(-E/T) Y_0, nu = -1 for species 0, +1 after
+        k0, E = case["arrhenius"]
+        mat.diffusivity = tuple(case["diff"])
+        mat.species_source = tuple((pb.SPECIES_SOURCE_ARRHENIUS, (k0, E, -1.0 if w == 0 else 1.0, 0))
+                                   for w in range(ns))
     bcs = {"cavity2d": pb.CAVITY2D_BCS, "bfs2d": pb.BFS2D_BCS,
-           "cube_heated": pb.HEATED3D_BCS}[case["bc"]]
-    return pb.Problem(mesh, mat, energy, list(bcs), (0, 0.0) if case["datum"] else (-1, 0.0))
+           "cube_heated": pb.HEATED3D_BCS, "cube_species": pb.SPECIES3D_BCS}[case["bc"]]
+    return pb.Problem(mesh, mat, energy, list(bcs), (0, 0.0) if case["datum"] else (-1, 0.0),
+                      num_species=ns)
 
 
 def msr_row_scaled_error(ija, a, ref):

@@ -18,7 +18,8 @@ TOL_X = 1e-8
 def test_gpu_newton_matches_reference_solution(name, fp32_inner):
     g, case = gc.load(name)
     gn = GomaNewton(gc.problem_from_case(case))
-    x, conv, st = gn.solve_nonlinear_problem(residual_tol=1e-11, linear_tol=1e-10,
+    x0 = g["x0"] if "x0" in g else None
+    x, conv, st = gn.solve_nonlinear_problem(x0, residual_tol=1e-11, linear_tol=1e-10,
                                              fp32_inner=fp32_inner, max_newton=30)
     assert conv, st
     xc = g["x_converged"]
@@ -56,3 +57,26 @@ def test_gpu_newton_larger_cavity_against_oracle():
                                                  fp32_inner=fp32)
         assert conv
         assert np.abs(x - xo).max() <= TOL_X * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("case", ["cavity2d_12", "bouss3d_4"])
+def test_gpu_triangular_solve_modes_agree(case):
+    """Sync-free ILU(0) sweeps and the level-scheduled graph do the same
+    per-row arithmetic in the same order, so a fixed number of GMRES
+    iterations gives the same correction either way."""
+    prob = (pb.lid_cavity_2d(12, 100.0) if case.startswith("cavity")
+            else pb.boussinesq_cube_3d(4, 1e4, 0.71))
+    gn = GomaNewton(prob)
+    o = oracle.Oracle(prob)
+    x = o.dirichlet_init(np.random.default_rng(1).uniform(-0.5, 0.5, o.N))
+    R, a = gn.matrix_fill_full(x)
+    a_s, R_s, _ = o.row_sum_scale(a, R)
+    out = []
+    for mode in (1, 0, 0):
+        gn.set_triangular_solve(mode)
+        dx, its, rr = gn.linear_solve(a_s, R_s, linear_tol=1e-30, max_linear_its=40)
+        assert its == 40
+        out.append(dx)
+    scale = np.abs(out[0]).max()
+    assert np.abs(out[1] - out[0]).max() <= 1e-12 * scale
+    assert np.abs(out[2] - out[1]).max() <= 1e-12 * scale
