@@ -137,11 +137,12 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
                       % (done, nel_block, dt)}
 
 
-def time_to_solve(nel, ra_path=(1e4, 3e4, 1e5), tol=1e-10):
-    """Wall-clock time to the converged Boussinesq cube at Ra = ra_path[-1],
-    by Ra continuation from rest: plain FP64 Newton (ILU(0)-GMRES in FP64,
-    zeroth-order predictor, the reference's ALC_ZEROTH) against the learned
-    predictor + FP32-inner GMRES with FP64 refinement.  Returns a dict with
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10):
+    """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
+    continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
+    FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
+    reference's ALC_ZEROTH) against the learned predictor (zeroth-order
+    fallback) + FP32-inner GMRES with FP64 refinement.  Returns a dict with
     both times, Newton/Krylov counts and the relative difference of the two
     converged solutions."""
     import torch
@@ -154,24 +155,25 @@ def time_to_solve(nel, ra_path=(1e4, 3e4, 1e5), tol=1e-10):
         m.momentum_source = (0.0, 0.0, -ra * PR)
         gn.set_material(m)
 
-    out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra continuation %s, Pr=%g, scaled |R| < %g"
-           % (nel, list(ra_path), PR, tol)}
+    out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
+                       "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol)}
     sols = {}
     for mode in ("plain_fp64", "learned_fp32"):
-        prob = pb.boussinesq_cube_3d(nel, ra_path[0], PR)
+        prob = pb.boussinesq_cube_3d(nel, ra0, PR)
         gn = GomaNewton(prob)
         opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
                     fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3)
         torch.cuda.synchronize()
         t = time.perf_counter()
-        recs, x = continuation(gn, ra_path[0], ra_path[-1], len(ra_path) - 1,
+        recs, x = continuation(gn, ra0, ra1, nsteps,
                                predictor="learned" if mode == "learned_fp32" else "zeroth",
-                               set_param=set_ra, newton_opts=opts,
+                               set_param=set_ra, newton_opts=opts, spacing="log",
                                learned_opts=dict(steps=300, batch=4096, lr=2e-3))
         torch.cuda.synchronize()
         dt = time.perf_counter() - t
         sols[mode] = x
         out[mode] = {"seconds": dt, "newton_its": sum(r["newton_its"] for r in recs),
+                     "linear_its": sum(r.get("linear_its", 0) for r in recs[1:]),
                      "guesses": [r["guess"] for r in recs[1:]]}
         del gn
     a, b = sols["plain_fp64"], sols["learned_fp32"]
@@ -214,6 +216,8 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--path", type=int, default=0,
+                    help="element kernel: 0 automatic, 1 scalar FP64, 2 FP64 tensor pipe (DMMA)")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
     args = ap.parse_args()
@@ -237,6 +241,9 @@ def main():
 
     prob = pb.boussinesq_cube_3d(nel, RA, PR)
     gn = GomaNewton(prob)
+    gn.set_assembly_path(args.path)
+    kernel_name = ("assemble_tc_kernel<energy> (FP64 DMMA)" if args.path == 2
+                   else "assemble_kernel<3,energy> (scalar FP64)")
     L = gn._L
     N, nnz, msr_len = gn.N, gn.nnz, gn.msr_len
     x_host = gn.dirichlet_init(np.random.default_rng(11).uniform(-1.0, 1.0, N))
@@ -329,7 +336,7 @@ def main():
     roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": dmma.value,
                 "unit": "TFLOP/s", "frac": achieved_tf / dmma.value,
                 "traffic": None,
-                "kernel": "assemble_kernel<3,energy> (one colour, %d elements)" % elems_per_launch,
+                "kernel": "%s, one colour, %d elements" % (kernel_name, elems_per_launch),
                 "launch_ms": per_launch_ms,
                 "flop_per_element": flop_el,
                 "peak_source": "FP64 mma.sync m8n8k4 (DMMA) throughput measured in-process on "
@@ -343,7 +350,8 @@ def main():
             "steps": args.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(workload_config(nel), unknowns=N, csr_nnz=nnz,
-                           colors=gn.num_colors, parallelism="replicas"),
+                           colors=gn.num_colors, parallelism="replicas",
+                           element_kernel=kernel_name),
             "clocks": clk.summary(), "e2e": e2e, "roofline": roofline,
             "gpu_launches": int(gn.num_colors * args.steps)}
     if rank == 0 and not args.no_cpu:

@@ -11,9 +11,9 @@ number) sweep of a steady problem:
   :3753, :3796);
 - ``learned``: a 3 x 256 tanh network (GPU, FP32, trained online by the
   library's own kernels on every converged solution) predicts the fields
-  from (x, y, lambda); its guess is used only when its FP64 scaled residual
-  is smaller than the fallback's (``first`` when available, else
-  ``zeroth``), and the Newton solve always decides the answer.
+  from (x, y[, z], lambda); its guess is used only when its FP64 scaled
+  residual is smaller than the fallback's (``zeroth``; ``first`` with
+  ``learned+first``), and the Newton solve always decides the answer.
 
 On a failed Newton solve the step is halved and re-predicted
 (src/ac_conti.c:986-1045).
@@ -175,56 +175,84 @@ def tangent(gn, x, lam, set_param, rel=1e-6, **solve_opts):
     return sens.cpu().numpy()
 
 
+PREDICTORS = ("zeroth", "first", "learned", "learned+first")
+
+
 def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=_set_density,
-                 newton_opts=None, learned_opts=None, verbose=False):
-    """Sweep lambda from lam0 to lam1 in nsteps uniform steps.  Returns a list
-    of per-step records (lambda, guess used, guess residual, Newton
+                 newton_opts=None, learned_opts=None, spacing="linear", max_halvings=4,
+                 verbose=False):
+    """Sweep lambda from lam0 to lam1 in nsteps steps (uniform in lambda, or
+    in log lambda with spacing="log").  predictor: "zeroth" (ALC_ZEROTH),
+    "first" (ALC_FIRST), "learned" (the network, zeroth-order fallback) or
+    "learned+first" (the network, first-order fallback).  A step whose
+    Newton solve fails is halved and re-predicted from the last converged
+    point, at most max_halvings times (src/ac_conti.c:986-1045).  Returns a
+    list of per-step records (lambda, guess used, guess residuals, Newton
     iterations, wall time) and the final solution."""
+    if predictor not in PREDICTORS:
+        raise ValueError("predictor must be one of %s" % (PREDICTORS,))
     newton_opts = dict(newton_opts or {})
-    lams = np.linspace(lam0, lam1, nsteps + 1)
+    if spacing == "log":
+        lams = list(np.exp(np.linspace(math.log(lam0), math.log(lam1), nsteps + 1)))
+    else:
+        lams = list(np.linspace(lam0, lam1, nsteps + 1))
     set_param(gn, lams[0])
+    t0 = time.perf_counter()
     x, conv, st = gn.solve_nonlinear_problem(x0, **newton_opts)
     if not conv:
         raise RuntimeError("first continuation step did not converge")
     records = [{"lam": float(lams[0]), "guess": "initial", "newton_its": st["newton_its"],
-                "guess_residual": None, "wall_s": st["total_ms"] * 1e-3}]
+                "guess_residual": None, "wall_s": time.perf_counter() - t0}]
+    learned = predictor.startswith("learned")
+    first = predictor in ("first", "learned+first")
     lp = None
-    if predictor == "learned":
-        lp = LearnedPredictor(gn, (lam0, lam1), **(learned_opts or {}))
+    if learned:
+        lp = LearnedPredictor(gn, (min(lam0, lam1), max(lam0, lam1)), **(learned_opts or {}))
         lp.add(lams[0], x)
         lp.train(seed=0)
-    x_old, lam_old, sens = x, lams[0], None
-    for k in range(1, len(lams)):
-        lam = lams[k]
+    lin_keys = ("linear_tol", "fp32_inner", "krylov_dim", "max_linear_its", "inner_tol")
+    x_old, lam_old = x, lams[0]
+    targets = lams[1:]
+    k = 0
+    while k < len(targets):
+        lam = targets[k]
         t0 = time.perf_counter()
-        cands = {"zeroth": x_old}
-        if predictor in ("first", "learned"):
-            sens = tangent(gn, x_old, lam_old, set_param, **{
-                k2: v for k2, v in newton_opts.items() if k2 in ("linear_tol", "fp32_inner",
-                                                                 "krylov_dim", "max_linear_its")})
-            cands["first"] = x_old + (lam - lam_old) * sens
-        set_param(gn, lam)
-        if predictor == "learned" and lp.trained:
-            cands["learned"] = gn.dirichlet_init(lp.predict(lam))
-        res = {}
-        if len(cands) > 1:
-            for name, xc in cands.items():
-                res[name] = scaled_residual_l2(gn, xc)
-            choice = min(res, key=res.get)
-        else:
-            choice = "zeroth"
-        guess = gn.dirichlet_init(cands[choice])
-        x, conv, st = gn.solve_nonlinear_problem(guess, **newton_opts)
-        if not conv:
-            raise RuntimeError("continuation step at lambda=%g did not converge" % lam)
+        halvings = 0
+        while True:
+            cands = {"zeroth": x_old}
+            if first:
+                sens = tangent(gn, x_old, lam_old, set_param,
+                               **{k2: v for k2, v in newton_opts.items() if k2 in lin_keys})
+                cands["first"] = x_old + (lam - lam_old) * sens
+            set_param(gn, lam)
+            if learned and lp.trained:
+                cands["learned"] = gn.dirichlet_init(lp.predict(lam))
+            res = {}
+            if len(cands) > 1:
+                for name, xc in cands.items():
+                    res[name] = scaled_residual_l2(gn, xc)
+                choice = min(res, key=lambda n: (res[n] if np.isfinite(res[n]) else np.inf))
+            else:
+                choice = next(iter(cands))
+            guess = gn.dirichlet_init(cands[choice])
+            x, conv, st = gn.solve_nonlinear_problem(guess, **newton_opts)
+            if conv:
+                break
+            if halvings >= max_halvings:
+                raise RuntimeError("continuation step at lambda=%g did not converge" % lam)
+            halvings += 1
+            lam = 0.5 * (lam_old + lam)
+            targets.insert(k, lam)
         if lp is not None:
             lp.add(lam, x)
-            if k + 1 < len(lams):
-                lp.train(seed=k)
+            if k + 1 < len(targets):
+                lp.train(seed=len(records))
         wall = time.perf_counter() - t0
         records.append({"lam": float(lam), "guess": choice, "newton_its": st["newton_its"],
-                        "guess_residual": res.get(choice), "candidates": res, "wall_s": wall})
+                        "linear_its": st["linear_its"], "guess_residual": res.get(choice),
+                        "candidates": res, "halvings": halvings, "wall_s": wall})
         if verbose:
             print(records[-1])
         x_old, lam_old = x, lam
+        k += 1
     return records, x

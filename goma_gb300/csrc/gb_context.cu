@@ -224,7 +224,7 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   AsmArgs a = args(x, R, vals);
   const int ncol = (int)L.color_ptr.size() - 1;
   if (timing) cudaEventRecord(ev_k0, st);
-  const bool tc = L.dim == 3 && vals != nullptr && path == 0;
+  const bool tc = L.dim == 3 && vals != nullptr && path == 2;
   if (tc && tc_grid == 0) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -396,7 +396,8 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 }
 
 int gb_set_assembly_path(gb_ctx *ctx, int path) {
-  if (!ctx || path < 0 || path > 1) return fail("path must be 0 (auto) or 1 (scalar FP64)");
+  if (!ctx || path < 0 || path > 2)
+    return fail("path must be 0 (auto), 1 (scalar FP64) or 2 (FP64 tensor pipe)");
   ctx->c.path = path;
   return 0;
 }

@@ -21,7 +21,7 @@ struct Context {
   Layout L;
   MaterialDev mat{};
   bool carreau = false;
-  int path = 0;        // element kernel: 0 auto (DMMA in 3-D), 1 scalar FP64
+  int path = 0;        // element kernel: 0 auto (scalar), 1 scalar FP64, 2 DMMA in 3-D
   int tc_grid = 0;     // persistent grid of the DMMA kernel
   int trsv = 0;        // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph
   cudaStream_t stream = nullptr;

@@ -257,4 +257,29 @@ int gb_linear_solve(gb_ctx *ctx, const double *a_msr, const double *rhs, double 
   return rc;
 }
 
+int gb_ilu0_factors(gb_ctx *ctx, const double *a_msr, int fp32, double *lu_csr) {
+  if (!ctx || !a_msr || !lu_csr) return gb::fail("NULL argument");
+  Context &c = ctx->c;
+  const int N = c.L.N;
+  const int64_t len = gb::layout_msr_length(c.L), nnz = c.L.nnz;
+  if (gb::ensure_solver(&c, 30)) return -1;
+  double *d_msr = nullptr, *d_vals = nullptr;
+  cudaError_t e = cudaMalloc(&d_msr, sizeof(double) * len);
+  if (e == cudaSuccess) e = cudaMalloc(&d_vals, sizeof(double) * nnz);
+  int rc = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_msr, a_msr, sizeof(double) * len, cudaMemcpyHostToDevice, c.stream);
+  if (e != cudaSuccess) {
+    rc = gb::cuda_fail(e, "factor upload");
+  } else {
+    gb::msr_to_csr_kernel<<<(int)(((int64_t)N * 32 + 255) / 256), 256, 0, c.stream>>>(
+        N, c.d_rowptr, c.d_colidx, d_msr, d_vals);
+    rc = c.solver->factor(d_vals, fp32 != 0, c.stream);
+    if (rc == 0) rc = c.solver->copy_factors(lu_csr, fp32 != 0, c.stream);
+  }
+  cudaFree(d_msr);
+  cudaFree(d_vals);
+  return rc;
+}
+
 }  // extern "C"

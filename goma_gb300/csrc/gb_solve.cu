@@ -280,9 +280,11 @@ __global__ void __launch_bounds__(256)
     ilu0_block_kernel(const int *__restrict__ nodes, IluArgs g, const double *__restrict__ A,
                       T *__restrict__ lu) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  T *blk = reinterpret_cast<T *>(sm_raw);                      // [maxnr][lmax]
-  T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [16][16]
-  int *snb = reinterpret_cast<int *>(lnm + kMaxNodeDofs * kMaxNodeDofs);  // [maxnb]
+  int64_t *srow = reinterpret_cast<int64_t *>(sm_raw);          // [16] row starts of node m
+  T *blk = reinterpret_cast<T *>(srow + kMaxNodeDofs);           // [maxnr][lmax]
+  T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [16][16] L_nm
+  T *umm = lnm + kMaxNodeDofs * kMaxNodeDofs;                    // [16][16] U_mm
+  int *snb = reinterpret_cast<int *>(umm + kMaxNodeDofs * kMaxNodeDofs);  // [maxnb]
   int *soff = snb + g.maxnb;
   int *sndof = soff + g.maxnb;
   int *tmap = sndof + g.maxnb;                                   // [maxnb]
@@ -352,44 +354,54 @@ __global__ void __launch_bounds__(256)
       }
       mself = lo;
     }
-    // step 1: L_nm = A_nm U_mm^-1, one thread per row
+    // U_mm and node m's row starts into shared memory (one round of loads)
+    if (tid < nm) srow[tid] = g.rowptr[fm + tid];
+    for (int w = tid; w < nm * nm; w += nt) {
+      const int dk = w / nm, d2 = w - dk * nm;
+      const bool rowkT = dk == Tr;
+      T u = (T)0;
+      if (d2 >= dk && !(rowkT && d2 >= g.nvn))
+        u = lu[g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + mself] : g.nbr_off[mb + mself]) + d2];
+      umm[dk * kMaxNodeDofs + d2] = u;
+    }
+    __syncthreads();
+    // step 1: L_nm = A_nm U_mm^-1, one thread per row, from shared memory
     if (tid < nr) {
       const int r = tid;
+      T *br = blk + (size_t)r * g.lmax + cm;
       for (int dk = 0; dk < nm; dk++) {
-        const bool rowkT = dk == Tr;
         if (r == Tr && dk >= g.nvn) {
           lnm[r * kMaxNodeDofs + dk] = (T)0;
           continue;
         }
-        const int64_t rk = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + mself] : g.nbr_off[mb + mself]);
-        const T l = blk[r * g.lmax + cm + dk] / (T)lu[rk + dk];
-        blk[r * g.lmax + cm + dk] = l;
+        const T l = br[dk] / umm[dk * kMaxNodeDofs + dk];
+        br[dk] = l;
         lnm[r * kMaxNodeDofs + dk] = l;
         for (int d2 = dk + 1; d2 < nm; d2++) {
           if (r == Tr && d2 >= g.nvn) continue;
-          if (rowkT && d2 >= g.nvn) continue;
-          blk[r * g.lmax + cm + d2] -= l * (T)lu[rk + d2];
+          br[d2] -= l * umm[dk * kMaxNodeDofs + d2];  // zero where U_mm has no entry
         }
       }
     }
     __syncthreads();
-    // step 2: A_nq -= L_nm U_mq
-    for (int t = 0; t < mnb; t++) {
+    // step 2: A_nq -= L_nm U_mq for every shared neighbour q > m, all
+    // (q, row, column) targets at once: f = (t, r, d), d fastest so that a
+    // warp reads consecutive entries of U_mq
+    const int per_t = nr * kMaxNodeDofs;
+    for (int f = tid; f < mnb * per_t; f += nt) {
+      const int t = f / per_t, rem = f - t * per_t;
+      const int r = rem / kMaxNodeDofs, d = rem - r * kMaxNodeDofs;
       const int slot = tmap[t];
-      if (slot < 0) continue;
-      const int nq = sndof[slot], cq = soff[slot];
-      for (int w = tid; w < nq * nr; w += nt) {
-        const int d = w / nr, r = w - d * nr;
-        if (r == Tr && d >= g.nvn) continue;
-        T acc = (T)0;
-        for (int dk = 0; dk < nm; dk++) {
-          const bool rowkT = dk == Tr;
-          if (rowkT && d >= g.nvn) continue;
-          const int64_t pos = g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + t] : g.nbr_off[mb + t]) + d;
-          acc += lnm[r * kMaxNodeDofs + dk] * (T)lu[pos];
-        }
-        blk[r * g.lmax + cq + d] -= acc;
+      if (slot < 0 || d >= sndof[slot]) continue;
+      if (r == Tr && d >= g.nvn) continue;
+      const int off = g.nbr_off[mb + t], offT = g.nbr_offT[mb + t];
+      T acc = (T)0;
+      for (int dk = 0; dk < nm; dk++) {
+        const bool rowkT = dk == Tr;
+        if (rowkT && d >= g.nvn) continue;
+        acc += lnm[r * kMaxNodeDofs + dk] * (T)lu[srow[dk] + (rowkT ? offT : off) + d];
       }
+      blk[(size_t)r * g.lmax + soff[slot] + d] -= acc;
     }
     __syncthreads();
   }
@@ -487,18 +499,32 @@ __global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
   }
 }
 
-// Sync-free triangular solves: one cooperative launch per sweep.  Warps take
-// nodes in elimination order from an atomic ticket (ascending for L,
-// descending for U), wait until every node they depend on (lower / higher
-// neighbours) has published this solve's epoch in its flag, solve their
-// node's unknowns in order, and publish.  Tickets are handed out in order,
-// so the node a warp waits on is always held by a warp that is already
-// running; the cooperative launch keeps every block resident as well.
-// Every wait is bounded: past kSpinLimit polls the warp records an error,
-// publishes anyway (so no other warp can wait forever), every later wait of
-// the sweep stops within 1024 polls, and the host reports the failure after
-// the sweep.  A legitimate wait lasts microseconds; the limit is ~0.3 s.
+// Sync-free triangular solves: one launch per sweep, one CTA per node at a
+// time.  CTAs take nodes in elimination order from an atomic ticket
+// (ascending for L, descending for U), wait until every node they depend on
+// (lower / higher neighbours) has published this solve's epoch in its flag,
+// then solve the node in two stages:
+//   A  all warps: for every row of the node, the dot product with the
+//      unknowns of OTHER nodes (the long part of the row: independent loads,
+//      rows spread over the warps), and the node's own diagonal-block
+//      entries into shared memory;
+//   B  one thread: the small in-node triangular solve from shared memory.
+// The node's values are then published (fence + release store of the
+// epoch).  Tickets are handed out in order, so a node a CTA waits on is
+// always held by a CTA that is already running.  Every wait is bounded:
+// past kSpinLimit polls the CTA records an error, publishes anyway (so no
+// other CTA can wait forever), every later wait of the sweep stops within
+// 1024 polls, and the host reports the failure after the sweep.  A
+// legitimate wait lasts microseconds; the limit is ~0.3 s.
+//
+// Row structure used by the split: a node's unknowns are contiguous and
+// every row of the node holds every own-node column except the energy row,
+// which lacks the pressure columns (they come last).  So in row i (local
+// index r) the own-node columns below the diagonal are the r entries just
+// before it, and those above are the next nr-1-r entries (nvn-1-r for the
+// energy row).
 static constexpr long long kSpinLimit = 1LL << 22;
+static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
   const int *fu;
@@ -508,6 +534,8 @@ struct TrsvArgs {
   const int *nbr_ptr;
   const int *nbr_node;
   int num_nodes;
+  int Tr;              // local index of the energy row, -1 without energy
+  int nvn;             // nodal fields per node
   unsigned *flags;     // per node: epoch of the last sweep that finished it
   unsigned *tickets;   // [0] L sweep, [1] U sweep (reset before each sweep)
   int *error;          // set when a wait gave up
@@ -523,23 +551,31 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
 }
 
 template <class T, bool LOWER>
-__global__ void __launch_bounds__(256) trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu,
-                                                             T *z, unsigned epoch) {
-  const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g,
+                                                                      const T *__restrict__ lu,
+                                                                      T *z, unsigned epoch) {
+  __shared__ double part[kMaxNodeDofs];               // off-node sums per row
+  __shared__ double own[kMaxNodeDofs][kMaxNodeDofs];  // own-node entries of the sweep's factor
+  __shared__ double dg[kMaxNodeDofs];                 // U diagonal
+  __shared__ int s_node;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kTrsvThreads / 32;
   while (true) {
-    unsigned t = 0;
-    if (lane == 0) t = atomicAdd(g.tickets + (LOWER ? 0 : 1), 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= (unsigned)g.num_nodes) return;
-    const int n = LOWER ? (int)t : g.num_nodes - 1 - (int)t;
+    if (tid == 0) {
+      const unsigned t = atomicAdd(g.tickets + (LOWER ? 0 : 1), 1u);
+      s_node = t < (unsigned)g.num_nodes ? (LOWER ? (int)t : g.num_nodes - 1 - (int)t) : -1;
+    }
+    __syncthreads();
+    const int n = s_node;
+    if (n < 0) return;
     // wait for the dependencies
     bool gave_up = false;
-    for (int q = g.nbr_ptr[n] + lane; q < g.nbr_ptr[n + 1]; q += 32) {
+    for (int q = g.nbr_ptr[n] + tid; q < g.nbr_ptr[n + 1]; q += kTrsvThreads) {
       const int m = g.nbr_node[q];
       if (LOWER ? m >= n : m <= n) continue;
       long long polls = 0;
       while (ld_acquire(g.flags + m) != epoch) {
-        // past the limit, or once any warp of the sweep has given up
+        // past the limit, or once any CTA of the sweep has given up
         if (++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile int *)g.error)) {
           gave_up = true;
           break;
@@ -547,29 +583,61 @@ __global__ void __launch_bounds__(256) trsv_sync_free_kernel(TrsvArgs g, const T
         __nanosleep(64);
       }
     }
-    if (__any_sync(0xffffffffu, gave_up) && lane == 0) atomicExch(g.error, 1);
-    __syncwarp();
-    // solve the node's unknowns in order
-    const int f0 = g.fu[n], f1 = g.fu[n + 1];
-    for (int r = 0; r < f1 - f0; r++) {
-      const int i = LOWER ? f0 + r : f1 - 1 - r;
+    if (__syncthreads_or(gave_up) && tid == 0) atomicExch(g.error, 1);
+    // stage A
+    const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+    for (int r = warp; r < nr; r += NW) {
+      const int i = f0 + r;
       const int64_t di = g.diag[i];
-      const int64_t p0 = LOWER ? g.rowptr[i] : di + 1;
-      const int64_t p1 = LOWER ? di : g.rowptr[i + 1];
-      double sum = 0.0;
-      for (int64_t p = p0 + lane; p < p1; p += 32)
-        sum = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), sum);
-      sum = warp_sum(sum);
-      if (lane == 0) {
-        const double zi = (double)__ldcg(z + i);
-        const double v = LOWER ? zi - sum : (zi - sum) / (double)lu[di];
-        __stcg(z + i, (T)v);
+      const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
+      int64_t p0, p1;
+      if (LOWER) {
+        p0 = g.rowptr[i];
+        p1 = di - r;
+        if (lane < r) own[r][lane] = (double)lu[di - r + lane];
+      } else {
+        p0 = di + 1 + na;
+        p1 = g.rowptr[i + 1];
+        if (lane < na) own[r][lane] = (double)lu[di + 1 + lane];
+        if (lane == 0) dg[r] = (double)lu[di];
       }
-      __syncwarp();
+      double s0 = 0.0, s1 = 0.0;
+      int64_t p = p0 + lane;
+      for (; p + 32 < p1; p += 64) {
+        s0 = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), s0);
+        s1 = fma((double)lu[p + 32], (double)__ldcg(z + g.colidx[p + 32]), s1);
+      }
+      if (p < p1) s0 = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), s0);
+      const double sum = warp_sum(s0 + s1);
+      if (lane == 0) part[r] = sum;
     }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) st_release(g.flags + n, epoch);
+    __syncthreads();
+    // stage B: the in-node solve, one thread
+    if (tid == 0) {
+      double zl[kMaxNodeDofs];
+      if (LOWER) {
+#pragma unroll 1
+        for (int r = 0; r < nr; r++) {
+          double v = (double)__ldcg(z + f0 + r) - part[r];
+          for (int c = 0; c < r; c++) v = fma(-own[r][c], zl[c], v);
+          zl[r] = v;
+          __stcg(z + f0 + r, (T)v);
+        }
+      } else {
+#pragma unroll 1
+        for (int r = nr - 1; r >= 0; r--) {
+          const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
+          double v = (double)__ldcg(z + f0 + r) - part[r];
+          for (int c = 0; c < na; c++) v = fma(-own[r][c], zl[r + 1 + c], v);
+          v /= dg[r];
+          zl[r] = v;
+          __stcg(z + f0 + r, (T)v);
+        }
+      }
+      __threadfence();
+      st_release(g.flags + n, epoch);
+    }
+    __syncthreads();
   }
 }
 
@@ -671,8 +739,8 @@ int Solver::init(Context *c, int krylov) {
   }
   {
     const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
-    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
-    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
+    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
+    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
     if (sm64 > 200 * 1024) return fail("ILU(0) block row does not fit in shared memory");
     GB_CU(cudaFuncSetAttribute(ilu0_block_kernel<double>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64), "smem");
@@ -763,10 +831,10 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
     if (fp32) {
-      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
+      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
       ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu32);
     } else {
-      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + kMaxNodeDofs * kMaxNodeDofs) + ints;
+      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
       ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu);
     }
   }
@@ -777,6 +845,20 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
     if (!prec32) GB_CU(capture_prec<float>(this, d_lu32, d_t32, st, &prec32), "ILU32 graph");
   } else {
     if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");
+  }
+  return 0;
+}
+
+int Solver::copy_factors(double *host, bool fp32, cudaStream_t st) {
+  const int64_t nnz = C->L.nnz;
+  GB_CU(cudaStreamSynchronize(st), "factor");
+  if (fp32) {
+    std::vector<float> tmp((size_t)nnz);
+    GB_CU(cudaMemcpy(tmp.data(), d_lu32, sizeof(float) * nnz, cudaMemcpyDeviceToHost),
+          "factor copy");
+    for (int64_t k = 0; k < nnz; k++) host[k] = tmp[(size_t)k];
+  } else {
+    GB_CU(cudaMemcpy(host, d_lu, sizeof(double) * nnz, cudaMemcpyDeviceToHost), "factor copy");
   }
   return 0;
 }
@@ -796,12 +878,12 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
                           (const void *)trsv_sync_free_kernel<float, false>};
     for (const void *f : fns) {
       int b = 0;
-      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, 256, 0), "occupancy");
+      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kTrsvThreads, 0), "occupancy");
       per_sm = std::min(per_sm, b);
     }
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    S->trsv_grid = std::max(1, std::min(per_sm, 4)) * sms;
+    S->trsv_grid = std::max(1, per_sm) * sms;
   }
   TrsvArgs g;
   g.fu = C->d_fu;
@@ -811,16 +893,19 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
   g.nbr_ptr = C->d_nbr_ptr;
   g.nbr_node = C->d_nbr_node;
   g.num_nodes = C->L.num_nodes;
+  g.Tr = C->L.energy ? C->L.dim : -1;
+  g.nvn = C->L.nvn;
   g.flags = S->d_flags;
   g.tickets = S->d_flags + C->L.num_nodes;
   g.error = (int *)(S->d_flags + C->L.num_nodes + 4);
   for (int pass = 0; pass < 2; pass++) {
     const unsigned epoch = ++S->epoch;
     GB_CU(cudaMemsetAsync(g.tickets, 0, 2 * sizeof(unsigned), st), "tickets");
-    void *args[] = {&g, (void *)&lu, &z, (void *)&epoch};
-    void *fn = pass == 0 ? (void *)trsv_sync_free_kernel<T, true>
-                         : (void *)trsv_sync_free_kernel<T, false>;
-    GB_CU(cudaLaunchCooperativeKernel(fn, dim3(S->trsv_grid), dim3(256), args, 0, st), "trsv");
+    if (pass == 0)
+      trsv_sync_free_kernel<T, true><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, epoch);
+    else
+      trsv_sync_free_kernel<T, false><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, epoch);
+    GB_CU(cudaGetLastError(), "trsv");
   }
   return 0;
 }

@@ -52,6 +52,8 @@ struct Solver {
   ~Solver();
   int init(Context *c, int krylov);
   int factor(const double *vals, bool fp32, cudaStream_t st);
+  // the last factors (CSR order, FP64 or FP32 ones widened) to host memory
+  int copy_factors(double *host, bool fp32, cudaStream_t st);
   int apply_prec64(cudaStream_t st);  // in place on d_t
   int apply_prec32(cudaStream_t st);  // in place on d_t32
 };

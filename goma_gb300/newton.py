@@ -109,7 +109,8 @@ class GomaNewton:
         del keep
 
     def set_assembly_path(self, path):
-        """0: automatic (DMMA element Jacobians in 3-D), 1: scalar FP64."""
+        """0: automatic (scalar FP64), 1: scalar FP64, 2: DMMA element
+        Jacobians in 3-D."""
         _lib.check(self._L.gb_set_assembly_path(self.h, int(path)))
 
     def set_triangular_solve(self, mode):
@@ -171,6 +172,21 @@ class GomaNewton:
         _lib.check(self._L.gb_linear_solve(self.h, _dp(a_msr), _dp(rhs), _dp(dx), ctypes.byref(o),
                                            ctypes.byref(its), ctypes.byref(rr)))
         return dx, its.value, rr.value
+
+    def ilu0_factors(self, a_msr, fp32=False):
+        """ILU(0) factors the linear solve would use for this row-scaled MSR
+        matrix, returned in MSR layout (diagonal = U's, off-diagonal L and U)."""
+        a_msr = np.ascontiguousarray(a_msr, np.float64)
+        lu = np.empty(self.nnz)
+        _lib.check(self._L.gb_ilu0_factors(self.h, _dp(a_msr), 1 if fp32 else 0, _dp(lu)))
+        rowptr, colidx = self.csr_pattern()
+        rows = np.repeat(np.arange(self.N), np.diff(rowptr))
+        diag = colidx == rows
+        out = np.empty(self.msr_len)
+        out[:self.N] = lu[diag]
+        out[self.N] = 0.0
+        out[self.N + 1:] = lu[~diag]
+        return out
 
     def csr_to_msr(self, d_vals):
         a = np.empty(self.msr_len)

@@ -85,9 +85,10 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
-/* Element-kernel path of later assemblies: 0 = automatic (3-D Jacobians on
- * the FP64 tensor pipe, DMMA), 1 = scalar FP64 everywhere.  Both give the
- * same matrix to rounding. */
+/* Element-kernel path of later assemblies: 0 = automatic (the faster
+ * measured kernel: scalar FP64), 1 = scalar FP64, 2 = 3-D Jacobian
+ * contractions on the FP64 tensor pipe (DMMA; 2-D elements stay scalar).
+ * All give the same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
 
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
@@ -174,6 +175,14 @@ int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rh
  * (src/sl_aztecoo_interface.cpp:56). */
 int gb_linear_solve(gb_ctx *ctx, const double *a_msr, const double *rhs, double *dx,
                     const gb_newton_opts *opts, int *iterations, double *relres);
+
+/* The ILU(0) preconditioner of gb_linear_solve for a row-scaled MSR matrix
+ * (length ija[N]), in the library's CSR order (gb_csr_pattern): strictly
+ * lower entries hold L (unit diagonal implied), the rest U.  fp32 = 1 gives
+ * the factors of the FP32-refined mode (computed in FP32, widened).  For
+ * checking the preconditioner against a CPU ILU(0); no counterpart in the
+ * reference (AztecOO keeps its factors internal). */
+int gb_ilu0_factors(gb_ctx *ctx, const double *a_msr, int fp32, double *lu_csr);
 
 /* ---------------------------------------------- learned continuation guess */
 

@@ -53,6 +53,7 @@ def lib():
         L.orc_element_dofs.argtypes = [vp, ctypes.c_int, ip]
         L.orc_row_sum_scale.argtypes = [vp, dp, dp, dp]
         L.orc_newton.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp]
+        L.orc_ilu0.argtypes = [vp, dp, ctypes.c_double, dp]
         L.orc_mesh_sizes.argtypes = [ctypes.c_char_p, ip, ip, ip]
         L.orc_mesh_fill.argtypes = [ctypes.c_char_p, dp, ip, ip, ip]
         _lib = L
@@ -121,6 +122,14 @@ class Oracle:
         g = np.empty(self.nloc, np.int32)
         lib().orc_element_dofs(self.h, e, _p(g, ctypes.c_int))
         return Re, Je, g, st
+
+    def ilu0(self, a, tau=1e-4):
+        """ILU(0) factors of the MSR matrix a (same layout), pivot floor tau."""
+        a = np.ascontiguousarray(a, np.float64)
+        lu = np.empty(self.msr_len)
+        if lib().orc_ilu0(self.h, _p(a, ctypes.c_double), tau, _p(lu, ctypes.c_double)) != 0:
+            raise MemoryError("orc_ilu0")
+        return lu
 
     def row_sum_scale(self, a, R):
         a = a.copy()

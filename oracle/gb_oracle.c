@@ -649,6 +649,42 @@ void orc_row_sum_scale(const orc_problem *p, double *a, double *R, double *scale
   }
 }
 
+/* ILU(0) of an MSR matrix with a pivot floor, row by row in the IKJ order
+ * (Saad, Iterative Methods for Sparse Linear Systems, 2nd ed., Alg. 10.4):
+ * row i is eliminated with the finished rows k < i of its pattern, fill
+ * outside the pattern is dropped, then a pivot below tau in magnitude
+ * becomes +-tau.  The reference's preconditioner is AztecOO's ILU(0)
+ * (third-party, not in the reference tree); this restates the published
+ * algorithm to check the GPU factors. */
+int orc_ilu0(const orc_problem *p, const double *a, double tau, double *lu) {
+  const int N = p->N;
+  const int *ija = p->ija;
+  memcpy(lu, a, sizeof(double) * (size_t)p->msr_len);
+  long *pos = (long *)malloc(sizeof(long) * (size_t)N);
+  if (!pos) return -1;
+  for (int j = 0; j < N; j++) pos[j] = -1;
+  for (int i = 0; i < N; i++) {
+    pos[i] = i;
+    for (int k = ija[i]; k < ija[i + 1]; k++) pos[ija[k]] = k;
+    for (int k = ija[i]; k < ija[i + 1]; k++) {
+      const int j = ija[k];
+      if (j >= i) break; /* off-diagonal columns ascend */
+      const double l = lu[k] / lu[j];
+      lu[k] = l;
+      for (int kk = ija[j]; kk < ija[j + 1]; kk++) {
+        const int c = ija[kk];
+        if (c <= j || pos[c] < 0) continue;
+        lu[pos[c]] -= l * lu[kk];
+      }
+    }
+    if (fabs(lu[i]) < tau) lu[i] = lu[i] < 0.0 ? -tau : tau;
+    pos[i] = -1;
+    for (int k = ija[i]; k < ija[i + 1]; k++) pos[ija[k]] = -1;
+  }
+  free(pos);
+  return 0;
+}
+
 /* Banded Gaussian elimination with partial pivoting on the MSR system
  * (the oracle's stand-in for the Krylov solve; only converged fields are
  * compared). */

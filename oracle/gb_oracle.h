@@ -52,6 +52,9 @@ int orc_local_size(const orc_problem *p);
 void orc_element_dofs(const orc_problem *p, int e, int *gdof);
 /* scale[i] = sign(a_ii) * sum_j |a_ij|; a and R are divided by it. */
 void orc_row_sum_scale(const orc_problem *p, double *a, double *R, double *scale);
+/* ILU(0) (IKJ order, pivots below tau in magnitude set to +-tau) of the
+ * MSR matrix a into lu (same layout).  Returns 0, -1 on allocation failure. */
+int orc_ilu0(const orc_problem *p, const double *a, double tau, double *lu);
 /* Full Newton from x with a banded direct solve.  Returns the number of
  * iterations (>= 0) on convergence, -1 on failure.  norms (optional) gets
  * the scaled-residual L2 norm of every iteration (max_it entries). */

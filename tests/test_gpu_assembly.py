@@ -121,7 +121,7 @@ def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn):
     o = oracle.Oracle(prob)
     gn = GomaNewton(prob)
     x = _random_state(o, 23)
-    gn.set_assembly_path(0)
+    gn.set_assembly_path(2)
     R_tc, a_tc = gn.matrix_fill_full(x)
     gn.set_assembly_path(1)
     R_sc, a_sc = gn.matrix_fill_full(x)

@@ -24,15 +24,22 @@ def _run(pred, nx=12, ny=4, steps=8):
 
 
 def test_continuation_predictors_agree_and_learned_helps():
+    """The network with only the zeroth-order fallback: every Newton
+    iteration it saves is the network's doing."""
     rz, xz = _run("zeroth")
     rf, xf = _run("first")
     rl, xl = _run("learned")
+    rlf, xlf = _run("learned+first")
     scale = np.abs(xz).max()
-    assert np.abs(xf - xz).max() <= 1e-8 * scale
-    assert np.abs(xl - xz).max() <= 1e-8 * scale
+    for xo in (xf, xl, xlf):
+        assert np.abs(xo - xz).max() <= 1e-8 * scale
     its = {name: sum(r["newton_its"] for r in recs[1:])
-           for name, recs in (("zeroth", rz), ("first", rf), ("learned", rl))}
+           for name, recs in (("zeroth", rz), ("first", rf), ("learned", rl),
+                              ("learned+first", rlf))}
     print("newton iterations over the sweep:", its)
     print("learned-step guesses:", [r["guess"] for r in rl[1:]])
-    assert its["learned"] <= its["zeroth"]
     assert its["first"] <= its["zeroth"]
+    assert its["learned+first"] <= its["first"]
+    # the network's own gain over the method without it
+    assert any(r["guess"] == "learned" for r in rl[1:])
+    assert its["learned"] < its["zeroth"]

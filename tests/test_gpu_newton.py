@@ -61,9 +61,9 @@ def test_gpu_newton_larger_cavity_against_oracle():
 
 @pytest.mark.parametrize("case", ["cavity2d_12", "bouss3d_4"])
 def test_gpu_triangular_solve_modes_agree(case):
-    """Sync-free ILU(0) sweeps and the level-scheduled graph do the same
-    per-row arithmetic in the same order, so a fixed number of GMRES
-    iterations gives the same correction either way."""
+    """Sync-free ILU(0) sweeps and the level-scheduled graph apply the same
+    preconditioner (summation order differs), so a fixed number of GMRES
+    iterations gives the same correction to rounding."""
     prob = (pb.lid_cavity_2d(12, 100.0) if case.startswith("cavity")
             else pb.boussinesq_cube_3d(4, 1e4, 0.71))
     gn = GomaNewton(prob)
@@ -74,9 +74,29 @@ def test_gpu_triangular_solve_modes_agree(case):
     out = []
     for mode in (1, 0, 0):
         gn.set_triangular_solve(mode)
-        dx, its, rr = gn.linear_solve(a_s, R_s, linear_tol=1e-30, max_linear_its=40)
-        assert its == 40
+        dx, its, rr = gn.linear_solve(a_s, R_s, linear_tol=1e-30, max_linear_its=8)
+        assert its == 8
         out.append(dx)
     scale = np.abs(out[0]).max()
-    assert np.abs(out[1] - out[0]).max() <= 1e-12 * scale
-    assert np.abs(out[2] - out[1]).max() <= 1e-12 * scale
+    assert np.abs(out[1] - out[0]).max() <= 1e-10 * scale
+    assert np.array_equal(out[2], out[1])   # the sync-free sweeps are deterministic
+
+
+@pytest.mark.parametrize("name", ["cav2d_3x2_pert", "bfs2d_4x2_carreau", "box3d_2x2x2_bouss",
+                                  "box3d_2x2x2_species"])
+def test_gpu_ilu0_factors_match_oracle(name):
+    """The GPU's node-block ILU(0) (FP64 and FP32) equals the oracle's
+    row-by-row ILU(0) of the same row-scaled reference Jacobian, pivot
+    floor included (the Carreau channel without a pressure datum hits it).
+    FP32 tolerance: single-precision rounding (6e-8) amplified by the
+    floored pivots (1e-4) of that channel."""
+    g, case = gc.load(name)
+    prob = gc.problem_from_case(case)
+    o = oracle.Oracle(prob)
+    gn = GomaNewton(prob)
+    a_s, _, _ = o.row_sum_scale(g["a"], g["R"])
+    ref = o.ilu0(a_s, tau=1e-4)
+    ija = o.ija()
+    for fp32, tol in ((False, 1e-10), (True, 2e-3)):
+        lu = gn.ilu0_factors(a_s, fp32=fp32)
+        assert gc.msr_row_scaled_error(ija, lu, ref) < tol, fp32

@@ -56,3 +56,35 @@ def test_oracle_detects_inverted_element():
     o = oracle.Oracle(prob)
     _, _, st = o.matrix_fill(np.zeros(o.N))
     assert st == -1
+
+
+def test_oracle_ilu0_reproduces_matrix_on_pattern():
+    """ILU(0) property: (L U)_ij = A_ij on the sparsity pattern (no pivot
+    floor hit), on the reference's own row-scaled Jacobian."""
+    sp = pytest.importorskip("scipy.sparse")
+    g, case = gc.load("cav2d_3x2_pert")
+    o = oracle.Oracle(gc.problem_from_case(case))
+    a_s, _, _ = o.row_sum_scale(g["a"], g["R"])
+    lu = o.ilu0(a_s, tau=0.0)
+    ija = o.ija()
+    N = o.N
+
+    def to_csr(v):
+        rows, cols, vals = list(range(N)), list(range(N)), list(v[:N])
+        for i in range(N):
+            for k in range(ija[i], ija[i + 1]):
+                rows.append(i)
+                cols.append(ija[k])
+                vals.append(v[k])
+        return sp.csr_matrix((vals, (rows, cols)), shape=(N, N))
+
+    A = to_csr(a_s)
+    F = to_csr(lu)
+    Lm = sp.tril(F, -1) + sp.identity(N)
+    Um = sp.triu(F)
+    P = (Lm @ Um).tocsr()
+    Ad = A.toarray()
+    Pd = P.toarray()
+    mask = A.toarray() != 0
+    mask |= to_csr(np.ones_like(a_s)).toarray() != 0
+    assert np.abs((Pd - Ad)[mask]).max() <= 1e-12 * np.abs(Ad).max()
