@@ -168,13 +168,15 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10):
         recs, x = continuation(gn, ra0, ra1, nsteps,
                                predictor="learned" if mode == "learned_fp32" else "zeroth",
                                set_param=set_ra, newton_opts=opts, spacing="log",
-                               learned_opts=dict(steps=300, batch=4096, lr=2e-3))
+                               learned_opts=dict(steps=600, batch=4096, lr=2e-3))
         torch.cuda.synchronize()
         dt = time.perf_counter() - t
         sols[mode] = x
+        ms = {k: sum(r["newton_ms"][k] for r in recs) for k in recs[0]["newton_ms"]}
         out[mode] = {"seconds": dt, "newton_its": sum(r["newton_its"] for r in recs),
-                     "linear_its": sum(r.get("linear_its", 0) for r in recs[1:]),
-                     "guesses": [r["guess"] for r in recs[1:]]}
+                     "linear_its": sum(r.get("linear_its", 0) for r in recs),
+                     "guesses": [r["guess"] for r in recs[1:]],
+                     "newton_seconds": {k.replace("_ms", ""): v * 1e-3 for k, v in ms.items()}}
         del gn
     a, b = sols["plain_fp64"], sols["learned_fp32"]
     out["solution_rel_diff"] = float(np.abs(a - b).max() / np.abs(a).max())
@@ -217,7 +219,9 @@ def main():
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--path", type=int, default=0,
-                    help="element kernel: 0 automatic, 1 scalar FP64, 2 FP64 tensor pipe (DMMA)")
+                    help="element kernel: 0 automatic (3), 1 scalar FP64, 2 FP64 tensor pipe "
+                         "with per-fragment coefficients, 3 FP64 tensor-pipe products over "
+                         "operand tables")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
     args = ap.parse_args()
@@ -242,8 +246,9 @@ def main():
     prob = pb.boussinesq_cube_3d(nel, RA, PR)
     gn = GomaNewton(prob)
     gn.set_assembly_path(args.path)
-    kernel_name = ("assemble_tc_kernel<energy> (FP64 DMMA)" if args.path == 2
-                   else "assemble_kernel<3,energy> (scalar FP64)")
+    kernel_name = {1: "assemble_kernel<3,energy> (scalar FP64)",
+                   2: "assemble_tc_kernel<energy> (FP64 DMMA, per-fragment coefficients)"}.get(
+        args.path, "assemble_gemm_kernel<energy> (FP64 DMMA products over operand tables)")
     L = gn._L
     N, nnz, msr_len = gn.N, gn.nnz, gn.msr_len
     x_host = gn.dirichlet_init(np.random.default_rng(11).uniform(-1.0, 1.0, N))

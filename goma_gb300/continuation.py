@@ -1,7 +1,8 @@
-"""Zeroth/first-order parameter continuation with a learned initial guess.
+"""Parameter continuation with zeroth-order, first-order, secant and learned
+initial guesses.
 
-Mirrors continue_problem (src/ac_conti.c:106) for a density (Reynolds
-number) sweep of a steady problem:
+Mirrors continue_problem (src/ac_conti.c:106) for a parameter sweep of a
+steady problem (density / Reynolds number, or any parameter set_param sets):
 
 - ``zeroth``: ALC_ZEROTH, the previous solution is the next guess
   (src/ac_conti.c:759-784);
@@ -9,11 +10,16 @@ number) sweep of a steady problem:
   linear solve with the Jacobian at x_old and dR/dlambda by central
   differences of the residual (soln_sens, src/mm_sol_nonlinear.c:3615,
   :3753, :3796);
-- ``learned``: a 3 x 256 tanh network (GPU, FP32, trained online by the
-  library's own kernels on every converged solution) predicts the fields
-  from (x, y[, z], lambda); its guess is used only when its FP64 scaled
-  residual is smaller than the fallback's (``zeroth``; ``first`` with
-  ``learned+first``), and the Newton solve always decides the answer.
+- ``secant``: first-order extrapolation through the last two converged
+  solutions (no tangent solve);
+- ``learned``: the secant guess plus a curvature correction predicted by a
+  3 x 256 tanh network (GPU, FP32, trained online by the library's own
+  kernels on the secant errors of the earlier steps).  The plain secant
+  guess is the fallback: the learned guess is used only when its FP64
+  scaled residual is smaller, and the Newton solve always decides the
+  answer;
+- ``learned+first``: as ``learned``, with the tangent guess as a third
+  candidate.
 
 On a failed Newton solve the step is halved and re-predicted
 (src/ac_conti.c:986-1045).
@@ -27,8 +33,9 @@ from .newton import GomaNewton
 
 
 class FieldLayout:
-    """Where each unknown lives: nodal velocity components, and the P1
-    pressure unknowns at each element's centroid node."""
+    """Where each unknown lives: the nodal unknowns (velocity, temperature,
+    species) at every node, and the P1 pressure unknowns at each element's
+    centroid node."""
 
     def __init__(self, gn: GomaNewton):
         import ctypes
@@ -40,92 +47,151 @@ class FieldLayout:
         fu = np.empty(nn + 1, np.int32)
         _lib.check(gn._L.gb_first_unknown(gn.h, fu.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         self.fu = fu
-        self.nvn = p.dim + (1 if p.energy else 0)
-        self.centroids = p.mesh.conn[:, 8 if p.dim == 2 else 20]
-        self.n_out = self.nvn + p.dim + 1
-        # feature scaling: coordinates to [0, 1]
-        c = p.mesh.coords
-        self.lo = c.min(axis=0)
-        self.span = np.maximum(c.max(axis=0) - self.lo, 1e-300)
-        self.coords01 = (c - self.lo) / self.span
         cnt = np.diff(fu)
+        self.nvn = int(cnt.min())
+        self.n_out = self.nvn + p.dim + 1
+        # feature scaling: coordinates to [-1, 1]
+        c = p.mesh.coords
+        lo = c.min(axis=0)
+        span = np.maximum(c.max(axis=0) - lo, 1e-300)
+        self.coords11 = (c - lo) / span * 2.0 - 1.0
         self.is_cent = cnt > self.nvn
+        self.cn = np.nonzero(self.is_cent)[0]
 
     def targets(self, x):
-        """(n_nodes, n_out) targets and mask from an unknown vector."""
+        """(n_nodes, n_out) per-node values and their mask from an unknown
+        vector (the pressure columns exist at centroid nodes only)."""
         nn = len(self.fu) - 1
         T = np.zeros((nn, self.n_out))
         M = np.zeros((nn, self.n_out), np.float32)
         for a in range(self.nvn):
             T[:, a] = x[self.fu[:-1] + a]
             M[:, a] = 1.0
-        cn = np.nonzero(self.is_cent)[0]
         for l in range(self.dim + 1):
-            T[cn, self.nvn + l] = x[self.fu[cn] + self.nvn + l]
-            M[cn, self.nvn + l] = 1.0
+            T[self.cn, self.nvn + l] = x[self.fu[self.cn] + self.nvn + l]
+            M[self.cn, self.nvn + l] = 1.0
         return T, M
 
     def assemble(self, Y, N):
-        """Unknown vector from (n_nodes, n_out) predictions."""
+        """Unknown vector from (n_nodes, n_out) per-node values."""
         x = np.zeros(N)
         for a in range(self.nvn):
             x[self.fu[:-1] + a] = Y[:, a]
-        cn = np.nonzero(self.is_cent)[0]
         for l in range(self.dim + 1):
-            x[self.fu[cn] + self.nvn + l] = Y[cn, self.nvn + l]
+            x[self.fu[self.cn] + self.nvn + l] = Y[self.cn, self.nvn + l]
         return x
 
 
 class LearnedPredictor:
-    """(x, y[, z], lambda) -> unknowns at that node, trained online."""
+    """Secant predictor plus a learned correction for the curvature of the
+    solution path.
 
-    def __init__(self, gn, lam_range, width=256, hidden=3, seed=0, steps=400, batch=4096,
-                 lr=1e-3):
+    The secant predictor (the cheap first-order predictor, with no tangent
+    solve; ALC_FIRST of src/ac_conti.c:759 uses a tangent instead) misses
+    the second-order part of x(lambda): its error on a path with curvature
+    x''/2 = c is c h (h + h_prev) for a step h after a step h_prev.  A
+    network over (x, y[, z], lambda) is trained online, on the GPU by the
+    library's own kernels, on the secant errors of every earlier step
+    divided by h (h + h_prev) -- samples of the curvature field c -- and the
+    guess for the next step is
+
+        x_guess = secant(lam) + h (h + h_prev) * net(coords, lam).
+
+    A fit error in c costs only that fraction of the secant error, so the
+    learned guess improves on the secant wherever the curvature field
+    carries over from one step to the next."""
+
+    def __init__(self, gn, lam_range, width=256, hidden=3, seed=0, steps=1500, batch=4096,
+                 lr=2e-3, log_lambda=False):
         from .mlp import GpuMLP
         self.lay = FieldLayout(gn)
         self.N = gn.N
         self.net = GpuMLP(self.lay.dim + 1, width, hidden, self.lay.n_out, seed=seed)
-        self.lmin, self.lmax = math.log(lam_range[0]), math.log(lam_range[1])
+        self.log_lambda = log_lambda
+        self.lmin, self.lmax = self._t(lam_range[0]), self._t(lam_range[1])
         self.steps, self.batch, self.lr = steps, batch, lr
+        self.sols = []
         self.X, self.T, self.M = [], [], []
         self.tscale = None
         self.trained = 0
 
-    def _features(self, lam):
-        s = (math.log(lam) - self.lmin) / max(self.lmax - self.lmin, 1e-300) * 2.0 - 1.0
-        c = self.lay.coords01 * 2.0 - 1.0
+    def _t(self, lam):
+        """The sweep variable: lambda, or log lambda for a sweep uniform in
+        log lambda."""
+        return math.log(lam) if self.log_lambda else float(lam)
+
+    def _features(self, t):
+        s = (t - self.lmin) / max(self.lmax - self.lmin, 1e-300) * 2.0 - 1.0
+        c = self.lay.coords11
         return np.hstack([c, np.full((c.shape[0], 1), s)]).astype(np.float32)
 
+    def secant(self, lam):
+        """First-order extrapolation through the last two recorded solutions
+        (the last solution itself while only one is known)."""
+        t = self._t(lam)
+        tk, xk = self.sols[-1]
+        if len(self.sols) < 2:
+            return xk.copy()
+        tp, xp = self.sols[-2]
+        return xk + (t - tk) * (xk - xp) / (tk - tp)
+
+    def _hh(self, t):
+        tk = self.sols[-1][0]
+        tp = self.sols[-2][0]
+        h, hp = t - tk, tk - tp
+        return h * (h + hp)
+
     def add(self, lam, x):
-        T, M = self.lay.targets(x)
-        self.X.append(self._features(lam))
-        self.T.append(T)
-        self.M.append(M)
+        """Record a converged solution; once two earlier ones are known, the
+        secant predictor's error at this one becomes a training sample."""
+        t = self._t(lam)
+        x = np.array(x, np.float64)
+        if len(self.sols) >= 2:
+            hh = self._hh(t)
+            if hh != 0.0:
+                T, M = self.lay.targets((x - self.secant(lam)) / hh)
+                self.X.append(self._features(t))
+                self.T.append(T)
+                self.M.append(M)
+        self.sols.append((t, x))
+
+    @property
+    def ready(self):
+        return bool(self.X)
 
     def train(self, seed=0):
         import torch
+        if not self.X:
+            return None
         X = np.vstack(self.X)
         T = np.vstack(self.T)
         M = np.vstack(self.M)
         # per-output standardisation, refreshed with the data
         mu = (T * M).sum(0) / np.maximum(M.sum(0), 1)
-        sd = np.sqrt((((T - mu) * M) ** 2).sum(0) / np.maximum(M.sum(0), 1)) + 1e-12
+        sd = np.sqrt((((T - mu) * M) ** 2).sum(0) / np.maximum(M.sum(0), 1))
+        sd = np.where(sd > 0, sd, 1.0)
         self.tscale = (mu, sd)
         Tn = ((T - mu) / sd).astype(np.float32) * M
         dx = torch.tensor(X, device="cuda")
         dt = torch.tensor(Tn, device="cuda")
         dm = torch.tensor(M, device="cuda")
-        loss = self.net.train(dx, dt, dm, steps=self.steps, batch=self.batch, lr=self.lr,
-                              seed=seed)
+        # Adam at the given rate, then a quarter as many steps at a tenth of it
+        self.net.train(dx, dt, dm, steps=self.steps, batch=self.batch, lr=self.lr, seed=seed)
+        loss = self.net.train(dx, dt, dm, steps=max(self.steps // 4, 1), batch=self.batch,
+                              lr=0.1 * self.lr, seed=seed + 7919)
         self.trained += 1
         return loss
 
-    def predict(self, lam):
+    def curvature(self, lam):
+        """The network's curvature field at lam, as an unknown vector."""
         import torch
-        X = torch.tensor(self._features(lam), device="cuda")
+        X = torch.tensor(self._features(self._t(lam)), device="cuda")
         Y = self.net.forward(X).double().cpu().numpy()
         mu, sd = self.tscale
         return self.lay.assemble(Y * sd + mu, self.N)
+
+    def predict(self, lam):
+        return self.secant(lam) + self._hh(self._t(lam)) * self.curvature(lam)
 
 
 def _set_density(gn, rho):
@@ -175,7 +241,7 @@ def tangent(gn, x, lam, set_param, rel=1e-6, **solve_opts):
     return sens.cpu().numpy()
 
 
-PREDICTORS = ("zeroth", "first", "learned", "learned+first")
+PREDICTORS = ("zeroth", "first", "secant", "learned", "learned+first")
 
 
 def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=_set_density,
@@ -183,12 +249,14 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
                  verbose=False):
     """Sweep lambda from lam0 to lam1 in nsteps steps (uniform in lambda, or
     in log lambda with spacing="log").  predictor: "zeroth" (ALC_ZEROTH),
-    "first" (ALC_FIRST), "learned" (the network, zeroth-order fallback) or
-    "learned+first" (the network, first-order fallback).  A step whose
-    Newton solve fails is halved and re-predicted from the last converged
-    point, at most max_halvings times (src/ac_conti.c:986-1045).  Returns a
-    list of per-step records (lambda, guess used, guess residuals, Newton
-    iterations, wall time) and the final solution."""
+    "first" (ALC_FIRST), "secant", "learned" (secant + the network's
+    curvature correction, secant fallback) or "learned+first" (the same
+    with the tangent guess as another candidate).  Among several candidate
+    guesses the one with the smallest FP64 scaled residual is used.  A step
+    whose Newton solve fails is halved and re-predicted from the last
+    converged point, at most max_halvings times (src/ac_conti.c:986-1045).
+    Returns a list of per-step records (lambda, guess used, candidate
+    residuals, Newton iterations, wall time) and the final solution."""
     if predictor not in PREDICTORS:
         raise ValueError("predictor must be one of %s" % (PREDICTORS,))
     newton_opts = dict(newton_opts or {})
@@ -202,14 +270,19 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
     if not conv:
         raise RuntimeError("first continuation step did not converge")
     records = [{"lam": float(lams[0]), "guess": "initial", "newton_its": st["newton_its"],
-                "guess_residual": None, "wall_s": time.perf_counter() - t0}]
+                "linear_its": st["linear_its"], "guess_residual": None,
+                "wall_s": time.perf_counter() - t0,
+                "newton_ms": {k2: st[k2] for k2 in ("assemble_ms", "scale_ms", "factor_ms",
+                                                    "solve_ms", "total_ms")}}]
     learned = predictor.startswith("learned")
     first = predictor in ("first", "learned+first")
+    secant = predictor == "secant" or learned
     lp = None
     if learned:
-        lp = LearnedPredictor(gn, (min(lam0, lam1), max(lam0, lam1)), **(learned_opts or {}))
+        lp = LearnedPredictor(gn, (min(lam0, lam1), max(lam0, lam1)),
+                              log_lambda=(spacing == "log"), **(learned_opts or {}))
         lp.add(lams[0], x)
-        lp.train(seed=0)
+    hist = [(lams[0], x)]
     lin_keys = ("linear_tol", "fp32_inner", "krylov_dim", "max_linear_its", "inner_tol")
     x_old, lam_old = x, lams[0]
     targets = lams[1:]
@@ -219,7 +292,16 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
         t0 = time.perf_counter()
         halvings = 0
         while True:
-            cands = {"zeroth": x_old}
+            cands = {}
+            if secant and len(hist) >= 2:
+                (lp_, xp_), (lk_, xk_) = hist[-2], hist[-1]
+                if spacing == "log":
+                    ht, hp = math.log(lam) - math.log(lk_), math.log(lk_) - math.log(lp_)
+                else:
+                    ht, hp = lam - lk_, lk_ - lp_
+                cands["secant"] = xk_ + (ht / hp) * (xk_ - xp_)
+            else:
+                cands["zeroth"] = x_old
             if first:
                 sens = tangent(gn, x_old, lam_old, set_param,
                                **{k2: v for k2, v in newton_opts.items() if k2 in lin_keys})
@@ -243,14 +325,18 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
             halvings += 1
             lam = 0.5 * (lam_old + lam)
             targets.insert(k, lam)
+        hist.append((lam, x))
         if lp is not None:
             lp.add(lam, x)
-            if k + 1 < len(targets):
+            if k + 1 < len(targets) and lp.ready:
                 lp.train(seed=len(records))
         wall = time.perf_counter() - t0
         records.append({"lam": float(lam), "guess": choice, "newton_its": st["newton_its"],
                         "linear_its": st["linear_its"], "guess_residual": res.get(choice),
-                        "candidates": res, "halvings": halvings, "wall_s": wall})
+                        "candidates": res, "halvings": halvings, "wall_s": wall,
+                        "newton_ms": {k2: st[k2] for k2 in ("assemble_ms", "scale_ms",
+                                                            "factor_ms", "solve_ms",
+                                                            "total_ms")}})
         if verbose:
             print(records[-1])
         x_old, lam_old = x, lam

@@ -107,7 +107,7 @@ __global__ void csr_to_msr_kernel(int N, const int64_t *__restrict__ rowptr,
 Context::~Context() {
   void *ptrs[] = {d_coords, d_conn,   d_fu,     d_dbc,     d_dbc_val, d_rowptr, d_colidx,
                   d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nbr_node, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
-                  d_tab_pt, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
+                  d_tab_pt, d_tab_iso, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (ev_k0) cudaEventDestroy(ev_k0);
@@ -177,6 +177,11 @@ int Context::init(const gb_problem_desc *d) {
       upload(&d_tab_dphi, tdphi, "tab") || upload(&d_tab_w, tw, "tab") ||
       upload(&d_tab_pt, tpt, "tab") || upload(&d_color_elems, L.color_elems, "colors"))
     return -1;
+  if (L.dim == 3) {
+    std::vector<double> iso(112 * 28);
+    build_iso_table(tphi.data(), tdphi.data(), iso.data());
+    if (upload(&d_tab_iso, iso, "tab")) return -1;
+  }
   if ((e = cudaMalloc(&d_x, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "x");
   if ((e = cudaMalloc(&d_R, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "R");
   if ((e = cudaMalloc(&d_vals, sizeof(double) * L.nnz)) != cudaSuccess)
@@ -224,8 +229,8 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   AsmArgs a = args(x, R, vals);
   const int ncol = (int)L.color_ptr.size() - 1;
   if (timing) cudaEventRecord(ev_k0, st);
-  const bool tc = L.dim == 3 && vals != nullptr && path == 2;
-  if (tc && tc_grid == 0) {
+  const int kp = kernel_path(vals != nullptr);
+  if (kp >= 2 && tc_grid == 0) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -233,7 +238,10 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   }
   for (int c = 0; c < ncol; c++) {
     const int n = L.color_ptr[c + 1] - L.color_ptr[c];
-    if (tc)
+    if (kp == 3)
+      e = launch_assemble_gemm(a, L.energy != 0, d_tab_iso, d_color_elems + L.color_ptr[c], n,
+                               tc_grid, st);
+    else if (kp == 2)
       e = launch_assemble_tc(a, L.energy != 0, carreau, d_color_elems + L.color_ptr[c], n,
                              tc_grid, st);
     else
@@ -255,6 +263,13 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
     kernel_launches += ncol * (L.nspec > 0 ? 2 : 1);
   }
   return 0;
+}
+
+int Context::kernel_path(bool jacobian) const {
+  if (L.dim != 3) return 1;
+  const bool gemm_ok = !carreau && mat.viscosity > 0.0;
+  if (path == 0 || path == 3) return gemm_ok ? 3 : 1;
+  return jacobian ? path : 1;
 }
 
 int Context::check_status() {
@@ -396,8 +411,9 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 }
 
 int gb_set_assembly_path(gb_ctx *ctx, int path) {
-  if (!ctx || path < 0 || path > 2)
-    return fail("path must be 0 (auto), 1 (scalar FP64) or 2 (FP64 tensor pipe)");
+  if (!ctx || path < 0 || path > 3)
+    return fail("path must be 0 (auto), 1 (scalar FP64), 2 (FP64 tensor pipe, per-fragment "
+                "coefficients) or 3 (FP64 tensor pipe, operand tables; 3-D Newtonian)");
   ctx->c.path = path;
   return 0;
 }

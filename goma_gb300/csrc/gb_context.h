@@ -21,8 +21,11 @@ struct Context {
   Layout L;
   MaterialDev mat{};
   bool carreau = false;
-  int path = 0;        // element kernel: 0 auto (scalar), 1 scalar FP64, 2 DMMA in 3-D
-  int tc_grid = 0;     // persistent grid of the DMMA kernel
+  // element kernel: 0 automatic (3 where it applies, else 1), 1 scalar FP64,
+  // 2 DMMA with per-fragment coefficients, 3 DMMA products over operand tables
+  // (3-D Newtonian)
+  int path = 0;
+  int tc_grid = 0;     // persistent grid of the DMMA kernels
   int trsv = 0;        // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph
   cudaStream_t stream = nullptr;
   double *d_coords = nullptr;
@@ -35,6 +38,7 @@ struct Context {
   int *d_nbr_ptr = nullptr, *d_nbr_off = nullptr, *d_nbr_offT = nullptr, *d_nbr_node = nullptr;
   uint16_t *d_nslot = nullptr;
   double *d_tab_phi = nullptr, *d_tab_dphi = nullptr, *d_tab_w = nullptr, *d_tab_pt = nullptr;
+  double *d_tab_iso = nullptr;  // 3-D: [value, d/dxi_r] x points x nodes (gemm kernel)
   int *d_color_elems = nullptr;
   double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
   int *d_status = nullptr;
@@ -54,6 +58,8 @@ struct Context {
   int assemble(const double *x, double *R, double *vals, cudaStream_t st);
   int reset_status();
   int check_status();
+  // the element kernel an assembly with (vals != NULL) or without a Jacobian uses
+  int kernel_path(bool jacobian) const;
   int to_msr_host(const double *vals, double *a_msr);
 };
 

@@ -56,5 +56,11 @@ cudaError_t launch_assemble_species(const AsmArgs &a, int dim, bool energy, bool
 // 3-D Jacobian contractions on the FP64 tensor pipe (gb_assemble_tc.cu)
 cudaError_t launch_assemble_tc(const AsmArgs &a, bool energy, bool carreau, const int *elems,
                                int nelem, int grid_cap, cudaStream_t st);
+// 3-D Newtonian residual + Jacobian as dense DMMA products (gb_assemble_gemm.cu);
+// tab_iso is build_iso_table's [112][28] table on the device
+cudaError_t launch_assemble_gemm(const AsmArgs &a, bool energy, const double *tab_iso,
+                                 const int *elems, int nelem, int grid_cap, cudaStream_t st);
+size_t assemble_gemm_smem_bytes();
+void build_iso_table(const double *tab_phi, const double *tab_dphi, double *iso);
 
 }  // namespace gb

@@ -85,10 +85,14 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
-/* Element-kernel path of later assemblies: 0 = automatic (the faster
- * measured kernel: scalar FP64), 1 = scalar FP64, 2 = 3-D Jacobian
- * contractions on the FP64 tensor pipe (DMMA; 2-D elements stay scalar).
- * All give the same matrix to rounding. */
+/* Element-kernel path of later assemblies: 0 = automatic (3 where it
+ * applies, else 1), 1 = scalar FP64, 2 = 3-D Jacobian contractions on the
+ * FP64 tensor pipe (DMMA) with per-fragment coefficients, 3 = the whole 3-D
+ * residual + Jacobian as DMMA products over shared-memory operand tables
+ * (Newtonian viscosity; Carreau and 2-D elements use path 1).  A
+ * residual-only assembly uses the same kernel as the full one under paths
+ * 0, 1 and 3, so its R is bitwise the full assembly's; under path 2 it
+ * uses path 1.  All give the same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
 
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps

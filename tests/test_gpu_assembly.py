@@ -113,16 +113,29 @@ def test_gpu_reports_inverted_element():
                        pb.Material(density=5.0, viscosity_model=pb.VISC_CARREAU, mu0=1.0,
                                    mu_inf=0.01, lam=1.0, aexp=2.0, nexp=0.5),
                        False, [b for b in pb.HEATED3D_BCS if b[0] != pb.VAR_T], (0, 0.0)),
-], ids=["bouss3d", "carreau_t3d", "carreau_ns3d"])
-def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn):
-    """3-D Jacobians on the FP64 tensor pipe (DMMA) equal the scalar-FP64
-    kernel's within 1e-12 (row-scaled), and both equal the oracle."""
+    lambda: pb.Problem(pb.box_mesh(3, 2, 3, 2, 1.2, 0.8, 1.0, amp=0.12, seed=6),
+                       pb.Material(density=3.0, viscosity=0.7,
+                                   momentum_source=(0.5, -2.0, 1.0)),
+                       False, [b for b in pb.HEATED3D_BCS if b[0] != pb.VAR_T], (1, 0.3)),
+    lambda: pb.Problem(pb.box_mesh(3, 3, 2, 3, 1.0, 0.6, 1.4, amp=0.1, seed=9),
+                       pb.Material(density=1.7, viscosity=0.4, heat_capacity=2.2,
+                                   conductivity=0.35, momentum_source=(0.0, 0.0, -4.0)),
+                       True, list(pb.HEATED3D_BCS), (2, -0.1)),
+], ids=["bouss3d", "carreau_t3d", "carreau_ns3d", "newt_ns3d_pert", "newt_t3d_const_src"])
+@pytest.mark.parametrize("path", [2, 3])
+def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn, path):
+    """3-D residuals and Jacobians on the FP64 tensor pipe (DMMA; path 2 with
+    per-fragment coefficients, path 3 as products over operand tables, which
+    takes Newtonian problems and hands Carreau ones to the scalar kernel)
+    equal the scalar-FP64 kernel's within 1e-12 (row-scaled), and all equal
+    the oracle.  A residual-only assembly gives the same R bit for bit."""
     prob = prob_fn()
     o = oracle.Oracle(prob)
     gn = GomaNewton(prob)
     x = _random_state(o, 23)
-    gn.set_assembly_path(2)
+    gn.set_assembly_path(path)
     R_tc, a_tc = gn.matrix_fill_full(x)
+    R_res, _ = gn.matrix_fill_full(x, jacobian=False)
     gn.set_assembly_path(1)
     R_sc, a_sc = gn.matrix_fill_full(x)
     Ro, ao, _ = o.matrix_fill(x)
@@ -130,3 +143,6 @@ def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn):
     assert gc.msr_row_scaled_error(ija, a_tc, a_sc) < TOL
     assert gc.msr_row_scaled_error(ija, a_tc, ao) < TOL
     assert np.abs(R_tc - Ro).max() <= TOL * np.abs(Ro).max()
+    assert np.abs(R_tc - R_sc).max() <= TOL * np.abs(Ro).max()
+    if path == 3:
+        assert np.array_equal(R_res, R_tc)

@@ -1,8 +1,11 @@
 """Reynolds-number continuation of the Carreau channel: zeroth-order,
-first-order (tangent) and learned initial guesses.  All three must reach
-the same converged solutions (the Newton solve decides); the learned guess,
-with the reference's predictor as fallback, must not need more Newton
-iterations than the zeroth-order predictor it replaces."""
+first-order (tangent), secant and learned initial guesses.  All must reach
+the same converged solutions (the Newton solve decides).  The learned guess
+is the secant guess plus the network's curvature correction, with the plain
+secant guess as its fallback, so what the network gains over the method
+without it shows in the learned run against the secant run."""
+import math
+
 import numpy as np
 import pytest
 
@@ -19,27 +22,33 @@ def _run(pred, nx=12, ny=4, steps=8):
     prob = pb.carreau_step_2d(nx, ny, 10.0)
     gn = GomaNewton(prob)
     recs, x = continuation(gn, 10.0, 200.0, steps, predictor=pred, newton_opts=OPTS,
-                           learned_opts=dict(steps=300, batch=2048, lr=2e-3))
+                           learned_opts=dict(steps=1500, batch=2048, lr=2e-3))
     return recs, x
 
 
 def test_continuation_predictors_agree_and_learned_helps():
-    """The network with only the zeroth-order fallback: every Newton
-    iteration it saves is the network's doing."""
-    rz, xz = _run("zeroth")
-    rf, xf = _run("first")
-    rl, xl = _run("learned")
-    rlf, xlf = _run("learned+first")
+    runs = {p: _run(p) for p in ("zeroth", "first", "secant", "learned", "learned+first")}
+    xz = runs["zeroth"][1]
     scale = np.abs(xz).max()
-    for xo in (xf, xl, xlf):
-        assert np.abs(xo - xz).max() <= 1e-8 * scale
-    its = {name: sum(r["newton_its"] for r in recs[1:])
-           for name, recs in (("zeroth", rz), ("first", rf), ("learned", rl),
-                              ("learned+first", rlf))}
+    for name, (_, xo) in runs.items():
+        assert np.abs(xo - xz).max() <= 1e-8 * scale, name
+    its = {n: sum(r["newton_its"] for r in recs[1:]) for n, (recs, _) in runs.items()}
+    rl = runs["learned"][0]
     print("newton iterations over the sweep:", its)
-    print("learned-step guesses:", [r["guess"] for r in rl[1:]])
+    print("per-step Newton iterations:",
+          {n: [r["newton_its"] for r in recs[1:]] for n, (recs, _) in runs.items()})
+    print("learned-run guesses:", [r["guess"] for r in rl[1:]])
+    print("learned-run candidate residuals:", [r["candidates"] for r in rl[1:]])
     assert its["first"] <= its["zeroth"]
+    assert its["secant"] <= its["zeroth"]
+    assert its["learned"] <= its["secant"]
     assert its["learned+first"] <= its["first"]
-    # the network's own gain over the method without it
-    assert any(r["guess"] == "learned" for r in rl[1:])
-    assert its["learned"] < its["zeroth"]
+    # the network's own gain over the secant guess it corrects: wherever both
+    # guesses were formed, the learned one's residual relative to the secant's
+    ratios = [r["candidates"]["learned"] / r["candidates"]["secant"] for r in rl[1:]
+              if "learned" in r["candidates"] and "secant" in r["candidates"]]
+    print("learned / secant guess residual per step:", ["%.3g" % q for q in ratios])
+    assert ratios, "the network never produced a guess"
+    assert min(ratios) < 0.9
+    gm = math.exp(sum(math.log(min(q, 1.0)) for q in ratios) / len(ratios))
+    assert gm < 1.0
