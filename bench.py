@@ -10,10 +10,11 @@ scatter, at a seeded synthetic state.
   value  elements/s with x, R and the matrix resident in HBM
   e2e    elements/s through the C ABI with host buffers: x copied in, R and
          the Jacobian (reference MSR layout) copied out, every step
-  roofline  the element kernel: algorithmic FP64 flops per launch
-         (2 Q n_loc^2 (d+1) per element) / measured kernel time, against
-         this GPU's FP64 tensor-pipe (DMMA) throughput measured in-process;
-         HBM view of the same launch alongside
+  roofline  the element kernel: the FP64 operations its algorithm performs
+         per launch (element_flops) / measured kernel time, against this
+         GPU's FP64 throughput measured in-process (scalar FMA and mma.sync
+         f64 run at the same rate); the dense-equivalent rate and the HBM
+         view of the same launch alongside
   cpu_baseline  the CPU oracle (a restatement of the reference's
          matrix_fill) on an 8^3-element block of the same problem
 
@@ -184,6 +185,30 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10):
     return out
 
 
+def element_flops(path):
+    """FP64 operations (FMA = 2) per 32^3-workload element (HEX27, NS + energy,
+    Jacobian) of the element kernel of `path`, counted from its algorithm.
+
+    Path 4 (sum factorisation, the automatic path): isoparametric passes
+    7 fields x (2 + 3 + 4) x 27 outputs x 5; per-point set-up ~263 x 27;
+    gradient tables 729 x 18; sum-factorisation stages 16 x (81 + 243) x 5;
+    residual rows 108 x 27 x 8; J_mP 324 x 27 x 2; upper triangle of the
+    81 x 81 gradient product 3,321 x 27 x 2; node pairs 729 x 113.
+    Paths 1-3 do the dense quadrature-point contractions: 2 Q n_loc^2 (d+1)."""
+    if path in (0, 4):
+        iso = 7 * (2 + 3 + 4) * 27 * 5
+        qp = 263 * 27
+        tables = 729 * 18
+        stages = 16 * (81 + 243) * 5
+        resid = 108 * 27 * 8
+        jmp = 324 * 27 * 2
+        h = 3321 * (27 * 2 + 2)
+        pairs = 729 * 113
+        return float(iso + qp + tables + stages + resid + jmp + h + pairs)
+    nloc = 4 * 27 + 4
+    return 2.0 * 27 * nloc * nloc * 4
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path.  The reference C compiles
     only where its source tree is (oracle/_ref, not on the GPU machine), so
@@ -219,9 +244,9 @@ def main():
     ap.add_argument("--nel", type=int, default=NEL)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--path", type=int, default=0,
-                    help="element kernel: 0 automatic (3), 1 scalar FP64, 2 FP64 tensor pipe "
+                    help="element kernel: 0 automatic (4), 1 scalar FP64, 2 FP64 tensor pipe "
                          "with per-fragment coefficients, 3 FP64 tensor-pipe products over "
-                         "operand tables")
+                         "operand tables, 4 sum factorisation")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
     args = ap.parse_args()
@@ -247,8 +272,9 @@ def main():
     gn = GomaNewton(prob)
     gn.set_assembly_path(args.path)
     kernel_name = {1: "assemble_kernel<3,energy> (scalar FP64)",
-                   2: "assemble_tc_kernel<energy> (FP64 DMMA, per-fragment coefficients)"}.get(
-        args.path, "assemble_gemm_kernel<energy> (FP64 DMMA products over operand tables)")
+                   2: "assemble_tc_kernel<energy> (FP64 DMMA, per-fragment coefficients)",
+                   3: "assemble_gemm_kernel<energy> (FP64 DMMA products over operand tables)"}.get(
+        args.path, "assemble_sf_kernel<energy> (sum factorisation, FP64)")
     L = gn._L
     N, nnz, msr_len = gn.N, gn.nnz, gn.msr_len
     x_host = gn.dirichlet_init(np.random.default_rng(11).uniform(-1.0, 1.0, N))
@@ -326,11 +352,15 @@ def main():
     per_launch_ms = kms.value / max(kl.value, 1)
     elems_per_launch = elems / gn.num_colors
     nloc = 4 * 27 + 4
-    flop_el = 2.0 * 27 * nloc * nloc * 4
+    dense_flop_el = 2.0 * 27 * nloc * nloc * 4
+    flop_el = element_flops(args.path)
     achieved_tf = flop_el * elems_per_launch / (per_launch_ms * 1e-3) / 1e12
     dmma = ctypes.c_double()
     fma = ctypes.c_double()
+    dmma_var = ctypes.c_double()
     _lib.check(L.gb_probe_fp64_peaks(ctypes.byref(dmma), ctypes.byref(fma)))
+    _lib.check(L.gb_probe_dmma_varying(ctypes.byref(dmma_var)))
+    fp64_peak = max(fma.value, dmma_var.value)
     peaks = read_peaks()
     # algorithmic bytes of one launch: its share of the matrix values written,
     # R, x, connectivity and coordinates
@@ -338,15 +368,25 @@ def main():
     bytes_asm = 8 * nnz + 8 * N + 8 * N + 4 * elems * 27 + 8 * 3 * nodes
     bytes_launch = bytes_asm / gn.num_colors
     hbm_gbs = bytes_launch / (per_launch_ms * 1e-3) / 1e9
-    roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": dmma.value,
-                "unit": "TFLOP/s", "frac": achieved_tf / dmma.value,
+    roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak,
                 "traffic": None,
                 "kernel": "%s, one colour, %d elements" % (kernel_name, elems_per_launch),
                 "launch_ms": per_launch_ms,
                 "flop_per_element": flop_el,
-                "peak_source": "FP64 mma.sync m8n8k4 (DMMA) throughput measured in-process on "
-                               "this GPU (MEASURED_PEAKS.json has HBM and bf16 only)",
-                "fp64_fma_peak_tflops": fma.value,
+                "flop_count": "FP64 operations the kernel's algorithm performs per element "
+                              "(FMA = 2), counted term by term",
+                "pipe": "FP64 (scalar FMA and mma.sync f64 run at the same rate on GB300)",
+                "peak_source": "FP64 throughput measured in-process on this GPU (best of scalar "
+                               "FMA chains and mma.sync m8n8k4 f64 with changing operands; "
+                               "MEASURED_PEAKS.json has HBM and bf16 only)",
+                "fp64_fma_tflops": fma.value, "fp64_dmma_tflops": dmma_var.value,
+                "fp64_dmma_constant_operands_tflops": dmma.value,
+                "dense_equivalent": {"flop_per_element": dense_flop_el,
+                                     "tflops": dense_flop_el * elems_per_launch /
+                                     (per_launch_ms * 1e-3) / 1e12,
+                                     "note": "2 Q n_loc^2 (d+1): the same Jacobian by dense "
+                                             "quadrature-point contractions"},
                 "hbm_view": {"achieved_gbs": hbm_gbs, "peak_gbs": peaks.get("hbm_gbs"),
                              "frac": hbm_gbs / peaks.get("hbm_gbs", 6800.0),
                              "bytes_per_launch": bytes_launch}}

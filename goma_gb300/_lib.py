@@ -78,6 +78,7 @@ def load():
         "gb_linear_solve_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.POINTER(NewtonOpts), ip,
                                                   dp]),
         "gb_probe_fp64_peaks": (ctypes.c_int, [dp, dp]),
+        "gb_probe_dmma_varying": (ctypes.c_int, [dp]),
         "gb_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_ulonglong, ctypes.POINTER(vp)]),
         "gb_mlp_destroy": (None, [vp]),

@@ -12,12 +12,12 @@ steady problem (density / Reynolds number, or any parameter set_param sets):
   :3753, :3796);
 - ``secant``: first-order extrapolation through the last two converged
   solutions (no tangent solve);
-- ``learned``: the secant guess plus a curvature correction predicted by a
-  3 x 256 tanh network (GPU, FP32, trained online by the library's own
-  kernels on the secant errors of the earlier steps).  The plain secant
-  guess is the fallback: the learned guess is used only when its FP64
-  scaled residual is smaller, and the Newton solve always decides the
-  answer;
+- ``learned``: the secant guess with a correction of the rate of change
+  predicted, unknown by unknown, by a 3 x 256 tanh network from the recent
+  rate history (GPU, FP32, trained online by the library's own kernels on
+  the earlier steps of the sweep).  The plain secant guess is the
+  fallback: the learned guess is used only when its FP64 scaled residual
+  is smaller, and the Newton solve always decides the answer;
 - ``learned+first``: as ``learned``, with the tangent guess as a third
   candidate.
 
@@ -33,9 +33,9 @@ from .newton import GomaNewton
 
 
 class FieldLayout:
-    """Where each unknown lives: the nodal unknowns (velocity, temperature,
-    species) at every node, and the P1 pressure unknowns at each element's
-    centroid node."""
+    """Where each unknown lives: its node and its position in the node's
+    block of unknowns (the nodal fields, then at centroid nodes the P1
+    pressures)."""
 
     def __init__(self, gn: GomaNewton):
         import ctypes
@@ -46,73 +46,47 @@ class FieldLayout:
         nn = p.mesh.num_nodes
         fu = np.empty(nn + 1, np.int32)
         _lib.check(gn._L.gb_first_unknown(gn.h, fu.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
-        self.fu = fu
         cnt = np.diff(fu)
-        self.nvn = int(cnt.min())
-        self.n_out = self.nvn + p.dim + 1
-        # feature scaling: coordinates to [-1, 1]
+        self.N = int(fu[-1])
+        self.nfield = int(cnt.max())
+        self.node = np.repeat(np.arange(nn), cnt)
+        self.field = np.arange(self.N) - np.repeat(fu[:-1], cnt)
         c = p.mesh.coords
         lo = c.min(axis=0)
         span = np.maximum(c.max(axis=0) - lo, 1e-300)
-        self.coords11 = (c - lo) / span * 2.0 - 1.0
-        self.is_cent = cnt > self.nvn
-        self.cn = np.nonzero(self.is_cent)[0]
-
-    def targets(self, x):
-        """(n_nodes, n_out) per-node values and their mask from an unknown
-        vector (the pressure columns exist at centroid nodes only)."""
-        nn = len(self.fu) - 1
-        T = np.zeros((nn, self.n_out))
-        M = np.zeros((nn, self.n_out), np.float32)
-        for a in range(self.nvn):
-            T[:, a] = x[self.fu[:-1] + a]
-            M[:, a] = 1.0
-        for l in range(self.dim + 1):
-            T[self.cn, self.nvn + l] = x[self.fu[self.cn] + self.nvn + l]
-            M[self.cn, self.nvn + l] = 1.0
-        return T, M
-
-    def assemble(self, Y, N):
-        """Unknown vector from (n_nodes, n_out) per-node values."""
-        x = np.zeros(N)
-        for a in range(self.nvn):
-            x[self.fu[:-1] + a] = Y[:, a]
-        for l in range(self.dim + 1):
-            x[self.fu[self.cn] + self.nvn + l] = Y[self.cn, self.nvn + l]
-        return x
+        self.coords11 = ((c - lo) / span * 2.0 - 1.0)[self.node]
 
 
 class LearnedPredictor:
-    """Secant predictor plus a learned correction for the curvature of the
-    solution path.
+    """Learned extrapolation along the sweep, one unknown at a time.
 
-    The secant predictor (the cheap first-order predictor, with no tangent
-    solve; ALC_FIRST of src/ac_conti.c:759 uses a tangent instead) misses
-    the second-order part of x(lambda): its error on a path with curvature
-    x''/2 = c is c h (h + h_prev) for a step h after a step h_prev.  A
-    network over (x, y[, z], lambda) is trained online, on the GPU by the
-    library's own kernels, on the secant errors of every earlier step
-    divided by h (h + h_prev) -- samples of the curvature field c -- and the
-    guess for the next step is
+    For every unknown the network sees the rate of change of the last step
+    r1 = (x_k - x_{k-1}) / h1, how that rate changed over the step before,
+    (r1 - r2) (h + h1) / (h1 + h2), which field it belongs to and where its
+    node is, and predicts the change of the rate over the next step,
+    r - r1.  The guess is the secant guess corrected by it:
 
-        x_guess = secant(lam) + h (h + h_prev) * net(coords, lam).
+        x_guess = x_k + h (r1 + net(...)).
 
-    A fit error in c costs only that fraction of the secant error, so the
-    learned guess improves on the secant wherever the curvature field
-    carries over from one step to the next."""
+    A zero network is the secant predictor (the cheap first-order
+    predictor, with no tangent solve; ALC_FIRST of src/ac_conti.c:759 uses a
+    tangent instead), and a network that answers the rate change itself is
+    quadratic extrapolation; trained online (on the GPU, by the library's
+    own kernels) on every earlier step of the sweep, it learns how the
+    rates of this problem's fields actually evolve.  Inputs and targets are
+    scaled per field by the RMS of r1."""
 
     def __init__(self, gn, lam_range, width=256, hidden=3, seed=0, steps=1500, batch=4096,
                  lr=2e-3, log_lambda=False):
         from .mlp import GpuMLP
         self.lay = FieldLayout(gn)
         self.N = gn.N
-        self.net = GpuMLP(self.lay.dim + 1, width, hidden, self.lay.n_out, seed=seed)
+        self.n_in = 2 + self.lay.nfield + self.lay.dim
+        self.net = GpuMLP(self.n_in, width, hidden, 1, seed=seed)
         self.log_lambda = log_lambda
-        self.lmin, self.lmax = self._t(lam_range[0]), self._t(lam_range[1])
         self.steps, self.batch, self.lr = steps, batch, lr
         self.sols = []
-        self.X, self.T, self.M = [], [], []
-        self.tscale = None
+        self.X, self.T = [], []
         self.trained = 0
 
     def _t(self, lam):
@@ -120,39 +94,42 @@ class LearnedPredictor:
         log lambda."""
         return math.log(lam) if self.log_lambda else float(lam)
 
-    def _features(self, t):
-        s = (t - self.lmin) / max(self.lmax - self.lmin, 1e-300) * 2.0 - 1.0
-        c = self.lay.coords11
-        return np.hstack([c, np.full((c.shape[0], 1), s)]).astype(np.float32)
+    def _sigma(self, r1):
+        f = self.lay.field
+        ms = np.bincount(f, weights=r1 * r1, minlength=self.lay.nfield)
+        n = np.maximum(np.bincount(f, minlength=self.lay.nfield), 1)
+        s = np.sqrt(ms / n)
+        return np.where(s > 0, s, 1.0)[f]
 
-    def secant(self, lam):
-        """First-order extrapolation through the last two recorded solutions
-        (the last solution itself while only one is known)."""
-        t = self._t(lam)
-        tk, xk = self.sols[-1]
-        if len(self.sols) < 2:
-            return xk.copy()
-        tp, xp = self.sols[-2]
-        return xk + (t - tk) * (xk - xp) / (tk - tp)
+    def _features(self, r1, dr, sig):
+        lay = self.lay
+        X = np.zeros((self.N, self.n_in), np.float32)
+        X[:, 0] = r1 / sig
+        X[:, 1] = dr / sig
+        X[np.arange(self.N), 2 + lay.field] = 1.0
+        X[:, 2 + lay.nfield:] = lay.coords11
+        return X
 
-    def _hh(self, t):
-        tk = self.sols[-1][0]
-        tp = self.sols[-2][0]
-        h, hp = t - tk, tk - tp
-        return h * (h + hp)
+    def _history(self, t_next, upto):
+        """Rates r1, r2 and the scaled rate change for predicting the step to
+        t_next from the first `upto` recorded solutions."""
+        (t2, x2), (t1, x1), (t0, x0) = self.sols[upto - 3], self.sols[upto - 2], self.sols[upto - 1]
+        h1, h2, h = t0 - t1, t1 - t2, t_next - t0
+        r1 = (x0 - x1) / h1
+        r2 = (x1 - x2) / h2
+        return r1, (r1 - r2) * (h + h1) / (h1 + h2), h
 
     def add(self, lam, x):
-        """Record a converged solution; once two earlier ones are known, the
-        secant predictor's error at this one becomes a training sample."""
+        """Record a converged solution; once three earlier ones are known, the
+        step to this one becomes a training sample (a row per unknown)."""
         t = self._t(lam)
         x = np.array(x, np.float64)
-        if len(self.sols) >= 2:
-            hh = self._hh(t)
-            if hh != 0.0:
-                T, M = self.lay.targets((x - self.secant(lam)) / hh)
-                self.X.append(self._features(t))
-                self.T.append(T)
-                self.M.append(M)
+        if len(self.sols) >= 3:
+            r1, dr, h = self._history(t, len(self.sols))
+            sig = self._sigma(r1)
+            r = (x - self.sols[-1][1]) / h
+            self.X.append(self._features(r1, dr, sig))
+            self.T.append(((r - r1) / sig).astype(np.float32)[:, None])
         self.sols.append((t, x))
 
     @property
@@ -163,18 +140,9 @@ class LearnedPredictor:
         import torch
         if not self.X:
             return None
-        X = np.vstack(self.X)
-        T = np.vstack(self.T)
-        M = np.vstack(self.M)
-        # per-output standardisation, refreshed with the data
-        mu = (T * M).sum(0) / np.maximum(M.sum(0), 1)
-        sd = np.sqrt((((T - mu) * M) ** 2).sum(0) / np.maximum(M.sum(0), 1))
-        sd = np.where(sd > 0, sd, 1.0)
-        self.tscale = (mu, sd)
-        Tn = ((T - mu) / sd).astype(np.float32) * M
-        dx = torch.tensor(X, device="cuda")
-        dt = torch.tensor(Tn, device="cuda")
-        dm = torch.tensor(M, device="cuda")
+        dx = torch.tensor(np.vstack(self.X), device="cuda")
+        dt = torch.tensor(np.vstack(self.T), device="cuda")
+        dm = torch.ones_like(dt)
         # Adam at the given rate, then a quarter as many steps at a tenth of it
         self.net.train(dx, dt, dm, steps=self.steps, batch=self.batch, lr=self.lr, seed=seed)
         loss = self.net.train(dx, dt, dm, steps=max(self.steps // 4, 1), batch=self.batch,
@@ -182,16 +150,14 @@ class LearnedPredictor:
         self.trained += 1
         return loss
 
-    def curvature(self, lam):
-        """The network's curvature field at lam, as an unknown vector."""
-        import torch
-        X = torch.tensor(self._features(self._t(lam)), device="cuda")
-        Y = self.net.forward(X).double().cpu().numpy()
-        mu, sd = self.tscale
-        return self.lay.assemble(Y * sd + mu, self.N)
-
     def predict(self, lam):
-        return self.secant(lam) + self._hh(self._t(lam)) * self.curvature(lam)
+        import torch
+        t = self._t(lam)
+        r1, dr, h = self._history(t, len(self.sols))
+        sig = self._sigma(r1)
+        X = torch.tensor(self._features(r1, dr, sig), device="cuda")
+        corr = self.net.forward(X).double().cpu().numpy()[:, 0] * sig
+        return self.sols[-1][1] + h * (r1 + corr)
 
 
 def _set_density(gn, rho):
@@ -250,7 +216,7 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
     """Sweep lambda from lam0 to lam1 in nsteps steps (uniform in lambda, or
     in log lambda with spacing="log").  predictor: "zeroth" (ALC_ZEROTH),
     "first" (ALC_FIRST), "secant", "learned" (secant + the network's
-    curvature correction, secant fallback) or "learned+first" (the same
+    rate correction, secant fallback) or "learned+first" (the same
     with the tangent guess as another candidate).  Among several candidate
     guesses the one with the smallest FP64 scaled residual is used.  A step
     whose Newton solve fails is halved and re-predicted from the last

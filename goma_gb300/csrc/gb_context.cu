@@ -110,6 +110,7 @@ Context::~Context() {
                   d_tab_pt, d_tab_iso, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (d_sf) cudaFree(d_sf);
   if (ev_k0) cudaEventDestroy(ev_k0);
   if (ev_k1) cudaEventDestroy(ev_k1);
   if (stream) cudaStreamDestroy(stream);
@@ -181,6 +182,15 @@ int Context::init(const gb_problem_desc *d) {
     std::vector<double> iso(112 * 28);
     build_iso_table(tphi.data(), tdphi.data(), iso.data());
     if (upload(&d_tab_iso, iso, "tab")) return -1;
+    double ell[9], dell[9];
+    for (int a = 0; a < 3; a++)
+      for (int g = 0; g < 3; g++) {
+        ell[a * 3 + g] = lag(a, kPt[g]);
+        dell[a * 3 + g] = dlag(a, kPt[g]);
+      }
+    std::vector<SfTables> sft(1);
+    build_sf_tables(tphi.data(), tdphi.data(), kLoc27, ell, dell, sft[0]);
+    if (upload(&d_sf, sft, "tab")) return -1;
   }
   if ((e = cudaMalloc(&d_x, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "x");
   if ((e = cudaMalloc(&d_R, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "R");
@@ -238,7 +248,10 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
   }
   for (int c = 0; c < ncol; c++) {
     const int n = L.color_ptr[c + 1] - L.color_ptr[c];
-    if (kp == 3)
+    if (kp == 4)
+      e = launch_assemble_sf(a, L.energy != 0, d_sf, d_color_elems + L.color_ptr[c], n, tc_grid,
+                             st);
+    else if (kp == 3)
       e = launch_assemble_gemm(a, L.energy != 0, d_tab_iso, d_color_elems + L.color_ptr[c], n,
                                tc_grid, st);
     else if (kp == 2)
@@ -268,7 +281,8 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
 int Context::kernel_path(bool jacobian) const {
   if (L.dim != 3) return 1;
   const bool gemm_ok = !carreau && mat.viscosity > 0.0;
-  if (path == 0 || path == 3) return gemm_ok ? 3 : 1;
+  if (path == 0) return gemm_ok ? 4 : 1;
+  if (path == 3 || path == 4) return gemm_ok ? path : 1;
   return jacobian ? path : 1;
 }
 
@@ -411,9 +425,10 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 }
 
 int gb_set_assembly_path(gb_ctx *ctx, int path) {
-  if (!ctx || path < 0 || path > 3)
+  if (!ctx || path < 0 || path > 4)
     return fail("path must be 0 (auto), 1 (scalar FP64), 2 (FP64 tensor pipe, per-fragment "
-                "coefficients) or 3 (FP64 tensor pipe, operand tables; 3-D Newtonian)");
+                "coefficients), 3 (FP64 tensor pipe, operand tables; 3-D Newtonian) or 4 (sum "
+                "factorisation; 3-D Newtonian)");
   ctx->c.path = path;
   return 0;
 }

@@ -21,9 +21,9 @@ struct Context {
   Layout L;
   MaterialDev mat{};
   bool carreau = false;
-  // element kernel: 0 automatic (3 where it applies, else 1), 1 scalar FP64,
+  // element kernel: 0 automatic (4 where it applies, else 1), 1 scalar FP64,
   // 2 DMMA with per-fragment coefficients, 3 DMMA products over operand tables
-  // (3-D Newtonian)
+  // (3-D Newtonian), 4 sum factorisation (3-D Newtonian)
   int path = 0;
   int tc_grid = 0;     // persistent grid of the DMMA kernels
   int trsv = 0;        // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph
@@ -39,6 +39,7 @@ struct Context {
   uint16_t *d_nslot = nullptr;
   double *d_tab_phi = nullptr, *d_tab_dphi = nullptr, *d_tab_w = nullptr, *d_tab_pt = nullptr;
   double *d_tab_iso = nullptr;  // 3-D: [value, d/dxi_r] x points x nodes (gemm kernel)
+  SfTables *d_sf = nullptr;     // 3-D: tables of the sum-factorised kernel
   int *d_color_elems = nullptr;
   double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
   int *d_status = nullptr;

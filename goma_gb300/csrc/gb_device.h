@@ -56,6 +56,25 @@ cudaError_t launch_assemble_species(const AsmArgs &a, int dim, bool energy, bool
 // 3-D Jacobian contractions on the FP64 tensor pipe (gb_assemble_tc.cu)
 cudaError_t launch_assemble_tc(const AsmArgs &a, bool energy, bool carreau, const int *elems,
                                int nelem, int grid_cap, cudaStream_t st);
+// Constant tables of the sum-factorised 3-D kernel (gb_assemble_sf.cu), one
+// device copy per context: 1-D Lagrange factors at the Gauss points and their
+// pair products, phi and reference gradients in lexicographic node order, the
+// local <-> lexicographic node maps, and the (row, column) list of the upper
+// triangle of the 81 x 81 gradient product.
+struct SfTables {
+  double ell[2][3][3];
+  double pp[2][9][3];
+  double phi[27][27];
+  double dref[27][27][3];
+  int lex[27];
+  int loc[27];
+  uint16_t hmap[81 * 82 / 2];
+};
+void build_sf_tables(const double *tab_phi, const double *tab_dphi, const int (*loc27)[3],
+                     const double *ell, const double *dell, SfTables &T);
+cudaError_t launch_assemble_sf(const AsmArgs &a, bool energy, const SfTables *tb,
+                               const int *elems, int nelem, int grid_cap, cudaStream_t st);
+size_t assemble_sf_smem_bytes();
 // 3-D Newtonian residual + Jacobian as dense DMMA products (gb_assemble_gemm.cu);
 // tab_iso is build_iso_table's [112][28] table on the device
 cudaError_t launch_assemble_gemm(const AsmArgs &a, bool energy, const double *tab_iso,

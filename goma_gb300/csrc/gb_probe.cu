@@ -43,7 +43,59 @@ __global__ void probe_dmma(double *out, double s) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + d0 + d1 + e0 + e1 + f0 + f1;
 }
 
+// DMMA chains whose operands change every iteration (integer updates of the
+// low mantissa bits, so no FP64 instruction besides the mma itself): the
+// loop-invariant operands of probe_dmma can run faster than mma.sync on
+// operands that change, as in a real contraction.
+__global__ void probe_dmma_varying(double *out, double s) {
+  long long a0 = __double_as_longlong(1.0 + threadIdx.x * 1e-3), b0 = __double_as_longlong(s);
+  long long a1 = a0 ^ 3, b1 = b0 ^ 5, a2 = a0 ^ 6, b2 = b0 ^ 9, a3 = a0 ^ 12, b3 = b0 ^ 17;
+  double c0 = 0, c1 = 0, d0 = 0, d1 = 0, e0 = 0, e1 = 0, f0 = 0, f1 = 0;
+  for (int i = 0; i < kProbeIters / 4; i++) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(c0), "+d"(c1) : "d"(__longlong_as_double(a0)), "d"(__longlong_as_double(b0)));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(d0), "+d"(d1) : "d"(__longlong_as_double(a1)), "d"(__longlong_as_double(b1)));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(e0), "+d"(e1) : "d"(__longlong_as_double(a2)), "d"(__longlong_as_double(b2)));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                 : "+d"(f0), "+d"(f1) : "d"(__longlong_as_double(a3)), "d"(__longlong_as_double(b3)));
+    a0 ^= 0x11; b0 ^= 0x22; a1 ^= 0x33; b1 ^= 0x44; a2 ^= 0x55; b2 ^= 0x66; a3 ^= 0x77; b3 ^= 0x88;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + d0 + d1 + e0 + e1 + f0 + f1;
+}
+
 }  // namespace gb
+
+// TFLOP/s of the varying-operand DMMA probe (see probe_dmma_varying)
+extern "C" int gb_probe_dmma_varying(double *tflops) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256;
+  double *out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double) * blocks * threads);
+  if (e != cudaSuccess) return gb::cuda_fail(e, "probe buffer");
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  float best = 1e30f, ms;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(t0);
+    gb::probe_dmma_varying<<<blocks, threads>>>(out, 0.999);
+    cudaEventRecord(t1);
+    cudaEventSynchronize(t1);
+    cudaEventElapsedTime(&ms, t0, t1);
+    best = ms < best ? ms : best;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(out);
+  if (e != cudaSuccess) return gb::cuda_fail(e, "probe");
+  if (tflops) *tflops = 512.0 * gb::kProbeIters * (double)blocks * (threads / 32) / (best * 1e-3) / 1e12;
+  return 0;
+}
 
 extern "C" int gb_probe_fp64_peaks(double *dmma_tflops, double *fma_tflops) {
   int dev = 0, sms = 0;

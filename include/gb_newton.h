@@ -85,14 +85,16 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
 /* The library's CUDA stream (a cudaStream_t). */
 void *gb_stream(gb_ctx *ctx);
 
-/* Element-kernel path of later assemblies: 0 = automatic (3 where it
+/* Element-kernel path of later assemblies: 0 = automatic (4 where it
  * applies, else 1), 1 = scalar FP64, 2 = 3-D Jacobian contractions on the
  * FP64 tensor pipe (DMMA) with per-fragment coefficients, 3 = the whole 3-D
- * residual + Jacobian as DMMA products over shared-memory operand tables
- * (Newtonian viscosity; Carreau and 2-D elements use path 1).  A
- * residual-only assembly uses the same kernel as the full one under paths
- * 0, 1 and 3, so its R is bitwise the full assembly's; under path 2 it
- * uses path 1.  All give the same matrix to rounding. */
+ * residual + Jacobian as DMMA products over shared-memory operand tables,
+ * 4 = the 3-D residual + Jacobian by sum factorisation over the
+ * tensor-product basis (the fewest FP64 operations).  Paths 3 and 4 take
+ * Newtonian viscosity; Carreau and 2-D elements use path 1.  A residual-only
+ * assembly uses the same kernel as the full one under paths 0, 1, 3 and 4,
+ * so its R is bitwise the full assembly's; under path 2 it uses path 1.  All
+ * give the same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
 
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
@@ -239,6 +241,9 @@ int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const flo
  * mma.sync m8n8k4 f64 (tensor pipe) and scalar FMA.  The FP64 roofline
  * denominators of the element kernels. */
 int gb_probe_fp64_peaks(double *dmma_tflops, double *fma_tflops);
+/* FP64 mma.sync m8n8k4 throughput (TFLOP/s) with operands that change every
+ * iteration, as in a real contraction. */
+int gb_probe_dmma_varying(double *tflops);
 
 #ifdef __cplusplus
 }

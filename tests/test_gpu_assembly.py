@@ -122,13 +122,15 @@ def test_gpu_reports_inverted_element():
                                    conductivity=0.35, momentum_source=(0.0, 0.0, -4.0)),
                        True, list(pb.HEATED3D_BCS), (2, -0.1)),
 ], ids=["bouss3d", "carreau_t3d", "carreau_ns3d", "newt_ns3d_pert", "newt_t3d_const_src"])
-@pytest.mark.parametrize("path", [2, 3])
-def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn, path):
-    """3-D residuals and Jacobians on the FP64 tensor pipe (DMMA; path 2 with
-    per-fragment coefficients, path 3 as products over operand tables, which
-    takes Newtonian problems and hands Carreau ones to the scalar kernel)
-    equal the scalar-FP64 kernel's within 1e-12 (row-scaled), and all equal
-    the oracle.  A residual-only assembly gives the same R bit for bit."""
+@pytest.mark.parametrize("path", [2, 3, 4])
+def test_3d_element_kernels_agree(prob_fn, path):
+    """3-D residuals and Jacobians of the other element kernels (path 2: DMMA
+    with per-fragment coefficients; path 3: DMMA products over operand
+    tables; path 4: sum factorisation -- paths 3 and 4 take Newtonian
+    problems and hand Carreau ones to the scalar kernel) equal the
+    scalar-FP64 kernel's within 1e-12 (row-scaled), and all equal the oracle.
+    Under paths 3 and 4 a residual-only assembly gives the same R bit for
+    bit."""
     prob = prob_fn()
     o = oracle.Oracle(prob)
     gn = GomaNewton(prob)
@@ -144,5 +146,5 @@ def test_tensor_pipe_and_scalar_element_kernels_agree(prob_fn, path):
     assert gc.msr_row_scaled_error(ija, a_tc, ao) < TOL
     assert np.abs(R_tc - Ro).max() <= TOL * np.abs(Ro).max()
     assert np.abs(R_tc - R_sc).max() <= TOL * np.abs(Ro).max()
-    if path == 3:
+    if path in (3, 4):
         assert np.array_equal(R_res, R_tc)
