@@ -96,6 +96,7 @@ def load():
                                                fp]),
         "gb_set_material": (ctypes.c_int, [vp, vp]),
         "gb_set_assembly_path": (ctypes.c_int, [vp, ctypes.c_int]),
+        "gb_set_element_density": (ctypes.c_int, [vp, dp]),
         "gb_set_triangular_solve": (ctypes.c_int, [vp, ctypes.c_int]),
         "gb_ilu0_factors": (ctypes.c_int, [vp, dp, ctypes.c_int, dp]),
         "gb_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int, dp, llp]),

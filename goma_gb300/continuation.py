@@ -257,7 +257,9 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
         lam = targets[k]
         t0 = time.perf_counter()
         halvings = 0
+        pred_s = cand_s = res_s = 0.0
         while True:
+            tp = time.perf_counter()
             cands = {}
             if secant and len(hist) >= 2:
                 (lp_, xp_), (lk_, xk_) = hist[-2], hist[-1]
@@ -275,6 +277,8 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
             set_param(gn, lam)
             if learned and lp.trained:
                 cands["learned"] = gn.dirichlet_init(lp.predict(lam))
+            tr = time.perf_counter()
+            cand_s += tr - tp
             res = {}
             if len(cands) > 1:
                 for name, xc in cands.items():
@@ -283,6 +287,8 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
             else:
                 choice = next(iter(cands))
             guess = gn.dirichlet_init(cands[choice])
+            res_s += time.perf_counter() - tr
+            pred_s += time.perf_counter() - tp
             x, conv, st = gn.solve_nonlinear_problem(guess, **newton_opts)
             if conv:
                 break
@@ -292,14 +298,19 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
             lam = 0.5 * (lam_old + lam)
             targets.insert(k, lam)
         hist.append((lam, x))
+        train_s = 0.0
         if lp is not None:
+            tt = time.perf_counter()
             lp.add(lam, x)
             if k + 1 < len(targets) and lp.ready:
                 lp.train(seed=len(records))
+            train_s = time.perf_counter() - tt
         wall = time.perf_counter() - t0
         records.append({"lam": float(lam), "guess": choice, "newton_its": st["newton_its"],
                         "linear_its": st["linear_its"], "guess_residual": res.get(choice),
                         "candidates": res, "halvings": halvings, "wall_s": wall,
+                        "predictor_s": pred_s, "candidates_s": cand_s, "residuals_s": res_s,
+                        "train_s": train_s,
                         "newton_ms": {k2: st[k2] for k2 in ("assemble_ms", "scale_ms",
                                                             "factor_ms", "solve_ms",
                                                             "total_ms")}})

@@ -54,6 +54,7 @@ struct ElemSmem {
   double Pn[Q2<DIM>::NP];
   int nodes[Q2<DIM>::NN];
   int e;
+  double rho;  // density of this element
   QP<DIM> qp[Q2<DIM>::NQ];
   QN<DIM, CARREAU> qn[Q2<DIM>::NQ][Q2<DIM>::NN];
 };
@@ -83,7 +84,10 @@ __global__ void __launch_bounds__(256)
     const int n = A.conn[(int64_t)e * NN + k];
     Elem &E = S[s];
     E.nodes[k] = n;
-    if (k == 0) E.e = e;
+    if (k == 0) {
+      E.e = e;
+      E.rho = A.elem_rho ? A.elem_rho[e] : M.density;
+    }
     const int f0 = A.fu[n];
 #pragma unroll
     for (int j = 0; j < DIM; j++) {
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(256)
     if (ebase + s >= nelem) continue;
     Elem &E = S[s];
     qp_setup<DIM, ENERGY, CARREAU>(E.X, E.U, E.Tn, E.Pn, q, tab_phi, tab_dphi, A.tab_w, A.tab_pt,
-                                   M, E.qp[q]);
+                                   M, E.rho, E.qp[q]);
   }
   __syncthreads();
 
@@ -127,8 +131,8 @@ __global__ void __launch_bounds__(256)
       vg = fma(Q.v[p], s2, vg);
     }
     W.phi = tab_phi[q * NN + k];
-    W.cK = -M.density * Q.dA * vg;
-    if (ENERGY) W.cT = -M.density * M.heat_capacity * Q.dA * vg;
+    W.cK = -E.rho * Q.dA * vg;
+    if (ENERGY) W.cT = -E.rho * M.heat_capacity * Q.dA * vg;
     if (CARREAU) {
 #pragma unroll
       for (int a = 0; a < DIM; a++) {
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(256)
       double adv = 0.0;
 #pragma unroll
       for (int p = 0; p < DIM; p++) adv = fma(Q.v[p], Q.gv[p][ra], adv);
-      adv = adv * M.density * (-Wi.phi * dA);
+      adv = adv * E.rho * (-Wi.phi * dA);
       double dif = 0.0;
 #pragma unroll
       for (int p = 0; p < DIM; p++)
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(256)
         vgT = fma(Q.v[p], Q.gT[p], vgT);
         dif = fma(Wi.g[p], -M.conductivity * Q.gT[p], dif);
       }
-      Racc += vgT * (-Wi.phi * M.density * M.heat_capacity * dA) + dif * dA;
+      Racc += vgT * (-Wi.phi * E.rho * M.heat_capacity * dA) + dif * dA;
     } else if (own_c) {
       double divv = 0.0;
 #pragma unroll
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int p = 0; p < DIM; p++) dot = fma(Wi.g[p], Wj.g[p], dot);
       const double pij = Wi.phi * Wj.phi * dA;
-      const double prho = -M.density * pij;
+      const double prho = -E.rho * pij;
       const double K = fma(Wi.phi, Wj.cK, nmu * dot);
 #pragma unroll
       for (int a = 0; a < DIM; a++)
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(256)
         }
       if (ENERGY) {
         JTT[m] += fma(Wi.phi, Wj.cT, nkdA * dot);
-        const double pc = -M.density * M.heat_capacity * pij;
+        const double pc = -E.rho * M.heat_capacity * pij;
 #pragma unroll
         for (int b = 0; b < DIM; b++) {
           JTv[m][b] = fma(pc, Q.gT[b], JTv[m][b]);

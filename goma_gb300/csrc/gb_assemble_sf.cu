@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(256, 2)
 
   for (int ei = blockIdx.x; ei < nelem; ei += gridDim.x) {
     const int e = elems[ei];
+    const double rho_e = A.elem_rho ? A.elem_rho[e] : M.density;
     __syncthreads();  // the previous element is done with shared memory
     // ---- nodal data (lexicographic order)
     if (tid < NN) {
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(256, 2)
         double P = 0.0;
 #pragma unroll
         for (int l = 0; l < NP; l++) P = fma(S.Pn[l], psi[l], P);
-        const double mu = M.viscosity, rho = M.density;
+        const double mu = M.viscosity, rho = rho_e;
         const double divv = gv[0][0] + gv[1][1] + gv[2][2];
 #pragma unroll
         for (int l = 0; l < NP; l++) {
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(256, 2)
           S.W[C_S1 + a][q] = -rho * dA * (v[0] * B[0][a] + v[1] * B[1][a] + v[2] * B[2][a]);
           double f = M.source[a];
           if (M.source_model == GB_SOURCE_BOUSSINESQ)
-            f = ENERGY ? M.density * M.source[a] * (-M.beta * (T - M.Tref)) : 0.0;
+            f = ENERGY ? rho * M.source[a] * (-M.beta * (T - M.Tref)) : 0.0;
           const double adv = v[0] * gv[0][a] + v[1] * gv[1][a] + v[2] * gv[2][a];
           S.cR[a][q] = dA * (f - rho * adv);
 #pragma unroll
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(256, 2)
 #pragma unroll
       for (int a = 0; a < 3; a++)
         dfT[a] = (ENERGY && M.source_model == GB_SOURCE_BOUSSINESQ)
-                     ? -M.density * M.source[a] * M.beta
+                     ? -rho_e * M.source[a] * M.beta
                      : 0.0;
       const uint16_t *ns = A.elem_nslot + (int64_t)e * NN * NN;
       for (int t = tid; t < NN * NN; t += nt) {

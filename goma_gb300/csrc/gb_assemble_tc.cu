@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256, 1)
     // phase 1: quadrature points
     if (tid < NQ)
       qp_setup<DIM, ENERGY, CARREAU>(S.X, S.U, S.Tn, S.Pn, tid, tab_phi, tab_dphi, A.tab_w,
-                                     A.tab_pt, M, S.qp[tid]);
+                                     A.tab_pt, M, M.density, S.qp[tid]);
     __syncthreads();
     // phase 2: tables and coefficients
     for (int t = tid; t < NQ * NN; t += blockDim.x) {

@@ -107,7 +107,8 @@ __global__ void csr_to_msr_kernel(int N, const int64_t *__restrict__ rowptr,
 Context::~Context() {
   void *ptrs[] = {d_coords, d_conn,   d_fu,     d_dbc,     d_dbc_val, d_rowptr, d_colidx,
                   d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nbr_node, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
-                  d_tab_pt, d_tab_iso, d_color_elems, d_x, d_R, d_vals, d_status, d_msr};
+                  d_tab_pt, d_tab_iso, d_color_elems, d_x, d_R, d_vals, d_status, d_msr,
+                  d_elem_rho};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (d_sf) cudaFree(d_sf);
@@ -226,6 +227,7 @@ AsmArgs Context::args(const double *x, double *R, double *vals) const {
   a.R = R;
   a.vals = vals;
   a.status = d_status;
+  a.elem_rho = d_elem_rho;
   a.pofs = L.nvn;
   a.mat = mat;
   return a;
@@ -281,6 +283,8 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
 int Context::kernel_path(bool jacobian) const {
   if (L.dim != 3) return 1;
   const bool gemm_ok = !carreau && mat.viscosity > 0.0;
+  // per-element densities: the scalar and the sum-factorised kernels only
+  if (d_elem_rho) return gemm_ok && path != 1 ? 4 : 1;
   if (path == 0) return gemm_ok ? 4 : 1;
   if (path == 3 || path == 4) return gemm_ok ? path : 1;
   return jacobian ? path : 1;
@@ -422,6 +426,23 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
   if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
   if (d_colidx) *d_colidx = ctx->c.d_colidx;
   return 0;
+}
+
+int gb_set_element_density(gb_ctx *ctx, const double *rho) {
+  if (!ctx) return fail("NULL argument");
+  Context &c = ctx->c;
+  if (!rho) {
+    if (c.d_elem_rho) cudaFree(c.d_elem_rho);
+    c.d_elem_rho = nullptr;
+    return 0;
+  }
+  for (int e = 0; e < c.L.num_elems; e++)
+    if (!(rho[e] > 0.0)) return fail("element densities must be positive");
+  cudaError_t err = cudaSuccess;
+  if (!c.d_elem_rho) err = cudaMalloc(&c.d_elem_rho, sizeof(double) * c.L.num_elems);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(c.d_elem_rho, rho, sizeof(double) * c.L.num_elems, cudaMemcpyHostToDevice);
+  return err == cudaSuccess ? 0 : cuda_fail(err, "element densities");
 }
 
 int gb_set_assembly_path(gb_ctx *ctx, int path) {

@@ -43,6 +43,7 @@ struct Context {
   int *d_color_elems = nullptr;
   double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
   int *d_status = nullptr;
+  double *d_elem_rho = nullptr;  // per-element density (gb_set_element_density); NULL: none
   double *d_msr = nullptr;
   std::unique_ptr<Solver> solver;
   // optional kernel timing of the element kernels (events on the launch stream)

@@ -41,6 +41,7 @@ struct AsmArgs {
   double *R;                   // N
   double *vals;                // nnz (CSR, diagonal in row); NULL: residual only
   int *status;                 // [0] non-positive det J count, [1] first such element
+  const double *elem_rho;      // per-element density (overrides mat.density); NULL: none
   int pofs;                    // offset of the first P1 pressure at a centroid node
                                // (= nodal fields per node: dim + energy + species)
   MaterialDev mat;

@@ -36,7 +36,8 @@ struct QP {
   int bad;
 };
 
-// Quadrature-point set-up (one thread per point): isoparametric map
+// Quadrature-point set-up (one thread per point), for an element of density
+// rho: isoparametric map
 // (beer_belly, src/mm_fill_util.c:140), J^-1 and det J, field values and
 // gradients (load_fv / load_fv_grads, src/load_field_variables.c:128,
 // :2049), viscosity (src/mm_viscosity.c:108, Carreau :981, shear rate
@@ -48,7 +49,7 @@ __device__ __forceinline__ void qp_setup(const double (*X)[DIM], const double (*
                                          const double *__restrict__ tab_dphi,
                                          const double *__restrict__ tab_w,
                                          const double *__restrict__ tab_pt, const MaterialDev &M,
-                                         QP<DIM> &Q) {
+                                         double rho, QP<DIM> &Q) {
   constexpr int NN = Q2<DIM>::NN, NP = Q2<DIM>::NP;
     double Jm[DIM][DIM], Gh[DIM][DIM], Th[DIM];
 #pragma unroll
@@ -166,8 +167,8 @@ __device__ __forceinline__ void qp_setup(const double (*X)[DIM], const double (*
       double f = 0.0, dfT = 0.0;
       if (M.source_model == GB_SOURCE_BOUSSINESQ) {
         if (ENERGY) {
-          f = M.density * M.source[a] * (-M.beta * (T - M.Tref));
-          dfT = -M.density * M.source[a] * M.beta;
+          f = rho * M.source[a] * (-M.beta * (T - M.Tref));
+          dfT = -rho * M.source[a] * M.beta;
         }
       } else {
         f = M.source[a];

@@ -187,6 +187,8 @@ int build_layout(const gb_problem_desc *d, Layout &L, std::string &err) {
     else if (var >= GB_VAR_Y(0) && var < GB_VAR_Y(0) + GB_MAX_SPECIES) {
       if (var - GB_VAR_Y(0) >= L.nspec) continue;
       off = d->dim + L.energy + (var - GB_VAR_Y(0));
+    } else if (var == GB_VAR_P) {
+      off = L.nvn;  // first pressure unknown of a centroid node
     } else {
       err = "Dirichlet card on an unsupported variable";
       return -1;
@@ -195,6 +197,10 @@ int build_layout(const gb_problem_desc *d, Layout &L, std::string &err) {
       int n = d->bc_nodes[q];
       if (n < 0 || n >= nnod) {
         err = "Dirichlet node outside the mesh";
+        return -1;
+      }
+      if (var == GB_VAR_P && L.fu[n + 1] - L.fu[n] <= L.nvn) {
+        err = "pressure card on a node without pressure unknowns (not an element centroid)";
         return -1;
       }
       L.dbc[L.fu[n] + off] = 1;

@@ -15,6 +15,7 @@
 // below the time of one Newton solve.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -28,6 +29,7 @@
 namespace gb {
 
 constexpr int TM = 64, TN = 64, TK = 16;
+constexpr int kMaxSplit = 32;  // batch splits of the weight-gradient product
 
 // C[M][N] = A[M][K] * B^T where B is [N][K]  (i.e. X W^T), + bias[N],
 // optional tanh.  Row-major everything.
@@ -122,22 +124,26 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// G[N][K] = D^T[N][M] * X[M][K]  (weight gradient dW = dZ^T H), reduction
-// over the batch M inside one block tile (deterministic).
+// G[N][K] = D^T[N][M] * X[M][K]  (weight gradient dW = dZ^T H).  The batch
+// M is split over blockIdx.z in chunks of mchunk rows; split z writes its
+// partial sum to G + z N K (reduce_splits_kernel adds them in a fixed
+// order, so the result is deterministic).
 __global__ void __launch_bounds__(256)
     gemm_dTx_kernel(int M, int N, int K, const float *__restrict__ D, const float *__restrict__ X,
-                    float *__restrict__ G) {
+                    float *__restrict__ G, int mchunk) {
   __shared__ float Ds[TK][TM + 4];
   __shared__ float Xs[TK][TN + 4];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const int n0 = blockIdx.y * TM, k0c = blockIdx.x * TN;
+  const int mb = blockIdx.z * mchunk, me = min(M, mb + mchunk);
+  G += (int64_t)blockIdx.z * N * K;
   float acc[4][4] = {};
-  for (int m0 = 0; m0 < M; m0 += TK) {
+  for (int m0 = mb; m0 < me; m0 += TK) {
     for (int t = threadIdx.x; t < TM * TK; t += 256) {
       const int mm = t / TM, nn = t % TM;
       const int gm = m0 + mm;
-      Ds[mm][nn] = (gm < M && n0 + nn < N) ? D[(int64_t)gm * N + n0 + nn] : 0.f;
-      Xs[mm][nn] = (gm < M && k0c + nn < K) ? X[(int64_t)gm * K + k0c + nn] : 0.f;
+      Ds[mm][nn] = (gm < me && n0 + nn < N) ? D[(int64_t)gm * N + n0 + nn] : 0.f;
+      Xs[mm][nn] = (gm < me && k0c + nn < K) ? X[(int64_t)gm * K + k0c + nn] : 0.f;
     }
     __syncthreads();
 #pragma unroll
@@ -163,6 +169,16 @@ __global__ void __launch_bounds__(256)
       const int gk = k0c + tx * 4 + j;
       if (gk < K) G[(int64_t)gn * K + gk] = acc[i][j];
     }
+  }
+}
+
+// g[i] = sum over the splits z (in order) of P[z][i]
+__global__ void reduce_splits_kernel(int nsplit, int n, const float *__restrict__ P,
+                                     float *__restrict__ g) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < nsplit; z++) s += P[(int64_t)z * n + i];
+    g[i] = s;
   }
 }
 
@@ -240,6 +256,7 @@ struct Mlp {
   float *d_dA = nullptr, *d_dB = nullptr;  // backward scratch [cap][maxw]
   float *d_part = nullptr, *h_part = nullptr;
   float *d_xb = nullptr, *d_tb = nullptr, *d_mb = nullptr;
+  float *d_split = nullptr;          // weight-gradient partial sums [kMaxSplit][maxw][maxw]
   int *d_idx = nullptr;
   int adam_t = 0;
   cudaStream_t st = nullptr;
@@ -256,6 +273,7 @@ struct Mlp {
     cudaFree(d_tb);
     cudaFree(d_mb);
     cudaFree(d_idx);
+    cudaFree(d_split);
     if (h_part) cudaFreeHost(h_part);
     if (st) cudaStreamDestroy(st);
   }
@@ -286,6 +304,9 @@ struct Mlp {
         cudaMalloc(&d_mb, sizeof(float) * (size_t)B * width.back()) != cudaSuccess ||
         cudaMalloc(&d_idx, sizeof(int) * (size_t)B) != cudaSuccess)
       return fail("MLP scratch");
+    if (!d_split &&
+        cudaMalloc(&d_split, sizeof(float) * (size_t)kMaxSplit * maxw() * maxw()) != cudaSuccess)
+      return fail("MLP scratch");
     cap = B;
     return 0;
   }
@@ -299,7 +320,8 @@ struct Mlp {
       in = act[l];
     }
   }
-  // gradient of sum mask (Y - T)^2 / sum(mask) into d_g; returns loss (host)
+  // gradient of sum mask (Y - T)^2 / sum(mask) into d_g; with loss != NULL
+  // also waits for and returns the loss (host)
   int backward(const float *X, const float *T, const float *Mk, int B, float msum, float *loss) {
     const int nl = layers(), no = width.back();
     const int nb = 64;
@@ -308,9 +330,18 @@ struct Mlp {
     for (int l = nl - 1; l >= 0; l--) {
       const int K = width[l], N = width[l + 1];
       const float *Hin = l == 0 ? X : act[l - 1];
-      // dW_l = dZ^T Hin  [N][K]; db_l = colsum dZ
-      dim3 g1((K + TN - 1) / TN, (N + TM - 1) / TM);
-      gemm_dTx_kernel<<<g1, 256, 0, st>>>(B, N, K, dcur, Hin, d_g + woff[l]);
+      // dW_l = dZ^T Hin  [N][K], the batch split over up to kMaxSplit CTA
+      // layers so that the grid covers the GPU; db_l = colsum dZ
+      const int nsplit = std::max(1, std::min(kMaxSplit, B / 128));
+      const int mchunk = ((B + nsplit - 1) / nsplit + TK - 1) / TK * TK;
+      dim3 g1((K + TN - 1) / TN, (N + TM - 1) / TM, nsplit);
+      if (nsplit == 1) {
+        gemm_dTx_kernel<<<g1, 256, 0, st>>>(B, N, K, dcur, Hin, d_g + woff[l], mchunk);
+      } else {
+        gemm_dTx_kernel<<<g1, 256, 0, st>>>(B, N, K, dcur, Hin, d_split, mchunk);
+        reduce_splits_kernel<<<(N * K + 255) / 256, 256, 0, st>>>(nsplit, N * K, d_split,
+                                                                  d_g + woff[l]);
+      }
       colsum_kernel<<<N, 256, 0, st>>>(B, N, dcur, d_g + boff[l]);
       if (l == 0) break;
       // dH_{l-1} = dZ W_l  [B][K]; dZ_{l-1} = dH * (1 - H^2)
@@ -321,6 +352,7 @@ struct Mlp {
       dcur = dnext;
       dnext = t;
     }
+    if (!loss) return 0;  // no loss wanted: nothing to wait for
     cudaMemcpyAsync(h_part, d_part, sizeof(float) * nb, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "MLP backward");
@@ -491,7 +523,9 @@ int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const flo
     gb::gather_rows_kernel<<<304, 256, 0, M.st>>>(B, no, M.d_idx, d_t, M.d_tb);
     gb::gather_rows_kernel<<<304, 256, 0, M.st>>>(B, no, M.d_idx, d_mask, M.d_mb);
     M.forward(M.d_xb, B);
-    if (M.backward(M.d_xb, M.d_tb, M.d_mb, B, (float)ms, &loss)) return -1;
+    // the loss is read back on the last step only: no per-step host wait
+    if (M.backward(M.d_xb, M.d_tb, M.d_mb, B, (float)ms, s + 1 == steps ? &loss : nullptr))
+      return -1;
     M.adam(lr, 0.9f, 0.999f, 1e-8f);
   }
   e = cudaStreamSynchronize(M.st);

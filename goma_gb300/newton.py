@@ -83,6 +83,16 @@ class GomaNewton:
         _lib.check(self._L.gb_dirichlet_init(self.h, _dp(x)))
         return x
 
+    def set_element_density(self, rho):
+        """Per-element densities (None: the material's) for later assemblies."""
+        if rho is None:
+            _lib.check(self._L.gb_set_element_density(self.h, None))
+            return
+        rho = np.ascontiguousarray(rho, np.float64)
+        if rho.shape != (self.problem.mesh.num_elems,):
+            raise ValueError("one density per element")
+        _lib.check(self._L.gb_set_element_density(self.h, _dp(rho)))
+
     # --- matrix_fill_full
     def matrix_fill_full(self, x, jacobian=True):
         """Host arrays in and out: returns (R, a_msr or None)."""

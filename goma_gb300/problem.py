@@ -272,6 +272,31 @@ def boussinesq_cube_3d(n, ra=1e5, pr=0.71, mesh=None):
     return Problem(mesh, mat, True, list(HEATED3D_BCS), (0, 0.0))
 
 
+# reacting channel: plug inflow at x = 0, no-slip walls y = 0, Ly, z = 0, Lz
+# (walls win at the inlet edges), outflow at x = Lx; hot feed of species 0
+REACTING3D_BCS = ([(VAR_U1, 1, 1.0), (VAR_U2, 1, 0.0), (VAR_U3, 1, 0.0)]
+                  + [(c, s, 0.0) for s in (3, 4, 5, 6) for c in (VAR_U1, VAR_U2, VAR_U3)]
+                  + [(VAR_T, 1, 2.0), (VAR_T, 3, 1.0), (VAR_T, 4, 1.0),
+                     (VAR_Y(0), 1, 1.0), (VAR_Y(1), 1, 0.0)])
+
+
+def reacting_channel_3d(nx, ny, nz, lx=2.0, ly=2.0, lz=1.0, seed=0, re=100.0, diffusivity=1e-3,
+                        activation=2.0, mesh=None):
+    """Channel flow with energy and two dilute species reacting A -> B at an
+    Arrhenius rate: HEX27 box [0, Lx] x [0, Ly] x [0, Lz], rho = Cp = 1,
+    mu = 1 / Re, k = 1 / Re, Fickian D for both species, source
+    S_0 = -k0 exp(-E / T) Y_0, S_1 = +k0 exp(-E / T) Y_0 with the rate
+    constant k0 drawn uniformly from [0.1, 10] by `seed`.  The outflow face
+    fixes the pressure level, so there is no pressure datum."""
+    mesh = mesh or box_mesh(3, nx, ny, nz, lx, ly, lz)
+    k0 = float(np.random.default_rng(seed).uniform(0.1, 10.0))
+    mat = Material(density=1.0, viscosity=1.0 / re, heat_capacity=1.0, conductivity=1.0 / re,
+                   diffusivity=(diffusivity, diffusivity),
+                   species_source=((SPECIES_SOURCE_ARRHENIUS, (k0, activation, -1.0, 0.0)),
+                                   (SPECIES_SOURCE_ARRHENIUS, (k0, activation, 1.0, 0.0))))
+    return Problem(mesh, mat, True, list(REACTING3D_BCS), (-1, 0.0), 2)
+
+
 def carreau_step_2d(nx, ny, re, lx=3.0, ly=1.0, mesh=None, mu0=1.0, mu_inf=0.01, lam=1.0,
                     aexp=2.0, nexp=0.5):
     """Channel with a plug inlet on the upper half of x = 0 and a wall on
@@ -280,3 +305,90 @@ def carreau_step_2d(nx, ny, re, lx=3.0, ly=1.0, mesh=None, mu0=1.0, mu_inf=0.01,
     mat = Material(density=re, viscosity_model=VISC_CARREAU, mu0=mu0, mu_inf=mu_inf, lam=lam,
                    aexp=aexp, nexp=nexp)
     return Problem(mesh, mat, False, list(BFS2D_BCS), (-1, 0.0))
+
+
+# ------------------------------------------------------------ batches
+
+@dataclass
+class BatchMember:
+    kind: str          # "cavity" or "channel"
+    n: int             # n x n QUAD9 elements on the unit square
+    re: float          # Reynolds number (rho = Re, mu = U = L = 1)
+    elems: Tuple[int, int]   # element range in the union
+    nodes: Tuple[int, int]   # node range in the union
+
+
+@dataclass
+class ProblemBatch:
+    problem: Problem            # the disjoint union, material density 1
+    elem_re: np.ndarray         # Reynolds number (density) of every element
+    members: List[BatchMember]
+
+
+def _member_bcs(kind, mesh, set_base, node_base):
+    """Node sets (global node ids) and Dirichlet cards of one member.  Cavity:
+    no-slip walls, lid u = 1 on y = 1, its first element's first pressure
+    pinned to 0.  Channel: parabolic inflow u = 4 y (1 - y) on x = 0 (one
+    node set per inlet node), no-slip on y = 0 and y = 1 (walls win at the
+    inlet corners), natural outflow on x = 1."""
+    sets = [s + node_base for s in mesh.node_sets]
+    bcs = []
+    if kind == "cavity":
+        for var, sid, val in CAVITY2D_BCS:
+            bcs.append((var, set_base + sid, val))
+        sets.append(np.array([node_base + mesh.conn[0, 8]], np.int32))
+        bcs.append((VAR_P, set_base + len(sets), 0.0))
+    else:
+        inlet = mesh.node_sets[3]
+        for nd in inlet:
+            y = mesh.coords[nd, 1]
+            sets.append(np.array([node_base + nd], np.int32))
+            bcs.append((VAR_U1, set_base + len(sets), 4.0 * y * (1.0 - y)))
+        for sid in (4,):
+            bcs.append((VAR_U2, set_base + sid, 0.0))
+        for sid in (1, 3):
+            bcs.append((VAR_U1, set_base + sid, 0.0))
+            bcs.append((VAR_U2, set_base + sid, 0.0))
+    return sets, bcs
+
+
+def batch_sweep_2d(num=512, seed=0, nmin=16, nmax=64, re_min=10.0, re_max=1000.0,
+                   kinds=("cavity", "channel")):
+    """`num` independent unit-square QUAD9 Q2/P1 problems drawn from `seed`:
+    mesh n x n with n uniform in [nmin, nmax], Re log-uniform in
+    [re_min, re_max], lid-driven cavity or channel alternately.  Returned as
+    one disjoint union (nodes, elements and unknowns of member p follow those
+    of member p - 1) with the per-element Reynolds numbers, so that one
+    context assembles and solves all of them together."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(nmin, nmax + 1, num)
+    res = np.exp(rng.uniform(np.log(re_min), np.log(re_max), num))
+    coords, conns, sets, bcs, rho, members = [], [], [], [], [], []
+    node_base = elem_base = 0
+    for p in range(num):
+        kind = kinds[p % len(kinds)]
+        m = box_mesh(2, int(ns[p]), int(ns[p]))
+        msets, mbcs = _member_bcs(kind, m, len(sets), node_base)
+        coords.append(m.coords + np.array([1.5 * p, 0.0]))
+        conns.append(m.conn + node_base)
+        sets.extend(msets)
+        bcs.extend(mbcs)
+        rho.append(np.full(m.num_elems, res[p]))
+        members.append(BatchMember(kind, int(ns[p]), float(res[p]),
+                                   (elem_base, elem_base + m.num_elems),
+                                   (node_base, node_base + m.num_nodes)))
+        node_base += m.num_nodes
+        elem_base += m.num_elems
+    mesh = Mesh(2, np.vstack(coords), np.ascontiguousarray(np.vstack(conns), np.int32), sets,
+                None)
+    prob = Problem(mesh, Material(density=1.0, viscosity=1.0), False, bcs, (-1, 0.0))
+    return ProblemBatch(prob, np.concatenate(rho), members)
+
+
+def batch_member_problem(batch, p):
+    """Member p of a batch as a problem of its own."""
+    mb = batch.members[p]
+    m = box_mesh(2, mb.n, mb.n)
+    sets, bcs = _member_bcs(mb.kind, m, 0, 0)
+    m.node_sets = sets
+    return Problem(m, Material(density=mb.re, viscosity=1.0), False, bcs, (-1, 0.0))

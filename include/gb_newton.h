@@ -97,6 +97,13 @@ void *gb_stream(gb_ctx *ctx);
  * give the same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
 
+/* Per-element density (num_elems values, > 0) for later assemblies, in
+ * place of the material's: lets one context hold several independent
+ * problems that differ in Reynolds number (rho = Re with mu = U = L = 1).
+ * rho = NULL returns to the material's density.  With per-element
+ * densities, 3-D elements use path 4 (or 1 when path 1 is set). */
+int gb_set_element_density(gb_ctx *ctx, const double *rho);
+
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
  * (one cooperative launch per factor; each node waits on flags of the
  * nodes it depends on, bounded, then publishes), 1 = level-scheduled

@@ -86,7 +86,9 @@ typedef struct gb_problem_desc {
   /* Dirichlet cards, applied in order (a later card wins on a shared
    * node): card c sets variable bc_var[c] to bc_value[c] on the nodes
    * bc_nodes[bc_ptr[c] .. bc_ptr[c+1]-1].  bc_var: GB_VAR_U1..U3, GB_VAR_T
-   * or GB_VAR_Y(w). */
+   * or GB_VAR_Y(w); GB_VAR_P on element centroid nodes pins the element's
+   * first pressure unknown, as PRESSURE DATUM does for one element
+   * (several independent problems held in one description each need one). */
   int num_bc;
   const int *bc_var;
   const double *bc_value;

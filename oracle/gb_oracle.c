@@ -240,6 +240,10 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
     } else if (var >= GB_VAR_Y(0)) {
       if (var - GB_VAR_Y(0) >= p->ns) continue;
       offv = dim + (desc->energy ? 1 : 0) + (var - GB_VAR_Y(0));
+    } else if (var == GB_VAR_P) {
+      /* first pressure unknown of a centroid node: PRESSURE DATUM of that
+         element (src/mm_bc.c:418), one per independent member of a batch */
+      offv = p->nvn;
     } else {
       offv = var;
     }
