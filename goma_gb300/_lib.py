@@ -97,6 +97,9 @@ def load():
         "gb_set_material": (ctypes.c_int, [vp, vp]),
         "gb_set_assembly_path": (ctypes.c_int, [vp, ctypes.c_int]),
         "gb_set_element_density": (ctypes.c_int, [vp, dp]),
+        "gb_set_ilu_ordering": (ctypes.c_int, [vp, ctypes.c_int]),
+        "gb_ilu_permutation_host": (ctypes.c_int, [vp, ip, ip, ip, ctypes.POINTER(ctypes.c_longlong),
+                                                   ip, ctypes.POINTER(ctypes.c_longlong)]),
         "gb_set_triangular_solve": (ctypes.c_int, [vp, ctypes.c_int]),
         "gb_ilu0_factors": (ctypes.c_int, [vp, dp, ctypes.c_int, dp]),
         "gb_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int, dp, llp]),

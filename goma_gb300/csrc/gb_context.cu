@@ -370,6 +370,26 @@ int gb_msr_pattern_host(const gb_problem_desc *desc, int *ija, long long *msr_le
   return 0;
 }
 
+int gb_ilu_permutation_host(const gb_problem_desc *desc, int *perm, int *num_colours, int *umap,
+                            long long *rowptr, int *colidx, long long *vmap) {
+  gb::Layout L, Lp;
+  if (gb::build_layout(desc, L, gb::g_err) != 0) return -1;
+  std::vector<int> pm, um;
+  std::vector<int64_t> vm;
+  const int nc = gb::multicolour_order(L, pm);
+  if (num_colours) *num_colours = nc;
+  if (perm) memcpy(perm, pm.data(), sizeof(int) * pm.size());
+  if (!umap && !rowptr && !colidx && !vmap) return 0;
+  gb::permute_layout(L, pm, Lp, um, vm);
+  if (umap) memcpy(umap, um.data(), sizeof(int) * um.size());
+  if (rowptr)
+    for (int i = 0; i <= Lp.N; i++) rowptr[i] = Lp.rowptr[i];
+  if (colidx) memcpy(colidx, Lp.colidx.data(), sizeof(int) * Lp.colidx.size());
+  if (vmap)
+    for (size_t k = 0; k < vm.size(); k++) vmap[k] = vm[k];
+  return 0;
+}
+
 int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx) {
   if (!ctx || !rowptr || !colidx) return fail("NULL argument");
   const gb::Layout &L = ctx->c.L;
@@ -425,6 +445,16 @@ int gb_device_buffers(gb_ctx *ctx, double **d_x, double **d_R, double **d_vals,
   if (d_vals) *d_vals = ctx->c.d_vals;
   if (d_rowptr) *d_rowptr = (const long long *)ctx->c.d_rowptr;
   if (d_colidx) *d_colidx = ctx->c.d_colidx;
+  return 0;
+}
+
+int gb_set_ilu_ordering(gb_ctx *ctx, int ordering) {
+  if (!ctx || (ordering != GB_ILU_NATURAL && ordering != GB_ILU_MULTICOLOUR))
+    return fail("ordering must be GB_ILU_NATURAL or GB_ILU_MULTICOLOUR");
+  if (ctx->c.ilu_ordering != ordering) {
+    ctx->c.ilu_ordering = ordering;
+    ctx->c.solver.reset();  // rebuilt for the new order at the next solve
+  }
   return 0;
 }
 

@@ -27,6 +27,7 @@ struct Context {
   int path = 0;
   int tc_grid = 0;     // persistent grid of the DMMA kernels
   int trsv = 0;        // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph
+  int ilu_ordering = 0;  // ILU(0) node order: 0 the reference's, 1 multicoloured
   cudaStream_t stream = nullptr;
   double *d_coords = nullptr;
   int *d_conn = nullptr;

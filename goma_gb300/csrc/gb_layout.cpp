@@ -262,3 +262,119 @@ void layout_msr_pattern(const Layout &L, int *ija) {
 }
 
 }  // namespace gb
+
+namespace gb {
+
+int multicolour_order(const Layout &L, std::vector<int> &perm) {
+  const int nn = L.num_nodes;
+  std::vector<char> cent(nn);
+  for (int n = 0; n < nn; n++) cent[n] = (L.fu[n + 1] - L.fu[n]) > L.nvn;
+  std::vector<int> colour(nn, -1);
+  int ncol[2] = {0, 0};
+  std::vector<char> used;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int n = 0; n < nn; n++) {
+      if (cent[n] != pass) continue;
+      used.assign(ncol[pass] + 1, 0);
+      for (int q = L.nbr_ptr[n]; q < L.nbr_ptr[n + 1]; q++) {
+        const int m = L.nbr_node[q];
+        if (cent[m] == pass && colour[m] >= 0) used[colour[m]] = 1;
+      }
+      int c = 0;
+      while (used[c]) c++;
+      colour[n] = c;
+      if (c + 1 > ncol[pass]) ncol[pass] = c + 1;
+    }
+  }
+  // order: non-centroid colours, then centroid colours; ascending node id within
+  std::vector<int> count(ncol[0] + ncol[1] + 1, 0);
+  auto key = [&](int n) { return cent[n] ? ncol[0] + colour[n] : colour[n]; };
+  for (int n = 0; n < nn; n++) count[key(n) + 1]++;
+  for (size_t k = 1; k < count.size(); k++) count[k] += count[k - 1];
+  perm.assign(nn, 0);
+  for (int n = 0; n < nn; n++) perm[n] = count[key(n)]++;
+  return ncol[0] + ncol[1];
+}
+
+void permute_layout(const Layout &L, const std::vector<int> &perm, Layout &Lp,
+                    std::vector<int> &umap, std::vector<int64_t> &vmap) {
+  const int nn = L.num_nodes;
+  std::vector<int> iperm(nn);
+  for (int n = 0; n < nn; n++) iperm[perm[n]] = n;
+  Lp.dim = L.dim;
+  Lp.nn = L.nn;
+  Lp.centroid = L.centroid;
+  Lp.nvn = L.nvn;
+  Lp.npres = L.npres;
+  Lp.nloc = L.nloc;
+  Lp.energy = L.energy;
+  Lp.nspec = L.nspec;
+  Lp.num_nodes = nn;
+  Lp.num_elems = L.num_elems;
+  Lp.N = L.N;
+  Lp.fu.assign(nn + 1, 0);
+  for (int np = 0; np < nn; np++) {
+    const int n = iperm[np];
+    Lp.fu[np + 1] = Lp.fu[np] + (L.fu[n + 1] - L.fu[n]);
+  }
+  umap.assign(L.N, 0);
+  for (int np = 0; np < nn; np++)
+    for (int d = 0; d < Lp.fu[np + 1] - Lp.fu[np]; d++) umap[Lp.fu[np] + d] = L.fu[iperm[np]] + d;
+  // node graph in the new numbering
+  Lp.nbr_ptr.assign(nn + 1, 0);
+  for (int np = 0; np < nn; np++) {
+    const int n = iperm[np];
+    Lp.nbr_ptr[np + 1] = Lp.nbr_ptr[np] + (L.nbr_ptr[n + 1] - L.nbr_ptr[n]);
+  }
+  const size_t ne = (size_t)Lp.nbr_ptr[nn];
+  Lp.nbr_node.resize(ne);
+  Lp.nbr_off.resize(ne);
+  Lp.nbr_offT.resize(ne);
+  std::vector<int> oldslot(ne);  // new slot -> old slot index (absolute)
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int np = 0; np < nn; np++) {
+    const int n = iperm[np];
+    const int b0 = L.nbr_ptr[n], cnt = L.nbr_ptr[n + 1] - b0, q0 = Lp.nbr_ptr[np];
+    std::vector<std::pair<int, int>> v(cnt);
+    for (int s = 0; s < cnt; s++) v[s] = {perm[L.nbr_node[b0 + s]], b0 + s};
+    std::sort(v.begin(), v.end());
+    int off = 0, offT = 0;
+    for (int s = 0; s < cnt; s++) {
+      const int mp = v[s].first, m = iperm[mp];
+      Lp.nbr_node[q0 + s] = mp;
+      Lp.nbr_off[q0 + s] = off;
+      Lp.nbr_offT[q0 + s] = offT;
+      oldslot[q0 + s] = v[s].second;
+      off += L.fu[m + 1] - L.fu[m];
+      offT += L.nvn;
+    }
+  }
+  // CSR: row lengths are those of the old rows
+  Lp.rowptr.assign((size_t)L.N + 1, 0);
+  for (int i = 0; i < L.N; i++) Lp.rowptr[i + 1] = L.rowptr[umap[i] + 1] - L.rowptr[umap[i]];
+  for (int i = 0; i < L.N; i++) Lp.rowptr[i + 1] += Lp.rowptr[i];
+  Lp.nnz = Lp.rowptr[L.N];
+  Lp.colidx.resize((size_t)Lp.nnz);
+  vmap.resize((size_t)Lp.nnz);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int np = 0; np < nn; np++) {
+    const int n = iperm[np];
+    for (int d = 0; d < Lp.fu[np + 1] - Lp.fu[np]; d++) {
+      const int ip = Lp.fu[np] + d, i = L.fu[n] + d;
+      const bool rowT = L.energy && d == L.dim;
+      int64_t pos = Lp.rowptr[ip];
+      for (int q = Lp.nbr_ptr[np]; q < Lp.nbr_ptr[np + 1]; q++) {
+        const int mp = Lp.nbr_node[q], m = iperm[mp], oq = oldslot[q];
+        const int nd = rowT ? L.nvn : L.fu[m + 1] - L.fu[m];
+        const int64_t ob = L.rowptr[i] + (rowT ? L.nbr_offT[oq] : L.nbr_off[oq]);
+        for (int e = 0; e < nd; e++) {
+          Lp.colidx[(size_t)pos] = Lp.fu[mp] + e;
+          vmap[(size_t)pos] = ob + e;
+          pos++;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace gb

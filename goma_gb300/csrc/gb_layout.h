@@ -33,6 +33,19 @@ struct Layout {
 
 // Returns 0 on success, -1 with a message in err.
 int build_layout(const gb_problem_desc *d, Layout &L, std::string &err);
+// The same matrix with node n renumbered perm[n] (unknowns stay grouped by
+// node, in the same order within a node).  Fills the DOF map, CSR pattern
+// and node graph of Lp (no mesh data: elem_nslot, Dirichlet marks and
+// colours stay empty), umap (new unknown -> old unknown) and vmap (new CSR
+// entry -> old CSR entry).
+void permute_layout(const Layout &L, const std::vector<int> &perm, Layout &Lp,
+                    std::vector<int> &umap, std::vector<int64_t> &vmap);
+// A node order with few ILU(0) dependency levels: the nodes without
+// pressure unknowns by greedy colours of the node graph, then the element
+// centroid nodes (which carry the P1 pressures) by greedy colours of theirs,
+// so that every pressure pivot comes after all velocities of its element.
+// Returns perm (old node -> new node) and the number of colours.
+int multicolour_order(const Layout &L, std::vector<int> &perm);
 // MSR pattern of the reference (diagonal first, off-diagonals ascending).
 void layout_msr_pattern(const Layout &L, int *ija);
 int64_t layout_msr_length(const Layout &L);

@@ -207,6 +207,23 @@ __global__ void to_f32_scaled_kernel(int N, const double *__restrict__ x, double
     y[i] = (float)(x[i] / s);
 }
 
+// y[k] = x[map[k]]
+template <class T, class I>
+__global__ void gather_kernel(int64_t n, const I *__restrict__ map, const T *__restrict__ x,
+                              T *__restrict__ y) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    y[k] = x[map[k]];
+}
+// y[map[k]] = x[k]
+template <class T, class I>
+__global__ void scatter_kernel(int64_t n, const I *__restrict__ map, const T *__restrict__ x,
+                               T *__restrict__ y) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    y[map[k]] = x[k];
+}
+
 __global__ void to_f32_kernel(int64_t n, const double *__restrict__ x, float *__restrict__ y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -694,6 +711,8 @@ Solver::~Solver() {
                d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
+  for (void *q : owned)
+    if (q) cudaFree(q);
   if (h_work) cudaFreeHost(h_work);
 }
 
@@ -715,12 +734,64 @@ int Solver::init(Context *c, int krylov) {
     auto it = std::lower_bound(b, e, i);
     diag[i] = (int64_t)(it - L.colidx.begin());
   }
-  IluSchedule S;
-  build_ilu_schedule(L, S);
-  lo_ptr = S.lo_ptr;
-  up_ptr = S.up_ptr;
   GB_CU(cudaMalloc(&d_diag, sizeof(int64_t) * N), "diag");
   GB_CU(cudaMemcpy(d_diag, diag.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice), "diag");
+  ordering = c->ilu_ordering;
+  Layout Lp;
+  const Layout *LP = &L;  // the layout the factors live in
+  if (ordering == 1) {
+    std::vector<int> perm, um;
+    std::vector<int64_t> vm;
+    multicolour_order(L, perm);
+    permute_layout(L, perm, Lp, um, vm);
+    std::vector<int64_t> pdiag(N);
+    for (int i = 0; i < N; i++) {
+      auto b = Lp.colidx.begin() + Lp.rowptr[i], e = Lp.colidx.begin() + Lp.rowptr[i + 1];
+      pdiag[i] = (int64_t)(std::lower_bound(b, e, i) - Lp.colidx.begin());
+    }
+    auto up = [&](auto &vec, const char *what) -> void * {
+      void *d = nullptr;
+      if (cudaMalloc(&d, sizeof(vec[0]) * vec.size()) != cudaSuccess) return nullptr;
+      owned.push_back(d);
+      if (cudaMemcpy(d, vec.data(), sizeof(vec[0]) * vec.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+        return nullptr;
+      (void)what;
+      return d;
+    };
+    P.fu = (const int *)up(Lp.fu, "fu");
+    P.rowptr = (const int64_t *)up(Lp.rowptr, "rowptr");
+    P.colidx = (const int *)up(Lp.colidx, "colidx");
+    P.diag = (const int64_t *)up(pdiag, "diag");
+    P.nbr_ptr = (const int *)up(Lp.nbr_ptr, "nbr");
+    P.nbr_node = (const int *)up(Lp.nbr_node, "nbr");
+    P.nbr_off = (const int *)up(Lp.nbr_off, "nbr");
+    P.nbr_offT = (const int *)up(Lp.nbr_offT, "nbr");
+    d_umap = (int *)up(um, "umap");
+    d_vmap = (int64_t *)up(vm, "vmap");
+    if (!P.fu || !P.rowptr || !P.colidx || !P.diag || !P.nbr_ptr || !P.nbr_node || !P.nbr_off ||
+        !P.nbr_offT || !d_umap || !d_vmap)
+      return fail("multicoloured ILU(0) layout: device allocation");
+    GB_CU(cudaMalloc(&d_Ap, sizeof(double) * nnz), "permuted matrix");
+    owned.push_back(d_Ap);
+    GB_CU(cudaMalloc(&d_tp, sizeof(double) * N), "permuted vector");
+    owned.push_back(d_tp);
+    LP = &Lp;
+  } else {
+    P.fu = c->d_fu;
+    P.rowptr = c->d_rowptr;
+    P.colidx = c->d_colidx;
+    P.diag = d_diag;
+    P.nbr_ptr = c->d_nbr_ptr;
+    P.nbr_node = c->d_nbr_node;
+    P.nbr_off = c->d_nbr_off;
+    P.nbr_offT = c->d_nbr_offT;
+  }
+  IluSchedule S;
+  build_ilu_schedule(*LP, S);
+  lo_ptr = S.lo_ptr;
+  up_ptr = S.up_ptr;
+  num_levels = (int)lo_ptr.size() - 1;
   GB_CU(cudaMalloc(&d_lo_nodes, sizeof(int) * S.lo_nodes.size()), "sched");
   GB_CU(cudaMemcpy(d_lo_nodes, S.lo_nodes.data(), sizeof(int) * S.lo_nodes.size(),
                    cudaMemcpyHostToDevice), "sched");
@@ -731,11 +802,11 @@ int Solver::init(Context *c, int krylov) {
   if (L.nvn + L.npres > kMaxNodeDofs) return fail("ILU(0) supports at most 16 unknowns per node");
   maxnb = 0;
   lmax = 0;
-  for (int n = 0; n < L.num_nodes; n++) {
-    const int nb = L.nbr_ptr[n + 1] - L.nbr_ptr[n];
+  for (int n = 0; n < LP->num_nodes; n++) {
+    const int nb = LP->nbr_ptr[n + 1] - LP->nbr_ptr[n];
     maxnb = std::max(maxnb, nb);
-    const int q = L.nbr_node[L.nbr_ptr[n + 1] - 1];
-    lmax = std::max(lmax, L.nbr_off[L.nbr_ptr[n + 1] - 1] + L.fu[q + 1] - L.fu[q]);
+    const int q = LP->nbr_node[LP->nbr_ptr[n + 1] - 1];
+    lmax = std::max(lmax, LP->nbr_off[LP->nbr_ptr[n + 1] - 1] + LP->fu[q + 1] - LP->fu[q]);
   }
   {
     const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
@@ -779,19 +850,18 @@ static cudaError_t spmv(const Context *C, int lpr, const T *vals, const T *x, T 
 
 template <class T>
 static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, cudaGraphExec_t *out) {
-  const Context *C = S->C;
   cudaGraph_t g;
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
   for (size_t l = 0; l + 1 < S->lo_ptr.size(); l++) {
     const int cnt = S->lo_ptr[l + 1] - S->lo_ptr[l];
     lsolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        S->d_lo_nodes + S->lo_ptr[l], cnt, C->d_fu, C->d_rowptr, C->d_colidx, S->d_diag, lu, z);
+        S->d_lo_nodes + S->lo_ptr[l], cnt, S->P.fu, S->P.rowptr, S->P.colidx, S->P.diag, lu, z);
   }
   for (size_t l = 0; l + 1 < S->up_ptr.size(); l++) {
     const int cnt = S->up_ptr[l + 1] - S->up_ptr[l];
     usolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        S->d_up_nodes + S->up_ptr[l], cnt, C->d_fu, C->d_rowptr, C->d_colidx, S->d_diag, lu, z);
+        S->d_up_nodes + S->up_ptr[l], cnt, S->P.fu, S->P.rowptr, S->P.colidx, S->P.diag, lu, z);
   }
   e = cudaStreamEndCapture(st, &g);
   if (e != cudaSuccess) return e;
@@ -806,12 +876,12 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   GB_CU(cudaMemsetAsync(nfix, 0, sizeof(int), st), "pivot count");
   const Layout &L = C->L;
   IluArgs g;
-  g.fu = d_fu;
-  g.rowptr = C->d_rowptr;
-  g.nbr_ptr = C->d_nbr_ptr;
-  g.nbr_node = C->d_nbr_node;
-  g.nbr_off = C->d_nbr_off;
-  g.nbr_offT = C->d_nbr_offT;
+  g.fu = P.fu;
+  g.rowptr = P.rowptr;
+  g.nbr_ptr = P.nbr_ptr;
+  g.nbr_node = P.nbr_node;
+  g.nbr_off = P.nbr_off;
+  g.nbr_offT = P.nbr_offT;
   g.dim = L.dim;
   g.nvn = L.nvn;
   g.energy = L.energy;
@@ -826,31 +896,45 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
     GB_CU(cudaMalloc(&d_V32, sizeof(float) * (size_t)(max_krylov + 1) * N), "V32");
     GB_CU(cudaMalloc(&d_t32, sizeof(float) * N), "t32");
     GB_CU(cudaMalloc(&d_w32, sizeof(float) * N), "w32");
+    if (ordering == 1) {
+      GB_CU(cudaMalloc(&d_tp32, sizeof(float) * N), "permuted vector");
+      owned.push_back(d_tp32);
+    }
   }
   const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
+  const double *Af = vals;  // the matrix the factors are built from
+  if (ordering == 1) {
+    gather_kernel<double><<<1216, 256, 0, st>>>(nnz, d_vmap, vals, d_Ap);
+    GB_CU(cudaGetLastError(), "matrix permutation");
+    Af = d_Ap;
+  }
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
     if (fp32) {
       const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
-      ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu32);
+      ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, Af, d_lu32);
     } else {
       const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
-      ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, vals, d_lu);
+      ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, Af, d_lu);
     }
   }
   GB_CU(cudaGetLastError(), "ILU(0) factorisation");
   if (fp32) {
     to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
     GB_CU(cudaGetLastError(), "FP32 matrix copy");
-    if (!prec32) GB_CU(capture_prec<float>(this, d_lu32, d_t32, st, &prec32), "ILU32 graph");
+    if (!prec32)
+      GB_CU(capture_prec<float>(this, d_lu32, ordering ? d_tp32 : d_t32, st, &prec32),
+            "ILU32 graph");
   } else {
-    if (!prec64) GB_CU(capture_prec<double>(this, d_lu, d_t, st, &prec64), "ILU graph");
+    if (!prec64)
+      GB_CU(capture_prec<double>(this, d_lu, ordering ? d_tp : d_t, st, &prec64), "ILU graph");
   }
   return 0;
 }
 
 int Solver::copy_factors(double *host, bool fp32, cudaStream_t st) {
   const int64_t nnz = C->L.nnz;
+  if (ordering != 0) return fail("the factors are in the multicoloured order");
   GB_CU(cudaStreamSynchronize(st), "factor");
   if (fp32) {
     std::vector<float> tmp((size_t)nnz);
@@ -886,12 +970,12 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
     S->trsv_grid = std::max(1, per_sm) * sms;
   }
   TrsvArgs g;
-  g.fu = C->d_fu;
-  g.rowptr = C->d_rowptr;
-  g.colidx = C->d_colidx;
-  g.diag = S->d_diag;
-  g.nbr_ptr = C->d_nbr_ptr;
-  g.nbr_node = C->d_nbr_node;
+  g.fu = S->P.fu;
+  g.rowptr = S->P.rowptr;
+  g.colidx = S->P.colidx;
+  g.diag = S->P.diag;
+  g.nbr_ptr = S->P.nbr_ptr;
+  g.nbr_node = S->P.nbr_node;
   g.num_nodes = C->L.num_nodes;
   g.Tr = C->L.energy ? C->L.dim : -1;
   g.nvn = C->L.nvn;
@@ -922,15 +1006,29 @@ int Solver::check_trsv_error() {
   return 0;
 }
 
-int Solver::apply_prec64(cudaStream_t st) {
-  if (C->trsv == 0) return sync_free_apply<double>(this, d_lu, d_t, st);
-  GB_CU(cudaGraphLaunch(prec64, st), "ILU apply");
+template <class T>
+static int apply_prec(Solver *S, const T *lu, T *t, T *tp, cudaGraphExec_t graph,
+                      cudaStream_t st) {
+  T *z = t;
+  if (S->ordering == 1) {  // t -> P t, solve, P^T
+    gather_kernel<T><<<304, 256, 0, st>>>(S->N, S->d_umap, t, tp);
+    z = tp;
+  }
+  if (S->C->trsv == 0) {
+    if (sync_free_apply<T>(S, lu, z, st)) return -1;
+  } else {
+    GB_CU(cudaGraphLaunch(graph, st), "ILU apply");
+  }
+  if (S->ordering == 1) scatter_kernel<T><<<304, 256, 0, st>>>(S->N, S->d_umap, tp, t);
+  GB_CU(cudaGetLastError(), "ILU apply");
   return 0;
 }
+
+int Solver::apply_prec64(cudaStream_t st) {
+  return apply_prec<double>(this, d_lu, d_t, d_tp, prec64, st);
+}
 int Solver::apply_prec32(cudaStream_t st) {
-  if (C->trsv == 0) return sync_free_apply<float>(this, d_lu32, d_t32, st);
-  GB_CU(cudaGraphLaunch(prec32, st), "ILU32 apply");
-  return 0;
+  return apply_prec<float>(this, d_lu32, d_t32, d_tp32, prec32, st);
 }
 
 // ------------------------------------------------------------ helpers

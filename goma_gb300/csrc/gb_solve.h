@@ -21,8 +21,30 @@ struct IluSchedule {
 };
 void build_ilu_schedule(const Layout &L, IluSchedule &S);
 
+// Device view of the layout the ILU(0) factors live in: the context's own
+// arrays in the reference's node order, permuted copies in the multicoloured
+// order.
+struct PrecLayout {
+  const int *fu = nullptr;
+  const int64_t *rowptr = nullptr;
+  const int *colidx = nullptr;
+  const int64_t *diag = nullptr;
+  const int *nbr_ptr = nullptr, *nbr_node = nullptr, *nbr_off = nullptr, *nbr_offT = nullptr;
+};
+
 struct Solver {
   Context *C = nullptr;
+  // ILU(0) node order: 0 the reference's, 1 multicoloured (few dependency
+  // levels; the preconditioner of P A P^T, applied as P^T (LU)^-1 P)
+  int ordering = 0;
+  int num_levels = 0;
+  PrecLayout P;
+  int *d_umap = nullptr;        // permuted unknown -> unknown
+  int64_t *d_vmap = nullptr;    // permuted CSR entry -> CSR entry
+  double *d_Ap = nullptr;       // permuted scaled matrix
+  double *d_tp = nullptr;       // permuted preconditioner vector
+  float *d_tp32 = nullptr;
+  std::vector<void *> owned;    // permuted layout arrays
   int N = 0;
   int64_t nnz = 0;
   // ILU(0) factors (same pattern as A): FP64 and FP32 copies

@@ -83,6 +83,10 @@ class GomaNewton:
         _lib.check(self._L.gb_dirichlet_init(self.h, _dp(x)))
         return x
 
+    def set_ilu_ordering(self, ordering):
+        """ILU(0) node order of later solves: 0 the reference's, 1 multicoloured."""
+        _lib.check(self._L.gb_set_ilu_ordering(self.h, int(ordering)))
+
     def set_element_density(self, rho):
         """Per-element densities (None: the material's) for later assemblies."""
         if rho is None:
@@ -119,8 +123,8 @@ class GomaNewton:
         del keep
 
     def set_assembly_path(self, path):
-        """0: automatic (scalar FP64), 1: scalar FP64, 2: DMMA element
-        Jacobians in 3-D."""
+        """Element kernel (gb_set_assembly_path): 0 automatic, 1 scalar FP64,
+        2 / 3 FP64 DMMA variants, 4 sum factorisation (3-D Newtonian)."""
         _lib.check(self._L.gb_set_assembly_path(self.h, int(path)))
 
     def set_triangular_solve(self, mode):

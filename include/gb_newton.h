@@ -49,6 +49,14 @@ int gb_msr_pattern(const gb_ctx *ctx, int *ija);
  * (may be NULL) and its length, as alloc_MSR_sparse_arrays does
  * (src/mm_fill_util.c:2865). */
 int gb_msr_pattern_host(const gb_problem_desc *desc, int *ija, long long *msr_length);
+/* Host only: the multicoloured node order of the GB_ILU_MULTICOLOUR
+ * preconditioner (gb_set_ilu_ordering) and the matrix in it.  perm[n]: new
+ * number of node n (num_nodes); num_colours: its ILU dependency levels;
+ * umap[i']: old unknown of new unknown i' (N); rowptr/colidx: the permuted
+ * CSR pattern (N + 1, nnz); vmap[k']: old CSR position of new entry k'
+ * (nnz).  Any output may be NULL. */
+int gb_ilu_permutation_host(const gb_problem_desc *desc, int *perm, int *num_colours, int *umap,
+                            long long *rowptr, int *colidx, long long *vmap);
 /* CSR pattern used on the device: rowptr (N+1, int64), colidx (nnz). */
 int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx);
 /* First unknown of every node (num_nodes + 1 ints), as
@@ -96,6 +104,20 @@ void *gb_stream(gb_ctx *ctx);
  * so its R is bitwise the full assembly's; under path 2 it uses path 1.  All
  * give the same matrix to rounding. */
 int gb_set_assembly_path(gb_ctx *ctx, int path);
+
+/* Node order of the ILU(0) preconditioner of later solves.
+ * GB_ILU_NATURAL: the reference's node-major order (AztecOO's ILU(0) on one
+ * subdomain); its triangular solves have one dependency level per node
+ * "wavefront" (833 levels on the 32^3 HEX27 cube).  GB_ILU_MULTICOLOUR: the
+ * nodes without pressure unknowns in greedy colours of the node graph, then
+ * the element centroids (the pressure nodes) in theirs -- 28 levels on HEX27
+ * meshes, 10 on QUAD9 -- so factorisation and sweeps run level by level with
+ * a whole level in parallel; it preconditions the same system with a
+ * different (not the reference's) incomplete factorisation.  The converged
+ * Newton solution does not depend on the choice. */
+#define GB_ILU_NATURAL 0
+#define GB_ILU_MULTICOLOUR 1
+int gb_set_ilu_ordering(gb_ctx *ctx, int ordering);
 
 /* Per-element density (num_elems values, > 0) for later assemblies, in
  * place of the material's: lets one context hold several independent

@@ -13,11 +13,15 @@ pytestmark = pytest.mark.gpu
 TOL_X = 1e-8
 
 
+@pytest.mark.parametrize("ordering", [0, 1], ids=["ilu_natural", "ilu_multicolour"])
 @pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
 @pytest.mark.parametrize("name", gc.names("solve"))
-def test_gpu_newton_matches_reference_solution(name, fp32_inner):
+def test_gpu_newton_matches_reference_solution(name, fp32_inner, ordering):
+    """Both ILU(0) node orders: the preconditioner changes the Krylov
+    iterates, never the converged Newton solution."""
     g, case = gc.load(name)
     gn = GomaNewton(gc.problem_from_case(case))
+    gn.set_ilu_ordering(ordering)
     x0 = g["x0"] if "x0" in g else None
     x, conv, st = gn.solve_nonlinear_problem(x0, residual_tol=1e-11, linear_tol=1e-10,
                                              fp32_inner=fp32_inner, max_newton=30)
@@ -100,3 +104,22 @@ def test_gpu_ilu0_factors_match_oracle(name):
     for fp32, tol in ((False, 1e-10), (True, 2e-3)):
         lu = gn.ilu0_factors(a_s, fp32=fp32)
         assert gc.msr_row_scaled_error(ija, lu, ref) < tol, fp32
+
+
+@pytest.mark.parametrize("trsv", [0, 1], ids=["sync_free", "level_graph"])
+def test_multicolour_ilu_solves_the_cube(trsv):
+    """The multicoloured ILU(0) preconditioner on a 6^3 Boussinesq cube (both
+    triangular-solve modes): GMRES reaches the same Newton solution as the
+    reference-order ILU(0)."""
+    prob = pb.boussinesq_cube_3d(6, 1e4, 0.71)
+    sols = []
+    for ordering in (0, 1):
+        gn = GomaNewton(prob)
+        gn.set_triangular_solve(trsv)
+        gn.set_ilu_ordering(ordering)
+        x, conv, st = gn.solve_nonlinear_problem(residual_tol=1e-10, linear_tol=1e-9,
+                                                 max_newton=30, max_linear_its=4000)
+        assert conv, (ordering, st)
+        sols.append(x)
+        gn.close()
+    assert np.abs(sols[0] - sols[1]).max() <= TOL_X * np.abs(sols[0]).max()

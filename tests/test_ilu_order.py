@@ -1,0 +1,96 @@
+"""The multicoloured node order of the GPU-friendly ILU(0) variant, checked
+on the host: a permutation of the nodes whose renumbered CSR pattern is the
+original one entry for entry (the value map hits every original entry
+once), with few dependency levels, and every centroid (pressure) node after
+all other nodes."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from goma_gb300 import _lib
+from goma_gb300 import problem as pb
+from goma_gb300.newton import msr_pattern_host
+
+
+def _csr_from_msr(ija, N):
+    rowptr = np.zeros(N + 1, np.int64)
+    colidx = []
+    for i in range(N):
+        c = sorted([i] + list(ija[ija[i]:ija[i + 1]]))
+        colidx.extend(c)
+        rowptr[i + 1] = rowptr[i] + len(c)
+    return rowptr, np.array(colidx, np.int64)
+
+
+@pytest.mark.parametrize("prob_fn", [
+    lambda: pb.lid_cavity_2d(4),
+    lambda: pb.carreau_step_2d(5, 2, 10.0),
+    lambda: pb.boussinesq_cube_3d(3),
+    lambda: pb.reacting_channel_3d(2, 2, 1),
+    lambda: pb.batch_sweep_2d(3, seed=2, nmin=2, nmax=3).problem,
+], ids=["cavity2d", "carreau2d", "bouss3d", "reacting3d", "batch2d"])
+def test_multicolour_order_and_permuted_pattern(prob_fn):
+    prob = prob_fn()
+    L = _lib.load()
+    desc, keep = pb.make_desc(prob)
+    ija = msr_pattern_host(prob)
+    N = int(ija[0]) - 1
+    nnz = len(ija) - 1
+    nn = prob.mesh.num_nodes
+    perm = np.empty(nn, np.int32)
+    ncol = ctypes.c_int()
+    umap = np.empty(N, np.int32)
+    rp = np.empty(N + 1, np.int64)
+    ci = np.empty(nnz, np.int32)
+    vm = np.empty(nnz, np.int64)
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    _lib.check(L.gb_ilu_permutation_host(ctypes.byref(desc), P(perm, ctypes.c_int),
+                                         ctypes.byref(ncol), P(umap, ctypes.c_int),
+                                         P(rp, ctypes.c_longlong), P(ci, ctypes.c_int),
+                                         P(vm, ctypes.c_longlong)))
+    del keep
+    assert np.array_equal(np.sort(perm), np.arange(nn))
+    assert np.array_equal(np.sort(umap), np.arange(N))
+    orp, oci = _csr_from_msr(ija, N)
+    assert rp[-1] == nnz
+    # every permuted entry is the original entry (umap[i'], umap[j'])
+    rows_new = np.repeat(np.arange(N), np.diff(rp))
+    old_i = umap[rows_new]
+    old_j = umap[ci]
+    assert np.all(vm >= orp[old_i]) and np.all(vm < orp[old_i + 1])
+    assert np.array_equal(oci[vm], old_j)
+    assert np.array_equal(np.sort(vm), np.arange(nnz))
+    for i in range(N):  # ascending columns in every permuted row
+        assert np.all(np.diff(ci[rp[i]:rp[i + 1]]) > 0)
+    # node dependency levels of the permuted pattern (the unknowns of a node
+    # stay contiguous and in node order)
+    old_node = _old_node_of_unknowns(N, prob)
+    new_node = perm[old_node[umap]]
+    assert np.all(np.diff(new_node) >= 0)
+    level = np.zeros(nn, np.int64)
+    for i in range(N):
+        n = new_node[i]
+        lower = new_node[ci[rp[i]:rp[i + 1]]]
+        lower = lower[lower < n]
+        if lower.size:
+            level[n] = max(level[n], level[lower].max() + 1)
+    assert level.max() + 1 <= ncol.value
+    assert ncol.value <= (12 if prob.dim == 2 else 32)
+    # centroid (pressure) nodes come after every other node
+    counts = np.bincount(old_node, minlength=nn)
+    cent_new = perm[counts > counts.min()]
+    other_new = perm[counts == counts.min()]
+    assert cent_new.min() > other_new.max()
+
+
+def _old_node_of_unknowns(N, prob):
+    """Node of every original unknown: the nodal fields at every node, the
+    P1 pressures after them at element centroids (node-major order)."""
+    nn = prob.mesh.num_nodes
+    dim = prob.dim
+    nvn = dim + (1 if prob.energy else 0) + prob.num_species
+    cent = set(prob.mesh.conn[:, 8 if dim == 2 else 20].tolist())
+    counts = np.array([nvn + (dim + 1 if n in cent else 0) for n in range(nn)])
+    assert counts.sum() == N
+    return np.repeat(np.arange(nn), counts)
