@@ -138,7 +138,7 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
                       % (done, nel_block, dt)}
 
 
-def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10):
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
@@ -157,11 +157,14 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10):
         gn.set_material(m)
 
     out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
-                       "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol)}
+                       "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
+           "ilu_order": ("the reference's node order" if ilu_ordering == 0 else
+                         "multicoloured node order")}
     sols = {}
     for mode in ("plain_fp64", "learned_fp32"):
         prob = pb.boussinesq_cube_3d(nel, ra0, PR)
         gn = GomaNewton(prob)
+        gn.set_ilu_ordering(ilu_ordering)
         opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
                     fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3)
         torch.cuda.synchronize()
@@ -377,6 +380,9 @@ def main():
                          "operand tables, 4 sum factorisation")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
+    ap.add_argument("--solve-ilu", type=int, default=0,
+                    help="ILU(0) node order of the time-to-solve leg: 0 the reference's, "
+                         "1 multicoloured")
     ap.add_argument("--workloads", default="",
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
@@ -538,7 +544,7 @@ def main():
         gn.close()
         torch.cuda.empty_cache()
         try:
-            line["time_to_solve"] = time_to_solve(args.solve_nel)
+            line["time_to_solve"] = time_to_solve(args.solve_nel, ilu_ordering=args.solve_ilu)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:

@@ -714,6 +714,7 @@ Solver::~Solver() {
   for (void *q : owned)
     if (q) cudaFree(q);
   if (h_work) cudaFreeHost(h_work);
+  if (h_segout) cudaFreeHost(h_segout);
 }
 
 #define GB_CU(call, what)                          \
@@ -828,6 +829,50 @@ int Solver::init(Context *c, int krylov) {
   GB_CU(cudaMalloc(&d_w, sizeof(double) * N), "w");
   GB_CU(cudaMalloc(&d_r, sizeof(double) * N), "r");
   GB_CU(cudaMalloc(&d_xs, sizeof(double) * N), "xs");
+  // independent diagonal blocks: node n closes a block when no node up to n
+  // has a neighbour beyond n (the graph is symmetric)
+  {
+    seg_ptr.assign(1, 0);
+    int reach = 0;
+    for (int n = 0; n < L.num_nodes; n++) {
+      reach = std::max(reach, L.nbr_node[L.nbr_ptr[n + 1] - 1]);
+      if (reach <= n) seg_ptr.push_back(L.fu[n + 1]);
+    }
+    nseg = (int)seg_ptr.size() - 1;
+  }
+  if (nseg > 1) {
+    constexpr int64_t kTile = 2048;
+    std::vector<int> tseg, tptr(1, 0);
+    std::vector<int64_t> tbeg, tend;
+    for (int sg = 0; sg < nseg; sg++) {
+      for (int64_t u = seg_ptr[sg]; u < seg_ptr[sg + 1]; u += kTile) {
+        tseg.push_back(sg);
+        tbeg.push_back(u);
+        tend.push_back(std::min(seg_ptr[sg + 1], u + kTile));
+      }
+      tptr.push_back((int)tseg.size());
+    }
+    ntiles = (int)tseg.size();
+    auto upv = [&](auto &vec, auto **dst) -> int {
+      GB_CU(cudaMalloc((void **)dst, sizeof(vec[0]) * vec.size()), "segments");
+      owned.push_back(*dst);
+      GB_CU(cudaMemcpy(*dst, vec.data(), sizeof(vec[0]) * vec.size(), cudaMemcpyHostToDevice),
+            "segments");
+      return 0;
+    };
+    if (upv(tseg, &d_tile_seg) || upv(tptr, &d_tile_ptr) || upv(tbeg, &d_tile_beg) ||
+        upv(tend, &d_tile_end))
+      return -1;
+    GB_CU(cudaMalloc(&d_segpart, sizeof(double) * 32 * ntiles), "segments");
+    owned.push_back(d_segpart);
+    GB_CU(cudaMalloc(&d_segout, sizeof(double) * 3 * 32 * nseg), "segments");
+    owned.push_back(d_segout);
+    GB_CU(cudaMalloc(&d_segcoef, sizeof(double) * 32 * nseg), "segments");
+    owned.push_back(d_segcoef);
+    GB_CU(cudaMalloc(&d_segactive, sizeof(int) * nseg), "segments");
+    owned.push_back(d_segactive);
+    GB_CU(cudaMallocHost(&h_segout, sizeof(double) * 3 * 32 * nseg), "segments");
+  }
   return 0;
 }
 
@@ -1170,6 +1215,248 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
   return 0;
 }
 
+// ------------------------------------------------------------ batched GMRES
+//
+// Independent problems in one matrix (diagonal blocks over contiguous
+// unknown ranges): one GMRES per block, run together.  Every inner product
+// is segmented -- a tile of <= 2048 unknowns lies in one block; tiles give
+// partial sums, one warp per block adds them -- so each block has its own
+// Arnoldi coefficients, Hessenberg matrix, Givens rotations, restarts and
+// convergence test; SpMV and the (block-diagonal) ILU(0) serve all blocks
+// at once.
+
+// part[t][j] = sum over tile t of V_j . w, j < k (k <= 32)
+template <class T>
+__global__ void seg_dots_kernel(int k, const T *__restrict__ V, int64_t ld,
+                                const T *__restrict__ w, const int64_t *__restrict__ tbeg,
+                                const int64_t *__restrict__ tend, double *__restrict__ part) {
+  __shared__ double red[8];
+  const int t = blockIdx.x, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int64_t b = tbeg[t], e = tend[t];
+  for (int j = 0; j < k; j++) {
+    double sum = 0.0;
+    for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x)
+      sum = fma((double)V[j * ld + i], (double)w[i], sum);
+    sum = warp_sum(sum);
+    if (lane == 0) red[wp] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += red[q];
+      part[(int64_t)t * 32 + j] = tot;
+    }
+    __syncthreads();
+  }
+}
+
+// out[s][j] = sum over the tiles of block s of part[t][j]; one warp per block
+__global__ void seg_reduce_kernel(int nseg, int k, const int *__restrict__ tptr,
+                                  const double *__restrict__ part, double *__restrict__ out) {
+  const int sg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (sg >= nseg) return;
+  for (int j = 0; j < k; j++) {
+    double sum = 0.0;
+    for (int t = tptr[sg] + lane; t < tptr[sg + 1]; t += 32) sum += part[(int64_t)t * 32 + j];
+    sum = warp_sum(sum);
+    if (lane == 0) out[sg * 32 + j] = sum;
+  }
+}
+
+// w -= sum_j c[s][j] V_j on block s (c = the reduced dots), or with
+// ACCUMULATE = false: y = sum_j c[s][j] V_j
+template <class T, bool SUB>
+__global__ void seg_gemv_kernel(int k, const T *__restrict__ V, int64_t ld,
+                                const double *__restrict__ c, const int *__restrict__ tseg,
+                                const int64_t *__restrict__ tbeg, const int64_t *__restrict__ tend,
+                                T *__restrict__ y) {
+  __shared__ double cs[32];
+  const int t = blockIdx.x;
+  const int sg = tseg[t];
+  if (threadIdx.x < 32) cs[threadIdx.x] = threadIdx.x < k ? c[sg * 32 + threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int64_t i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < k; j++) acc = fma(cs[j], (double)V[j * ld + i], acc);
+    y[i] = SUB ? (T)((double)y[i] - acc) : (T)acc;
+  }
+}
+
+// dst = src * alpha[s] on block s; alpha = 1 / sqrt(norm2[s]) for active
+// blocks with a nonzero norm, else 0 (from the reduced norms when scale is NULL)
+template <class T>
+__global__ void seg_scale_kernel(const T *__restrict__ src, const double *__restrict__ norm2,
+                                 const int *__restrict__ active, const int *__restrict__ tseg,
+                                 const int64_t *__restrict__ tbeg, const int64_t *__restrict__ tend,
+                                 T *__restrict__ dst) {
+  const int t = blockIdx.x, sg = tseg[t];
+  const double n2 = norm2[sg * 32];
+  const double a = (active[sg] && n2 > 0.0) ? 1.0 / sqrt(n2) : 0.0;
+  for (int64_t i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x)
+    dst[i] = (T)((double)src[i] * a);
+}
+
+template <class T>
+static int gmres_seg(Context *C, const T *b, T *x, double tol, int maxit, int m, int *its,
+                     double *relres, cudaStream_t st) {
+  Solver &S = *C->solver;
+  const Layout &L = C->L;
+  const int N = L.N, lpr = lanes_per_row(L), ns = S.nseg, nt = S.ntiles;
+  m = std::min(m, 31);
+  const bool f32 = sizeof(T) == 4;
+  T *V = f32 ? (T *)S.d_V32 : (T *)S.d_V;
+  T *t = f32 ? (T *)S.d_t32 : (T *)S.d_t;
+  T *w = f32 ? (T *)S.d_w32 : (T *)S.d_w;
+  const T *A = f32 ? (const T *)S.d_a32 : (const T *)S.d_A;
+  const int64_t ld = N;
+  double *o1 = S.d_segout, *o2 = o1 + 32 * ns, *o3 = o2 + 32 * ns;
+  double *h1 = S.h_segout, *h2 = h1 + 32 * ns, *h3 = h2 + 32 * ns;
+  const int rblocks = (ns + 7) / 8;
+  auto dots = [&](int k, const T *Vb, const T *wv, double *out) {
+    seg_dots_kernel<T><<<nt, 256, 0, st>>>(k, Vb, ld, wv, S.d_tile_beg, S.d_tile_end,
+                                           S.d_segpart);
+    seg_reduce_kernel<<<rblocks, 256, 0, st>>>(ns, k, S.d_tile_ptr, S.d_segpart, out);
+  };
+  std::vector<int> active(ns, 1), done(ns, 0);
+  std::vector<double> bnorm(ns), beta(ns), coef(32 * (size_t)ns);
+  std::vector<double> H((size_t)ns * (m + 1) * m), cs((size_t)ns * m), sn((size_t)ns * m),
+      g((size_t)ns * (m + 1)), y(m);
+  std::vector<int> used(ns);
+  auto upload_active = [&]() -> int {
+    GB_CU(cudaMemcpyAsync(S.d_segactive, active.data(), sizeof(int) * ns, cudaMemcpyHostToDevice,
+                          st), "active");
+    return 0;
+  };
+  GB_CU(cudaMemsetAsync(x, 0, sizeof(T) * N, st), "x0");
+  dots(1, b, b, o3);
+  GB_CU(cudaMemcpyAsync(h3, o3, sizeof(double) * 32 * ns, cudaMemcpyDeviceToHost, st), "norms");
+  GB_CU(cudaStreamSynchronize(st), "norms");
+  bool any = false;
+  for (int sg = 0; sg < ns; sg++) {
+    bnorm[sg] = std::sqrt(h3[sg * 32]);
+    beta[sg] = bnorm[sg];
+    active[sg] = bnorm[sg] > 0.0;
+    any |= active[sg] != 0;
+  }
+  *its = 0;
+  *relres = 0.0;
+  if (!any) return 0;
+  GB_CU(cudaMemcpyAsync(V, b, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "r0");
+  int total = 0;
+  while (true) {
+    if (upload_active()) return -1;
+    // V0 = r / beta per block (o3 holds the squared norms of r)
+    seg_scale_kernel<T><<<nt, 256, 0, st>>>(V, o3, S.d_segactive, S.d_tile_seg, S.d_tile_beg,
+                                            S.d_tile_end, V);
+    for (int sg = 0; sg < ns; sg++) {
+      std::fill(&g[(size_t)sg * (m + 1)], &g[(size_t)sg * (m + 1)] + m + 1, 0.0);
+      g[(size_t)sg * (m + 1)] = beta[sg];
+      done[sg] = active[sg] ? 0 : -1;  // -1: converged before this cycle
+      used[sg] = 0;
+    }
+    int j = 0;
+    for (; j < m && total < maxit; j++) {
+      GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
+      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      GB_CU(spmv<T>(C, lpr, A, t, w, st), "spmv");
+      dots(j + 1, V, w, o1);
+      seg_gemv_kernel<T, true><<<nt, 256, 0, st>>>(j + 1, V, ld, o1, S.d_tile_seg,
+                                                   S.d_tile_beg, S.d_tile_end, w);
+      dots(j + 1, V, w, o2);
+      seg_gemv_kernel<T, true><<<nt, 256, 0, st>>>(j + 1, V, ld, o2, S.d_tile_seg,
+                                                   S.d_tile_beg, S.d_tile_end, w);
+      dots(1, w, w, o3);
+      seg_scale_kernel<T><<<nt, 256, 0, st>>>(w, o3, S.d_segactive, S.d_tile_seg, S.d_tile_beg,
+                                              S.d_tile_end, V + (j + 1) * ld);
+      GB_CU(cudaGetLastError(), "batched Arnoldi step");
+      GB_CU(cudaMemcpyAsync(h1, o1, sizeof(double) * 3 * 32 * ns, cudaMemcpyDeviceToHost, st),
+            "h");
+      GB_CU(cudaStreamSynchronize(st), "h sync");
+      total++;
+      bool changed = false, all_done = true;
+      for (int sg = 0; sg < ns; sg++) {
+        if (done[sg] != 0) continue;
+        double *Hs = &H[(size_t)sg * (m + 1) * m], *gs = &g[(size_t)sg * (m + 1)];
+        double *csg = &cs[(size_t)sg * m], *sng = &sn[(size_t)sg * m];
+        double hcol[33];
+        for (int i = 0; i <= j; i++) hcol[i] = h1[sg * 32 + i] + h2[sg * 32 + i];
+        const double hn = std::sqrt(h3[sg * 32]);
+        hcol[j + 1] = hn;
+        for (int i = 0; i < j; i++) {
+          const double a = csg[i] * hcol[i] + sng[i] * hcol[i + 1];
+          hcol[i + 1] = -sng[i] * hcol[i] + csg[i] * hcol[i + 1];
+          hcol[i] = a;
+        }
+        const double den = std::hypot(hcol[j], hcol[j + 1]);
+        csg[j] = den == 0.0 ? 1.0 : hcol[j] / den;
+        sng[j] = den == 0.0 ? 0.0 : hcol[j + 1] / den;
+        hcol[j] = den;
+        gs[j + 1] = -sng[j] * gs[j];
+        gs[j] = csg[j] * gs[j];
+        for (int i = 0; i <= j; i++) Hs[(size_t)i * m + j] = hcol[i];
+        used[sg] = j + 1;
+        if (std::fabs(gs[j + 1]) <= tol * bnorm[sg] || hn == 0.0) {
+          done[sg] = 1;
+          active[sg] = 0;
+          changed = true;
+        } else {
+          all_done = false;
+        }
+      }
+      if (changed && upload_active()) return -1;
+      if (all_done) {
+        j++;
+        break;
+      }
+    }
+    // x += M^-1 sum_j y_j V_j, block by block
+    std::fill(coef.begin(), coef.end(), 0.0);
+    int kmax = 0;
+    for (int sg = 0; sg < ns; sg++) {
+      const int js = used[sg];
+      if (js == 0) continue;
+      const double *Hs = &H[(size_t)sg * (m + 1) * m], *gs = &g[(size_t)sg * (m + 1)];
+      for (int i = js - 1; i >= 0; i--) {
+        double sum = gs[i];
+        for (int k2 = i + 1; k2 < js; k2++) sum -= Hs[(size_t)i * m + k2] * y[k2];
+        y[i] = Hs[(size_t)i * m + i] != 0.0 ? sum / Hs[(size_t)i * m + i] : 0.0;
+      }
+      for (int i = 0; i < js; i++) coef[(size_t)sg * 32 + i] = y[i];
+      kmax = std::max(kmax, js);
+    }
+    if (kmax > 0) {
+      GB_CU(cudaMemcpyAsync(S.d_segcoef, coef.data(), sizeof(double) * 32 * ns,
+                            cudaMemcpyHostToDevice, st), "y");
+      seg_gemv_kernel<T, false><<<nt, 256, 0, st>>>(kmax, V, ld, S.d_segcoef, S.d_tile_seg,
+                                                    S.d_tile_beg, S.d_tile_end, t);
+      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      add_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, t, x);
+    }
+    // true residual per block
+    GB_CU(spmv<T>(C, lpr, A, x, V, st), "spmv");
+    sub_from_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, b, V);
+    dots(1, V, V, o3);
+    GB_CU(cudaMemcpyAsync(h3, o3, sizeof(double) * 32 * ns, cudaMemcpyDeviceToHost, st), "norms");
+    GB_CU(cudaStreamSynchronize(st), "norms");
+    double worst = 0.0;
+    bool all_conv = true;
+    for (int sg = 0; sg < ns; sg++) {
+      if (bnorm[sg] == 0.0) {
+        active[sg] = 0;
+        continue;
+      }
+      beta[sg] = std::sqrt(h3[sg * 32]);
+      const bool conv = beta[sg] <= tol * bnorm[sg];
+      active[sg] = !conv;
+      all_conv &= conv;
+      worst = std::max(worst, beta[sg] / bnorm[sg]);
+    }
+    *its = total;
+    *relres = worst;
+    if (all_conv || total >= maxit) break;
+  }
+  return 0;
+}
+
 // Solves the scaled system A dx = R (both on the device, A = d_vals_scaled
 // after factorisation).  FP64: GMRES in FP64.  FP32 refined: FP32 GMRES on
 // the normalised residual inside FP64 iterative refinement.
@@ -1194,7 +1481,9 @@ static int linear_solve_impl(Context *C, const double *R, double *dx, const Line
   if (!o.fp32_inner) {
     int its;
     double rr;
-    if (gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st)) return -1;
+    if (S.nseg > 1 ? gmres_seg<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st)
+                   : gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st))
+      return -1;
     s->iterations = its;
     s->relres = rr;
     return 0;
@@ -1216,7 +1505,10 @@ static int linear_solve_impl(Context *C, const double *R, double *dx, const Line
     int its;
     double rr;
     float *sol32 = (float *)S.d_xs + N;
-    if (gmres<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr, st)) return -1;
+    if (S.nseg > 1 ? gmres_seg<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr,
+                                      st)
+                   : gmres<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr, st))
+      return -1;
     s->iterations += its;
     s->refinements++;
     axpy_f32_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, rn, sol32, dx);

@@ -45,6 +45,18 @@ struct Solver {
   double *d_tp = nullptr;       // permuted preconditioner vector
   float *d_tp32 = nullptr;
   std::vector<void *> owned;    // permuted layout arrays
+  // Independent problems held in one matrix (diagonal blocks over contiguous
+  // node ranges, found from the node graph): GMRES runs per block
+  // (segmented reductions, one Hessenberg per block).  nseg == 1: one system.
+  int nseg = 1, ntiles = 0;
+  std::vector<int64_t> seg_ptr;   // unknown range of block s: [seg_ptr[s], seg_ptr[s+1])
+  int *d_tile_seg = nullptr, *d_tile_ptr = nullptr;
+  int64_t *d_tile_beg = nullptr, *d_tile_end = nullptr;
+  double *d_segpart = nullptr;    // [ntiles][32] per-tile partial dot products
+  double *d_segout = nullptr;     // [3][nseg][32] reduced dots (two passes) and norms
+  double *d_segcoef = nullptr;    // [nseg][32] host-set coefficients
+  int *d_segactive = nullptr;     // [nseg] blocks still iterating in this cycle
+  double *h_segout = nullptr;     // pinned mirror of d_segout
   int N = 0;
   int64_t nnz = 0;
   // ILU(0) factors (same pattern as A): FP64 and FP32 copies
