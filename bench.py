@@ -160,6 +160,16 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
            "ilu_order": ("the reference's node order" if ilu_ordering == 0 else
                          "multicoloured node order")}
+    # first-use costs of the process (CUDA module loading of the network and
+    # copy kernels) are paid once here, outside both timed runs
+    from goma_gb300.mlp import GpuMLP
+    warm = GpuMLP(4, 32, 2, 1, seed=1)
+    xw = torch.zeros((64, 4), device="cuda")
+    tw = torch.zeros((64, 1), device="cuda")
+    warm.train(xw, tw, torch.ones_like(tw), steps=2, batch=32)
+    warm.forward(xw).cpu().numpy()
+    torch.cuda.synchronize()
+    del warm, xw, tw
     sols = {}
     for mode in ("plain_fp64", "learned_fp32"):
         prob = pb.boussinesq_cube_3d(nel, ra0, PR)
@@ -268,15 +278,18 @@ def reacting_channel_assembly(nx, ny, nz, steps=3, warmup=2):
     return out
 
 
-def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, check=2):
+def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, check=2,
+                      ilu_ordering=1, budget_s=300.0):
     """The 512-problem sweep: unit-square QUAD9 Q2/P1 cavities and channels,
     meshes n x n with n uniform in [16, 64], Re log-uniform in [10, 1000]
     (seeded), all held in one context as a disjoint union with per-element
     Reynolds numbers, so one assembly launch per colour and one Krylov solve
     serve every problem.  Newton from rest to the scaled residual `tol`,
     through `stages` geometric Reynolds ramps (Re_p 10^(k/stages) ... up to
-    each problem's own Re).  `check` of the smallest members are solved
-    again, on their own, by the CPU oracle, and compared."""
+    each problem's own Re).  The Krylov solve is the batched GMRES (one
+    Arnoldi process per problem).  `check` of the smallest members are solved
+    again, on their own, by the CPU oracle, and compared.  Stages stop once
+    `budget_s` seconds have passed (reported as not converged)."""
     import time as _time
 
     import torch
@@ -285,6 +298,7 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
     t0 = _time.perf_counter()
     b = pb.batch_sweep_2d(num, seed=seed)
     gn = GomaNewton(b.problem)
+    gn.set_ilu_ordering(ilu_ordering)
     setup_s = _time.perf_counter() - t0
     re = b.elem_re
     x = None
@@ -294,8 +308,11 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
     for k in range(stages + 1):
         rho = np.minimum(re, 10.0 * (re / 10.0) ** (k / stages)) if stages else re
         gn.set_element_density(rho)
+        if _time.perf_counter() - t1 > budget_s:
+            recs.append({"stage": k, "converged": False, "skipped": "time budget"})
+            break
         x, conv, st = gn.solve_nonlinear_problem(
-            x, residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=6000,
+            x, residual_tol=tol, linear_tol=1e-8, max_newton=20, max_linear_its=1500,
             fp32_inner=fp32_inner, inner_tol=1e-3)
         recs.append({"stage": k, "converged": conv, "newton_its": st["newton_its"],
                      "linear_its": st["linear_its"],
@@ -313,7 +330,8 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
            "elements": nelem, "unknowns": gn.N, "csr_nnz": gn.nnz,
            "seconds_to_solve_all": solve_s, "layout_and_upload_s": setup_s,
            "converged": all(r["converged"] for r in recs), "stages": recs,
-           "fp32_inner": fp32_inner}
+           "fp32_inner": fp32_inner,
+           "ilu_order": "multicoloured" if ilu_ordering == 1 else "the reference's"}
     if check and out["converged"]:
         import oracle
         ctypes_fu = np.empty(b.problem.mesh.num_nodes + 1, np.int32)

@@ -156,7 +156,7 @@ class LearnedPredictor:
         r1, dr, h = self._history(t, len(self.sols))
         sig = self._sigma(r1)
         X = torch.tensor(self._features(r1, dr, sig), device="cuda")
-        corr = self.net.forward(X).double().cpu().numpy()[:, 0] * sig
+        corr = self.net.forward(X).cpu().numpy()[:, 0].astype(np.float64) * sig
         return self.sols[-1][1] + h * (r1 + corr)
 
 
@@ -177,7 +177,7 @@ def scaled_residual_l2(gn, x):
     gn.status()
     gn.scale_device(dv.data_ptr(), dR.data_ptr())
     torch.cuda.synchronize()
-    return float(torch.linalg.vector_norm(dR).item())
+    return float(np.linalg.norm(dR.cpu().numpy()))
 
 
 def tangent(gn, x, lam, set_param, rel=1e-6, **solve_opts):
