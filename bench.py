@@ -138,14 +138,20 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
                       % (done, nel_block, dt)}
 
 
-def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=1, krylov=60,
+                  forcing=1, reference_solver=True):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
     reference's ALC_ZEROTH) against the learned predictor (zeroth-order
-    fallback) + FP32-inner GMRES with FP64 refinement.  Returns a dict with
-    both times, Newton/Krylov counts and the relative difference of the two
-    converged solutions."""
+    fallback) + FP32-inner GMRES with FP64 refinement.  Both use the same
+    linear-solver settings: ILU(0) in the multicoloured node order,
+    GMRES(krylov), Eisenstat-Walker forcing (the defaults; the converged
+    solution does not depend on them).  With reference_solver the plain
+    FP64 run is repeated with the reference's settings (ILU(0) in its node
+    order, GMRES(30), every linear solve to 1e-8).  Returns a dict with the
+    times, Newton/Krylov counts, per-phase splits and the relative
+    difference of the converged solutions."""
     import torch
     from goma_gb300 import problem as pb
     from goma_gb300.continuation import continuation
@@ -158,8 +164,9 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
 
     out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
-           "ilu_order": ("the reference's node order" if ilu_ordering == 0 else
-                         "multicoloured node order")}
+           "linear_solver": "ILU(0) in the %s node order, GMRES(%d), %s" % (
+               "reference's" if ilu_ordering == 0 else "multicoloured", krylov,
+               "Eisenstat-Walker forcing (1e-8 .. 1e-2)" if forcing else "linear tol 1e-8")}
     # first-use costs of the process (CUDA module loading of the network and
     # copy kernels) are paid once here, outside both timed runs
     from goma_gb300.mlp import GpuMLP
@@ -171,12 +178,17 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
     torch.cuda.synchronize()
     del warm, xw, tw
     sols = {}
-    for mode in ("plain_fp64", "learned_fp32"):
+    modes = ["plain_fp64", "learned_fp32"] + (["plain_fp64_reference_solver"]
+                                              if reference_solver else [])
+    for mode in modes:
         prob = pb.boussinesq_cube_3d(nel, ra0, PR)
         gn = GomaNewton(prob)
-        gn.set_ilu_ordering(ilu_ordering)
+        refs = mode == "plain_fp64_reference_solver"
+        gn.set_ilu_ordering(0 if refs else ilu_ordering)
         opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
-                    fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3)
+                    fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3,
+                    krylov_dim=30 if refs else krylov, forcing=0 if refs else forcing,
+                    forcing_max=1e-2)
         torch.cuda.synchronize()
         t = time.perf_counter()
         recs, x = continuation(gn, ra0, ra1, nsteps,
@@ -198,6 +210,9 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=0):
         del gn
     a, b = sols["plain_fp64"], sols["learned_fp32"]
     out["solution_rel_diff"] = float(np.abs(a - b).max() / np.abs(a).max())
+    if reference_solver:
+        c = sols["plain_fp64_reference_solver"]
+        out["solution_rel_diff_reference_solver"] = float(np.abs(a - c).max() / np.abs(a).max())
     out["speedup"] = out["plain_fp64"]["seconds"] / out["learned_fp32"]["seconds"]
     return out
 
@@ -313,7 +328,7 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
             break
         x, conv, st = gn.solve_nonlinear_problem(
             x, residual_tol=tol, linear_tol=1e-8, max_newton=20, max_linear_its=1500,
-            fp32_inner=fp32_inner, inner_tol=1e-3)
+            fp32_inner=fp32_inner, inner_tol=1e-3, forcing=1, forcing_max=1e-2)
         recs.append({"stage": k, "converged": conv, "newton_its": st["newton_its"],
                      "linear_its": st["linear_its"],
                      "newton_seconds": {kk.replace("_ms", ""): st[kk] * 1e-3
@@ -398,7 +413,7 @@ def main():
                          "operand tables, 4 sum factorisation")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
-    ap.add_argument("--solve-ilu", type=int, default=0,
+    ap.add_argument("--solve-ilu", type=int, default=1,
                     help="ILU(0) node order of the time-to-solve leg: 0 the reference's, "
                          "1 multicoloured")
     ap.add_argument("--workloads", default="",
@@ -562,7 +577,8 @@ def main():
         gn.close()
         torch.cuda.empty_cache()
         try:
-            line["time_to_solve"] = time_to_solve(args.solve_nel, ilu_ordering=args.solve_ilu)
+            line["time_to_solve"] = time_to_solve(args.solve_nel, ilu_ordering=args.solve_ilu,
+                                                  reference_solver=args.solve_nel <= 8)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:

@@ -18,7 +18,8 @@ class NewtonOpts(ctypes.Structure):
                 ("damping", ctypes.c_double), ("krylov_dim", ctypes.c_int),
                 ("max_linear_its", ctypes.c_int), ("linear_tol", ctypes.c_double),
                 ("linear_precision", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("max_refinements", ctypes.c_int), ("verbose", ctypes.c_int)]
+                ("max_refinements", ctypes.c_int), ("verbose", ctypes.c_int),
+                ("forcing", ctypes.c_int), ("forcing_max", ctypes.c_double)]
 
 
 class NewtonStats(ctypes.Structure):

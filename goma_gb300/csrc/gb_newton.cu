@@ -8,6 +8,7 @@
 // step runs on the device; the host reads back three norms per step.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -60,8 +61,11 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
            gb_newton_stats *st) {
-  const LinearOpts lo = linear_opts(o);
+  LinearOpts lo = linear_opts(o);
   if (ensure_solver(C, lo.krylov)) return -1;
+  const double tol_min = lo.tol;
+  const double eta_max = o.forcing_max > 0 ? std::max(o.forcing_max, tol_min) : 1e-2;
+  double eta = eta_max, prev_norm = -1.0;
   Solver &S = *C->solver;
   cudaStream_t s = C->stream;
   const int N = C->L.N;
@@ -111,6 +115,18 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
       *converged = 1;
       S_.newton_its = it;
       break;
+    }
+    if (o.forcing == 1) {
+      // Eisenstat-Walker choice 2 (gamma 0.9, alpha 2) with its safeguard
+      if (prev_norm > 0.0) {
+        const double r = n3[0] / prev_norm;
+        double e = 0.9 * r * r;
+        const double safe = 0.9 * eta * eta;
+        if (safe > 0.1) e = std::max(e, safe);
+        eta = std::min(eta_max, std::max(tol_min, e));
+      }
+      lo.tol = eta;
+      prev_norm = n3[0];
     }
     if (S.factor(C->d_vals, lo.fp32_inner, s)) {
       rc = -1;
@@ -163,6 +179,8 @@ void gb_newton_opts_default(gb_newton_opts *o) {
   o->linear_precision = GB_LINEAR_FP64;
   o->inner_tol = 1e-3;
   o->max_refinements = 20;
+  o->forcing = 0;
+  o->forcing_max = 1e-2;
 }
 
 int gb_solve_nonlinear_problem_device(gb_ctx *ctx, double *d_x, const gb_newton_opts *opts,

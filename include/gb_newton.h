@@ -166,6 +166,13 @@ typedef struct gb_newton_opts {
   double inner_tol;        /* FP32 inner GMRES tolerance (refined mode) */
   int max_refinements;     /* FP64 refinement steps (refined mode) */
   int verbose;             /* 1: one line per Newton step on stdout */
+  /* Inexact Newton: 0 solves every linear system to linear_tol; 1 chooses
+   * each step's tolerance by Eisenstat and Walker's second rule,
+   * eta_k = 0.9 (|R_k| / |R_k-1|)^2 (safeguarded by 0.9 eta_k-1^2 when that
+   * exceeds 0.1), kept within [linear_tol, forcing_max].  The converged
+   * solution is decided by residual_tol either way. */
+  int forcing;
+  double forcing_max;
 } gb_newton_opts;
 
 typedef struct gb_newton_stats {
