@@ -293,8 +293,52 @@ def reacting_channel_assembly(nx, ny, nz, steps=3, warmup=2):
     return out
 
 
-def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, check=2,
-                      ilu_ordering=1, budget_s=300.0):
+def batch_sweep_assembly(num=512, seed=0, steps=3, warmup=2):
+    """Assembly throughput of the 512-problem sweep held as one union: one
+    launch per colour over every problem's elements, per-element Reynolds
+    numbers, device-resident R + analytic J."""
+    import time as _time
+
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    t0 = _time.perf_counter()
+    b = pb.batch_sweep_2d(num, seed=seed)
+    gn = GomaNewton(b.problem)
+    gn.set_element_density(b.elem_re)
+    setup_s = _time.perf_counter() - t0
+    x = gn.dirichlet_init(np.random.default_rng(3).uniform(-1, 1, gn.N))
+    dx = torch.tensor(x, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        gn.matrix_fill_full_device(dx.data_ptr(), gn.d_R, gn.d_vals, sp)
+    torch.cuda.synchronize()
+    gn.status()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        gn.matrix_fill_full_device(dx.data_ptr(), gn.d_R, gn.d_vals, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    gn.status()
+    ms = e0.elapsed_time(e1) / steps
+    ne = b.problem.mesh.num_elems
+    out = {"workload": "%d unit-square QUAD9 Q2/P1 problems (cavity / channel), n x n with n "
+                       "uniform in [16, 64], Re log-uniform in [10, 1000], seed %d, one context"
+                       % (num, seed),
+           "elements": ne, "unknowns": gn.N, "csr_nnz": gn.nnz, "colors": gn.num_colors,
+           "ms_per_assembly": ms, "elements_per_s": ne / (ms * 1e-3),
+           "launches_per_assembly": gn.num_colors, "layout_and_upload_s": setup_s}
+    del dx
+    gn.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, check=2,
+                      ilu_ordering=0, budget_s=240.0, nmin=16, nmax=32, re_max=100.0):
     """The 512-problem sweep: unit-square QUAD9 Q2/P1 cavities and channels,
     meshes n x n with n uniform in [16, 64], Re log-uniform in [10, 1000]
     (seeded), all held in one context as a disjoint union with per-element
@@ -311,7 +355,7 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
     from goma_gb300 import problem as pb
     from goma_gb300.newton import GomaNewton
     t0 = _time.perf_counter()
-    b = pb.batch_sweep_2d(num, seed=seed)
+    b = pb.batch_sweep_2d(num, seed=seed, nmin=nmin, nmax=nmax, re_max=re_max)
     gn = GomaNewton(b.problem)
     gn.set_ilu_ordering(ilu_ordering)
     setup_s = _time.perf_counter() - t0
@@ -326,9 +370,13 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
         if _time.perf_counter() - t1 > budget_s:
             recs.append({"stage": k, "converged": False, "skipped": "time budget"})
             break
+        ts = _time.perf_counter()
         x, conv, st = gn.solve_nonlinear_problem(
-            x, residual_tol=tol, linear_tol=1e-8, max_newton=20, max_linear_its=1500,
+            x, residual_tol=tol, linear_tol=1e-8, max_newton=15, max_linear_its=600,
             fp32_inner=fp32_inner, inner_tol=1e-3, forcing=1, forcing_max=1e-2)
+        print("batch stage %d: converged %s, %d Newton, %d Krylov, %.1f s, |R| %s" % (
+            k, conv, st["newton_its"], st["linear_its"], _time.perf_counter() - ts,
+            st["residual_l2"][-1] if st["residual_l2"] else None), file=sys.stderr, flush=True)
         recs.append({"stage": k, "converged": conv, "newton_its": st["newton_its"],
                      "linear_its": st["linear_its"],
                      "newton_seconds": {kk.replace("_ms", ""): st[kk] * 1e-3
@@ -340,8 +388,8 @@ def batch_sweep_solve(num=512, seed=0, stages=3, tol=1e-10, fp32_inner=False, ch
     solve_s = _time.perf_counter() - t1
     nelem = b.problem.mesh.num_elems
     out = {"workload": "%d unit-square QUAD9 Q2/P1 problems (cavity / channel), n x n with n "
-                       "uniform in [16, 64], Re log-uniform in [10, 1000], seed %d, one context"
-                       % (num, seed),
+                       "uniform in [%d, %d], Re log-uniform in [10, %g], seed %d, one context"
+                       % (num, nmin, nmax, re_max, seed),
            "elements": nelem, "unknowns": gn.N, "csr_nnz": gn.nnz,
            "seconds_to_solve_all": solve_s, "layout_and_upload_s": setup_s,
            "converged": all(r["converged"] for r in recs), "stages": recs,
@@ -419,7 +467,8 @@ def main():
     ap.add_argument("--workloads", default="",
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
-                         "(the 512-problem sweep), batch64 (64 of its problems)")
+                         "(assembly of the 512-problem sweep), batch64_solve (Newton solve of "
+                         "64 such problems, n in [16, 32], Re in [10, 100])")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -589,8 +638,8 @@ def main():
             elif w == "reacting_small":
                 extra[w] = reacting_channel_assembly(16, 16, 8)
             elif w == "batch512":
-                extra[w] = batch_sweep_solve(512)
-            elif w == "batch64":
+                extra[w] = batch_sweep_assembly(512)
+            elif w == "batch64_solve":
                 extra[w] = batch_sweep_solve(64)
         line["workloads"] = extra
     if rank == 0:
