@@ -517,8 +517,10 @@ __global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
 }
 
 // Sync-free triangular solves: one launch per sweep, one CTA per node at a
-// time.  CTAs take nodes in elimination order from an atomic ticket
-// (ascending for L, descending for U), wait until every node they depend on
+// time.  CTAs take nodes from an atomic ticket in the order of their
+// dependency levels (the level schedule of the sweep: all of level 0, then
+// level 1, ...; independent problems in one matrix interleave), wait until
+// every node they depend on
 // (lower / higher neighbours) has published this solve's epoch in its flag,
 // then solve the node in two stages:
 //   A  all warps: for every row of the node, the dot product with the
@@ -527,8 +529,9 @@ __global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
 //      entries into shared memory;
 //   B  one thread: the small in-node triangular solve from shared memory.
 // The node's values are then published (fence + release store of the
-// epoch).  Tickets are handed out in order, so a node a CTA waits on is
-// always held by a CTA that is already running.  Every wait is bounded:
+// epoch).  A node depends only on nodes of lower levels, which hold earlier
+// tickets, and every CTA of the grid is resident, so a node a CTA waits on is
+// always held by a CTA that is running or done.  Every wait is bounded:
 // past kSpinLimit polls the CTA records an error, publishes anyway (so no
 // other CTA can wait forever), every later wait of the sweep stops within
 // 1024 polls, and the host reports the failure after the sweep.  A
@@ -544,6 +547,7 @@ static constexpr long long kSpinLimit = 1LL << 22;
 static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
+  const int *order;    // nodes in the order the sweep hands them out (by level)
   const int *fu;
   const int64_t *rowptr;
   const int *colidx;
@@ -580,7 +584,7 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
   while (true) {
     if (tid == 0) {
       const unsigned t = atomicAdd(g.tickets + (LOWER ? 0 : 1), 1u);
-      s_node = t < (unsigned)g.num_nodes ? (LOWER ? (int)t : g.num_nodes - 1 - (int)t) : -1;
+      s_node = t < (unsigned)g.num_nodes ? g.order[t] : -1;
     }
     __syncthreads();
     const int n = s_node;
@@ -1015,6 +1019,7 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
     S->trsv_grid = std::max(1, per_sm) * sms;
   }
   TrsvArgs g;
+  g.order = nullptr;  // set per sweep below
   g.fu = S->P.fu;
   g.rowptr = S->P.rowptr;
   g.colidx = S->P.colidx;
@@ -1030,6 +1035,7 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
   for (int pass = 0; pass < 2; pass++) {
     const unsigned epoch = ++S->epoch;
     GB_CU(cudaMemsetAsync(g.tickets, 0, 2 * sizeof(unsigned), st), "tickets");
+    g.order = pass == 0 ? S->d_lo_nodes : S->d_up_nodes;
     if (pass == 0)
       trsv_sync_free_kernel<T, true><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, epoch);
     else
