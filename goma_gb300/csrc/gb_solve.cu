@@ -41,6 +41,26 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
+// Arithmetic type of the vector kernels: FP64 data is combined in FP64, FP32
+// data in FP32.  On GB300 FP64 arithmetic runs at 1/64 of the FP32 rate, so
+// an FP32 kernel that widened its operands to FP64 would be bound by the
+// FP64 pipe instead of HBM; the FP32 inner solve gets its accuracy from the
+// FP64 refinement around it.
+template <class T>
+struct AccT {
+  using type = double;
+};
+template <>
+struct AccT<float> {
+  using type = float;
+};
+template <class T>
+using acc_t = typename AccT<T>::type;
+__device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double wsum(double v) { return warp_sum(v); }
+__device__ __forceinline__ float wsum(float v) { return warp_sumf(v); }
+
 // ------------------------------------------------------------ scaling
 
 __global__ void row_sum_scale_kernel(int N, const int64_t *__restrict__ rowptr,
@@ -71,16 +91,17 @@ __global__ void row_sum_scale_kernel(int N, const int64_t *__restrict__ rowptr,
 template <class T>
 __global__ void norms_partial_kernel(int N, const T *__restrict__ x, double *__restrict__ part) {
   __shared__ double sh[3][kRedThreads];
-  double s2 = 0.0, s1 = 0.0, mx = 0.0;
+  using A = acc_t<T>;
+  A s2 = 0, s1 = 0, mx = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    const double v = (double)x[i];
-    s2 = fma(v, v, s2);
+    const A v = (A)x[i];
+    s2 = fmx(v, v, s2);
     s1 += fabs(v);
     mx = fmax(mx, fabs(v));
   }
-  sh[0][threadIdx.x] = s2;
-  sh[1][threadIdx.x] = s1;
-  sh[2][threadIdx.x] = mx;
+  sh[0][threadIdx.x] = (double)s2;
+  sh[1][threadIdx.x] = (double)s1;
+  sh[2][threadIdx.x] = (double)mx;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
@@ -116,11 +137,12 @@ template <class T>
 __global__ void multidot_partial_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
                                         const T *__restrict__ w, double *__restrict__ part) {
   __shared__ double sh[kRedThreads];
+  using A = acc_t<T>;
   for (int j = 0; j < k; j++) {
-    double s = 0.0;
+    A s = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
-      s = fma((double)V[j * ld + i], (double)w[i], s);
-    sh[threadIdx.x] = s;
+      s = fmx((A)V[j * ld + i], (A)w[i], s);
+    sh[threadIdx.x] = (double)s;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
       if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
@@ -144,9 +166,10 @@ __global__ void multidot_final_kernel(int k, int nblocks, const double *__restri
 template <class T>
 __global__ void gemv_sub_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
                                 const double *__restrict__ h, T *__restrict__ w) {
+  using A = acc_t<T>;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    double s = (double)w[i];
-    for (int j = 0; j < k; j++) s = fma(-h[j], (double)V[j * ld + i], s);
+    A s = (A)w[i];
+    for (int j = 0; j < k; j++) s = fmx((A)-h[j], (A)V[j * ld + i], s);
     w[i] = (T)s;
   }
 }
@@ -155,18 +178,20 @@ __global__ void gemv_sub_kernel(int N, int k, const T *__restrict__ V, int64_t l
 template <class T>
 __global__ void gemv_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
                             const double *__restrict__ c, T *__restrict__ y) {
+  using A = acc_t<T>;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < k; j++) s = fma(c[j], (double)V[j * ld + i], s);
+    A s = 0;
+    for (int j = 0; j < k; j++) s = fmx((A)c[j], (A)V[j * ld + i], s);
     y[i] = (T)s;
   }
 }
 
 template <class T>
 __global__ void scale_copy_kernel(int N, const T *x, const double *__restrict__ alpha_inv, T *y) {
-  const double a = alpha_inv[0] != 0.0 ? 1.0 / alpha_inv[0] : 0.0;
+  using A = acc_t<T>;
+  const A a = (A)(alpha_inv[0] != 0.0 ? 1.0 / alpha_inv[0] : 0.0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
-    y[i] = (T)((double)x[i] * a);
+    y[i] = (T)((A)x[i] * a);
 }
 
 __global__ void axpy_kernel(int N, double a, const double *__restrict__ x, double *__restrict__ y) {
@@ -184,14 +209,14 @@ __global__ void axpy_f32_kernel(int N, double a, const float *__restrict__ x,
 template <class T>
 __global__ void add_kernel(int N, const T *__restrict__ t, T *__restrict__ x) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
-    x[i] = (T)((double)x[i] + (double)t[i]);
+    x[i] = x[i] + t[i];
 }
 
 // r = b - r   (r holds A x on entry)
 template <class T>
 __global__ void sub_from_kernel(int N, const T *__restrict__ b, T *__restrict__ r) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
-    r[i] = (T)((double)b[i] - (double)r[i]);
+    r[i] = b[i] - r[i];
 }
 
 // r = b - r   (r holds A x on entry)
@@ -241,8 +266,9 @@ __global__ void spmv_kernel(int N, const int64_t *__restrict__ rowptr,
   const int l = threadIdx.x % LPR;
   if (g >= N) return;
   const int64_t r0 = rowptr[g], r1 = rowptr[g + 1];
-  double s = 0.0;
-  for (int64_t k = r0 + l; k < r1; k += LPR) s = fma((double)vals[k], (double)__ldg(x + colidx[k]), s);
+  using A = acc_t<T>;
+  A s = 0;
+  for (int64_t k = r0 + l; k < r1; k += LPR) s = fmx((A)vals[k], (A)__ldg(x + colidx[k]), s);
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
   if (l == 0) y[g] = (T)s;
@@ -488,10 +514,10 @@ __global__ void lsolve_level_kernel(const int *__restrict__ nodes, int count,
   const int n = nodes[w];
   for (int i = fu[n]; i < fu[n + 1]; i++) {
     const int64_t r0 = rowptr[i], di = diag[i];
-    double s = 0.0;
-    for (int64_t p = r0 + lane; p < di; p += 32) s = fma((double)lu[p], (double)z[colidx[p]], s);
-    s = warp_sum(s);
-    if (lane == 0) z[i] = (T)((double)z[i] - s);
+    acc_t<T> s = 0;
+    for (int64_t p = r0 + lane; p < di; p += 32) s = fmx((acc_t<T>)lu[p], (acc_t<T>)z[colidx[p]], s);
+    s = wsum(s);
+    if (lane == 0) z[i] = (T)(z[i] - s);
     __syncwarp();
   }
 }
@@ -508,10 +534,11 @@ __global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
   const int n = nodes[w];
   for (int i = fu[n + 1] - 1; i >= fu[n]; i--) {
     const int64_t r1 = rowptr[i + 1], di = diag[i];
-    double s = 0.0;
-    for (int64_t p = di + 1 + lane; p < r1; p += 32) s = fma((double)lu[p], (double)z[colidx[p]], s);
-    s = warp_sum(s);
-    if (lane == 0) z[i] = (T)(((double)z[i] - s) / (double)lu[di]);
+    acc_t<T> s = 0;
+    for (int64_t p = di + 1 + lane; p < r1; p += 32)
+      s = fmx((acc_t<T>)lu[p], (acc_t<T>)z[colidx[p]], s);
+    s = wsum(s);
+    if (lane == 0) z[i] = (T)((z[i] - s) / lu[di]);
     __syncwarp();
   }
 }
@@ -575,9 +602,10 @@ template <class T, bool LOWER>
 __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g,
                                                                       const T *__restrict__ lu,
                                                                       T *z, unsigned epoch) {
-  __shared__ double part[kMaxNodeDofs];               // off-node sums per row
-  __shared__ double own[kMaxNodeDofs][kMaxNodeDofs];  // own-node entries of the sweep's factor
-  __shared__ double dg[kMaxNodeDofs];                 // U diagonal
+  using A = acc_t<T>;
+  __shared__ A part[kMaxNodeDofs];               // off-node sums per row
+  __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];  // own-node entries of the sweep's factor
+  __shared__ A dg[kMaxNodeDofs];                 // U diagonal
   __shared__ int s_node;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
@@ -615,32 +643,32 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
       if (LOWER) {
         p0 = g.rowptr[i];
         p1 = di - r;
-        if (lane < r) own[r][lane] = (double)lu[di - r + lane];
+        if (lane < r) own[r][lane] = (A)lu[di - r + lane];
       } else {
         p0 = di + 1 + na;
         p1 = g.rowptr[i + 1];
-        if (lane < na) own[r][lane] = (double)lu[di + 1 + lane];
-        if (lane == 0) dg[r] = (double)lu[di];
+        if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
+        if (lane == 0) dg[r] = (A)lu[di];
       }
-      double s0 = 0.0, s1 = 0.0;
+      A s0 = 0, s1 = 0;
       int64_t p = p0 + lane;
       for (; p + 32 < p1; p += 64) {
-        s0 = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), s0);
-        s1 = fma((double)lu[p + 32], (double)__ldcg(z + g.colidx[p + 32]), s1);
+        s0 = fmx((A)lu[p], (A)__ldcg(z + g.colidx[p]), s0);
+        s1 = fmx((A)lu[p + 32], (A)__ldcg(z + g.colidx[p + 32]), s1);
       }
-      if (p < p1) s0 = fma((double)lu[p], (double)__ldcg(z + g.colidx[p]), s0);
-      const double sum = warp_sum(s0 + s1);
+      if (p < p1) s0 = fmx((A)lu[p], (A)__ldcg(z + g.colidx[p]), s0);
+      const A sum = wsum(s0 + s1);
       if (lane == 0) part[r] = sum;
     }
     __syncthreads();
     // stage B: the in-node solve, one thread
     if (tid == 0) {
-      double zl[kMaxNodeDofs];
+      A zl[kMaxNodeDofs];
       if (LOWER) {
 #pragma unroll 1
         for (int r = 0; r < nr; r++) {
-          double v = (double)__ldcg(z + f0 + r) - part[r];
-          for (int c = 0; c < r; c++) v = fma(-own[r][c], zl[c], v);
+          A v = (A)__ldcg(z + f0 + r) - part[r];
+          for (int c = 0; c < r; c++) v = fmx(-own[r][c], zl[c], v);
           zl[r] = v;
           __stcg(z + f0 + r, (T)v);
         }
@@ -648,8 +676,8 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
 #pragma unroll 1
         for (int r = nr - 1; r >= 0; r--) {
           const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
-          double v = (double)__ldcg(z + f0 + r) - part[r];
-          for (int c = 0; c < na; c++) v = fma(-own[r][c], zl[r + 1 + c], v);
+          A v = (A)__ldcg(z + f0 + r) - part[r];
+          for (int c = 0; c < na; c++) v = fmx(-own[r][c], zl[r + 1 + c], v);
           v /= dg[r];
           zl[r] = v;
           __stcg(z + f0 + r, (T)v);
@@ -1239,11 +1267,12 @@ __global__ void seg_dots_kernel(int k, const T *__restrict__ V, int64_t ld,
   __shared__ double red[8];
   const int t = blockIdx.x, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   const int64_t b = tbeg[t], e = tend[t];
+  using A = acc_t<T>;
   for (int j = 0; j < k; j++) {
-    double sum = 0.0;
+    A acc = 0;
     for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x)
-      sum = fma((double)V[j * ld + i], (double)w[i], sum);
-    sum = warp_sum(sum);
+      acc = fmx((A)V[j * ld + i], (A)w[i], acc);
+    const double sum = warp_sum((double)acc);
     if (lane == 0) red[wp] = sum;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1280,10 +1309,11 @@ __global__ void seg_gemv_kernel(int k, const T *__restrict__ V, int64_t ld,
   const int sg = tseg[t];
   if (threadIdx.x < 32) cs[threadIdx.x] = threadIdx.x < k ? c[sg * 32 + threadIdx.x] : 0.0;
   __syncthreads();
+  using A = acc_t<T>;
   for (int64_t i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x) {
-    double acc = 0.0;
-    for (int j = 0; j < k; j++) acc = fma(cs[j], (double)V[j * ld + i], acc);
-    y[i] = SUB ? (T)((double)y[i] - acc) : (T)acc;
+    A acc = 0;
+    for (int j = 0; j < k; j++) acc = fmx((A)cs[j], (A)V[j * ld + i], acc);
+    y[i] = SUB ? (T)((A)y[i] - acc) : (T)acc;
   }
 }
 
@@ -1296,9 +1326,9 @@ __global__ void seg_scale_kernel(const T *__restrict__ src, const double *__rest
                                  T *__restrict__ dst) {
   const int t = blockIdx.x, sg = tseg[t];
   const double n2 = norm2[sg * 32];
-  const double a = (active[sg] && n2 > 0.0) ? 1.0 / sqrt(n2) : 0.0;
+  const acc_t<T> a = (acc_t<T>)((active[sg] && n2 > 0.0) ? 1.0 / sqrt(n2) : 0.0);
   for (int64_t i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x)
-    dst[i] = (T)((double)src[i] * a);
+    dst[i] = (T)((acc_t<T>)src[i] * a);
 }
 
 template <class T>
