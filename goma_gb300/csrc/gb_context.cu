@@ -485,7 +485,8 @@ int gb_set_assembly_path(gb_ctx *ctx, int path) {
 }
 
 int gb_set_triangular_solve(gb_ctx *ctx, int mode) {
-  if (!ctx || mode < 0 || mode > 1) return fail("mode must be 0 (sync-free) or 1 (level graph)");
+  if (!ctx || mode < 0 || mode > 2)
+    return fail("mode must be 0 (sync-free), 1 (level graph) or 2 (automatic)");
   ctx->c.trsv = mode;
   return 0;
 }

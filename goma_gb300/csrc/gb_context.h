@@ -26,7 +26,9 @@ struct Context {
   // (3-D Newtonian), 4 sum factorisation (3-D Newtonian)
   int path = 0;
   int tc_grid = 0;     // persistent grid of the DMMA kernels
-  int trsv = 0;        // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph
+  // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph,
+  // 2 automatic (the graph for short level schedules)
+  int trsv = 2;
   int ilu_ordering = 0;  // ILU(0) node order: 0 the reference's, 1 multicoloured
   cudaStream_t stream = nullptr;
   double *d_coords = nullptr;

@@ -502,47 +502,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// forward solve with the unit lower factor, in place on z
-template <class T>
-__global__ void lsolve_level_kernel(const int *__restrict__ nodes, int count,
-                                    const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
-                                    const int *__restrict__ colidx,
-                                    const int64_t *__restrict__ diag, const T *__restrict__ lu,
-                                    T *__restrict__ z) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= count) return;
-  const int n = nodes[w];
-  for (int i = fu[n]; i < fu[n + 1]; i++) {
-    const int64_t r0 = rowptr[i], di = diag[i];
-    acc_t<T> s = 0;
-    for (int64_t p = r0 + lane; p < di; p += 32) s = fmx((acc_t<T>)lu[p], (acc_t<T>)z[colidx[p]], s);
-    s = wsum(s);
-    if (lane == 0) z[i] = (T)(z[i] - s);
-    __syncwarp();
-  }
-}
-
-// backward solve with the upper factor, in place on z
-template <class T>
-__global__ void usolve_level_kernel(const int *__restrict__ nodes, int count,
-                                    const int *__restrict__ fu, const int64_t *__restrict__ rowptr,
-                                    const int *__restrict__ colidx,
-                                    const int64_t *__restrict__ diag, const T *__restrict__ lu,
-                                    T *__restrict__ z) {
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= count) return;
-  const int n = nodes[w];
-  for (int i = fu[n + 1] - 1; i >= fu[n]; i--) {
-    const int64_t r1 = rowptr[i + 1], di = diag[i];
-    acc_t<T> s = 0;
-    for (int64_t p = di + 1 + lane; p < r1; p += 32)
-      s = fmx((acc_t<T>)lu[p], (acc_t<T>)z[colidx[p]], s);
-    s = wsum(s);
-    if (lane == 0) z[i] = (T)((z[i] - s) / lu[di]);
-    __syncwarp();
-  }
-}
-
 // Sync-free triangular solves: one launch per sweep, one CTA per node at a
 // time.  CTAs take nodes from an atomic ticket in the order of their
 // dependency levels (the level schedule of the sweep: all of level 0, then
@@ -688,6 +647,93 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
     }
     __syncthreads();
   }
+}
+
+// One dependency level of a triangular sweep, one CTA per node: the nodes of
+// a level do not depend on each other, so the launch boundary is the only
+// synchronisation.  Same two stages as the sync-free sweep (rows over the
+// warps, then the in-node solve); used for short level schedules (the
+// multicoloured order), launched level after level from a captured graph.
+template <class T, bool LOWER>
+__global__ void __launch_bounds__(kTrsvThreads)
+    trsv_level_cta_kernel(const int *__restrict__ nodes, TrsvArgs g, const T *__restrict__ lu,
+                          T *__restrict__ z) {
+  using A = acc_t<T>;
+  __shared__ A part[kMaxNodeDofs];
+  __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];
+  __shared__ A dg[kMaxNodeDofs];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kTrsvThreads / 32;
+  const int n = nodes[blockIdx.x];
+  const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+  for (int r = warp; r < nr; r += NW) {
+    const int i = f0 + r;
+    const int64_t di = g.diag[i];
+    const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
+    int64_t p0, p1;
+    if (LOWER) {
+      p0 = g.rowptr[i];
+      p1 = di - r;
+      if (lane < r) own[r][lane] = (A)lu[di - r + lane];
+    } else {
+      p0 = di + 1 + na;
+      p1 = g.rowptr[i + 1];
+      if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
+      if (lane == 0) dg[r] = (A)lu[di];
+    }
+    A s0 = 0, s1 = 0;
+    int64_t p = p0 + lane;
+    for (; p + 32 < p1; p += 64) {
+      s0 = fmx((A)lu[p], (A)z[g.colidx[p]], s0);
+      s1 = fmx((A)lu[p + 32], (A)z[g.colidx[p + 32]], s1);
+    }
+    if (p < p1) s0 = fmx((A)lu[p], (A)z[g.colidx[p]], s0);
+    const A sum = wsum(s0 + s1);
+    if (lane == 0) part[r] = sum;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    A zl[kMaxNodeDofs];
+    if (LOWER) {
+#pragma unroll 1
+      for (int r = 0; r < nr; r++) {
+        A v = (A)z[f0 + r] - part[r];
+        for (int c = 0; c < r; c++) v = fmx(-own[r][c], zl[c], v);
+        zl[r] = v;
+        z[f0 + r] = (T)v;
+      }
+    } else {
+#pragma unroll 1
+      for (int r = nr - 1; r >= 0; r--) {
+        const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
+        A v = (A)z[f0 + r] - part[r];
+        for (int c = 0; c < na; c++) v = fmx(-own[r][c], zl[r + 1 + c], v);
+        v /= dg[r];
+        zl[r] = v;
+        z[f0 + r] = (T)v;
+      }
+    }
+  }
+}
+
+// the sweeps' view of the preconditioner layout (flags, tickets and the
+// order are set by the sync-free sweep)
+static TrsvArgs trsv_args(const Solver *S) {
+  TrsvArgs g;
+  g.order = nullptr;
+  g.fu = S->P.fu;
+  g.rowptr = S->P.rowptr;
+  g.colidx = S->P.colidx;
+  g.diag = S->P.diag;
+  g.nbr_ptr = S->P.nbr_ptr;
+  g.nbr_node = S->P.nbr_node;
+  g.num_nodes = S->C->L.num_nodes;
+  g.Tr = S->C->L.energy ? S->C->L.dim : -1;
+  g.nvn = S->C->L.nvn;
+  g.flags = nullptr;
+  g.tickets = nullptr;
+  g.error = nullptr;
+  return g;
 }
 
 // ------------------------------------------------------------ schedule
@@ -928,17 +974,18 @@ static cudaError_t spmv(const Context *C, int lpr, const T *vals, const T *x, T 
 template <class T>
 static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, cudaGraphExec_t *out) {
   cudaGraph_t g;
+  const TrsvArgs a = trsv_args(S);
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
   for (size_t l = 0; l + 1 < S->lo_ptr.size(); l++) {
     const int cnt = S->lo_ptr[l + 1] - S->lo_ptr[l];
-    lsolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        S->d_lo_nodes + S->lo_ptr[l], cnt, S->P.fu, S->P.rowptr, S->P.colidx, S->P.diag, lu, z);
+    trsv_level_cta_kernel<T, true><<<cnt, kTrsvThreads, 0, st>>>(S->d_lo_nodes + S->lo_ptr[l], a,
+                                                                 lu, z);
   }
   for (size_t l = 0; l + 1 < S->up_ptr.size(); l++) {
     const int cnt = S->up_ptr[l + 1] - S->up_ptr[l];
-    usolve_level_kernel<T><<<(cnt * 32 + 255) / 256, 256, 0, st>>>(
-        S->d_up_nodes + S->up_ptr[l], cnt, S->P.fu, S->P.rowptr, S->P.colidx, S->P.diag, lu, z);
+    trsv_level_cta_kernel<T, false><<<cnt, kTrsvThreads, 0, st>>>(S->d_up_nodes + S->up_ptr[l],
+                                                                  a, lu, z);
   }
   e = cudaStreamEndCapture(st, &g);
   if (e != cudaSuccess) return e;
@@ -999,11 +1046,11 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   if (fp32) {
     to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
     GB_CU(cudaGetLastError(), "FP32 matrix copy");
-    if (!prec32)
+    if (!prec32 && use_level_graph())
       GB_CU(capture_prec<float>(this, d_lu32, ordering ? d_tp32 : d_t32, st, &prec32),
             "ILU32 graph");
   } else {
-    if (!prec64)
+    if (!prec64 && use_level_graph())
       GB_CU(capture_prec<double>(this, d_lu, ordering ? d_tp : d_t, st, &prec64), "ILU graph");
   }
   return 0;
@@ -1046,17 +1093,7 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     S->trsv_grid = std::max(1, per_sm) * sms;
   }
-  TrsvArgs g;
-  g.order = nullptr;  // set per sweep below
-  g.fu = S->P.fu;
-  g.rowptr = S->P.rowptr;
-  g.colidx = S->P.colidx;
-  g.diag = S->P.diag;
-  g.nbr_ptr = S->P.nbr_ptr;
-  g.nbr_node = S->P.nbr_node;
-  g.num_nodes = C->L.num_nodes;
-  g.Tr = C->L.energy ? C->L.dim : -1;
-  g.nvn = C->L.nvn;
+  TrsvArgs g = trsv_args(S);  // the order is set per sweep below
   g.flags = S->d_flags;
   g.tickets = S->d_flags + C->L.num_nodes;
   g.error = (int *)(S->d_flags + C->L.num_nodes + 4);
@@ -1071,6 +1108,10 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
     GB_CU(cudaGetLastError(), "trsv");
   }
   return 0;
+}
+
+bool Solver::use_level_graph() const {
+  return C->trsv == 1 || (C->trsv == 2 && num_levels <= kMaxGraphLevels);
 }
 
 int Solver::check_trsv_error() {
@@ -1093,7 +1134,7 @@ static int apply_prec(Solver *S, const T *lu, T *t, T *tp, cudaGraphExec_t graph
     gather_kernel<T><<<304, 256, 0, st>>>(S->N, S->d_umap, t, tp);
     z = tp;
   }
-  if (S->C->trsv == 0) {
+  if (!S->use_level_graph()) {
     if (sync_free_apply<T>(S, lu, z, st)) return -1;
   } else {
     GB_CU(cudaGraphLaunch(graph, st), "ILU apply");

@@ -83,6 +83,9 @@ struct Solver {
   unsigned epoch = 0;
   int trsv_grid = 0;
   int check_trsv_error();
+  // level-scheduled sweeps from a captured graph (else the sync-free ones)
+  bool use_level_graph() const;
+  static constexpr int kMaxGraphLevels = 64;  // automatic mode: graph up to this depth
   ~Solver();
   int init(Context *c, int krylov);
   int factor(const double *vals, bool fp32, cudaStream_t st);

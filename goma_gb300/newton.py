@@ -128,7 +128,8 @@ class GomaNewton:
         _lib.check(self._L.gb_set_assembly_path(self.h, int(path)))
 
     def set_triangular_solve(self, mode):
-        """ILU(0) solves: 0 sync-free sweeps, 1 level-scheduled graph."""
+        """ILU(0) solves: 0 sync-free sweeps, 1 level-scheduled graph,
+        2 automatic (the default)."""
         _lib.check(self._L.gb_set_triangular_solve(self.h, int(mode)))
 
     def scale_device(self, d_vals, d_R, d_scale=None):

@@ -127,11 +127,13 @@ int gb_set_ilu_ordering(gb_ctx *ctx, int ordering);
 int gb_set_element_density(gb_ctx *ctx, const double *rho);
 
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
- * (one cooperative launch per factor; each node waits on flags of the
- * nodes it depends on, bounded, then publishes), 1 = level-scheduled
- * sweeps replayed as a CUDA graph.  Both give the same result to
- * rounding.  No counterpart in the reference (AztecOO's ILU solves are
- * sequential). */
+ * (one launch per factor; each node waits on flags of the nodes it depends
+ * on, bounded, then publishes), 1 = level-scheduled sweeps (one launch per
+ * dependency level, a CTA per node) replayed as a CUDA graph, 2 = automatic
+ * (the default: the graph when the schedule has at most 64 levels, as in
+ * the multicoloured order; the sync-free sweeps otherwise).  All give the
+ * same result to rounding.  No counterpart in the reference (AztecOO's ILU
+ * solves are sequential). */
 int gb_set_triangular_solve(gb_ctx *ctx, int mode);
 
 /* Replaces the material of a context (same mesh, DOF map and pattern), as
