@@ -352,20 +352,39 @@ def _member_bcs(kind, mesh, set_base, node_base):
     return sets, bcs
 
 
+def batch_shard(num, seed, rank, world, nmin=16, nmax=64):
+    """Members of a `num`-problem sweep that rank `rank` of `world` solves:
+    the problems are independent, so they are dealt out with no exchange.
+    Members go largest first to the rank with the least work so far (the
+    work of a member ~ its element count n^2), so the ranks' loads differ by
+    at most one member; the same seed gives every rank the same partition."""
+    ns = np.random.default_rng(seed).integers(nmin, nmax + 1, num)
+    load = [0] * world
+    owner = np.empty(num, np.int64)
+    for p in sorted(range(num), key=lambda q: (-int(ns[q]), q)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[p] = r
+        load[r] += int(ns[p]) ** 2
+    return [p for p in range(num) if owner[p] == rank]
+
+
 def batch_sweep_2d(num=512, seed=0, nmin=16, nmax=64, re_min=10.0, re_max=1000.0,
-                   kinds=("cavity", "channel")):
+                   kinds=("cavity", "channel"), members=None):
     """`num` independent unit-square QUAD9 Q2/P1 problems drawn from `seed`:
     mesh n x n with n uniform in [nmin, nmax], Re log-uniform in
     [re_min, re_max], lid-driven cavity or channel alternately.  Returned as
     one disjoint union (nodes, elements and unknowns of member p follow those
     of member p - 1) with the per-element Reynolds numbers, so that one
-    context assembles and solves all of them together."""
+    context assembles and solves all of them together.  `members` (a list of
+    member indices, e.g. from batch_shard) keeps only those problems, with
+    the same draws as the full sweep."""
     rng = np.random.default_rng(seed)
     ns = rng.integers(nmin, nmax + 1, num)
     res = np.exp(rng.uniform(np.log(re_min), np.log(re_max), num))
+    chosen = range(num) if members is None else members
     coords, conns, sets, bcs, rho, members = [], [], [], [], [], []
     node_base = elem_base = 0
-    for p in range(num):
+    for p in chosen:
         kind = kinds[p % len(kinds)]
         m = box_mesh(2, int(ns[p]), int(ns[p]))
         msets, mbcs = _member_bcs(kind, m, len(sets), node_base)
