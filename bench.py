@@ -424,6 +424,51 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
     return out
 
 
+def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
+                     predictors=("zeroth", "secant", "learned")):
+    """The learned-predictor configuration: backward-facing step, nx x ny
+    QUAD9 Q2/P1, Carreau-Yasuda fluid (mu0 = 1, mu_inf = 0.01, lambda = 1,
+    a = 2, n = 0.5), Re re0 -> re1 in nsteps uniform continuation steps, the
+    Newton solve to scaled |R| < 1e-10 at every step.  Each predictor runs
+    the same sweep (stopped after budget_s seconds); reported: steps done,
+    Newton and Krylov iterations, wall time, and for the learned run the
+    ratio of its guess residual to the secant guess's."""
+    import time as _time
+
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.continuation import continuation
+    from goma_gb300.newton import GomaNewton
+    out = {"workload": "backward-facing step %dx%d QUAD9 Q2/P1, Carreau-Yasuda, Re %g -> %g in "
+                       "%d steps, scaled |R| < 1e-10" % (nx, ny, re0, re1, nsteps)}
+    for pred in predictors:
+        gn = GomaNewton(pb.carreau_step_2d(nx, ny, re0))
+        opts = dict(residual_tol=1e-10, linear_tol=1e-8, max_newton=25, max_linear_its=3000,
+                    forcing=1, forcing_max=1e-2)
+        t0 = _time.perf_counter()
+        recs, _ = continuation(gn, re0, re1, nsteps, predictor=pred, newton_opts=opts,
+                               learned_opts=dict(steps=300, batch=4096, lr=2e-3),
+                               time_budget_s=budget_s)
+        torch.cuda.synchronize()
+        dt = _time.perf_counter() - t0
+        res = {"steps_done": len(recs) - 1, "last_re": recs[-1]["lam"], "seconds": dt,
+               "newton_its": sum(r["newton_its"] for r in recs[1:]),
+               "linear_its": sum(r.get("linear_its", 0) for r in recs[1:]),
+               "guesses": {g: sum(1 for r in recs[1:] if r["guess"] == g)
+                           for g in ("zeroth", "secant", "learned")}}
+        if pred == "learned":
+            ratios = [r["candidates"]["learned"] / r["candidates"]["secant"] for r in recs[1:]
+                      if "learned" in r.get("candidates", {}) and "secant" in r["candidates"]]
+            if ratios:
+                res["learned_over_secant_residual"] = {
+                    "median": float(np.median(ratios)), "min": float(np.min(ratios)),
+                    "max": float(np.max(ratios)), "steps": len(ratios)}
+        out[pred] = res
+        gn.close()
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path.  The reference C compiles
     only where its source tree is (oracle/_ref, not on the GPU machine), so
@@ -644,6 +689,8 @@ def main():
                 extra[w] = batch_sweep_assembly(512)
             elif w == "batch64_solve":
                 extra[w] = batch_sweep_solve(64)
+            elif w == "bfs":
+                extra[w] = bfs_continuation()
         line["workloads"] = extra
     if rank == 0:
         print(json.dumps(line))

@@ -212,7 +212,7 @@ PREDICTORS = ("zeroth", "first", "secant", "learned", "learned+first")
 
 def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=_set_density,
                  newton_opts=None, learned_opts=None, spacing="linear", max_halvings=4,
-                 verbose=False):
+                 verbose=False, time_budget_s=None):
     """Sweep lambda from lam0 to lam1 in nsteps steps (uniform in lambda, or
     in log lambda with spacing="log").  predictor: "zeroth" (ALC_ZEROTH),
     "first" (ALC_FIRST), "secant", "learned" (secant + the network's
@@ -221,8 +221,10 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
     guesses the one with the smallest FP64 scaled residual is used.  A step
     whose Newton solve fails is halved and re-predicted from the last
     converged point, at most max_halvings times (src/ac_conti.c:986-1045).
-    Returns a list of per-step records (lambda, guess used, candidate
-    residuals, Newton iterations, wall time) and the final solution."""
+    With time_budget_s the sweep stops after the first step that ends past
+    that many seconds.  Returns a list of per-step records (lambda, guess
+    used, candidate residuals, Newton iterations, wall time) and the last
+    solution."""
     if predictor not in PREDICTORS:
         raise ValueError("predictor must be one of %s" % (PREDICTORS,))
     newton_opts = dict(newton_opts or {})
@@ -253,7 +255,10 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
     x_old, lam_old = x, lams[0]
     targets = lams[1:]
     k = 0
+    t_sweep = time.perf_counter()
     while k < len(targets):
+        if time_budget_s is not None and time.perf_counter() - t_sweep > time_budget_s:
+            break
         lam = targets[k]
         t0 = time.perf_counter()
         halvings = 0
