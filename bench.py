@@ -138,20 +138,27 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
                       % (done, nel_block, dt)}
 
 
-def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=1, krylov=60,
-                  forcing=1, reference_solver=True):
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=60,
+                  forcing=1, reference_solver=True, modes=None, budget_s=None):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
     reference's ALC_ZEROTH) against the learned predictor (secant fallback)
-    with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement.  Both use the same
-    linear-solver settings: ILU(0) in the multicoloured node order,
-    GMRES(krylov), Eisenstat-Walker forcing (the defaults; the converged
-    solution does not depend on them).  With reference_solver the plain
-    FP64 run is repeated with the reference's settings (ILU(0) in its node
-    order, GMRES(30), every linear solve to 1e-8).  Returns a dict with the
-    times, Newton/Krylov counts, per-phase splits and the relative
-    difference of the converged solutions."""
+    with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement.  All use the same
+    linear-solver settings: ILU(0), GMRES(krylov), Eisenstat-Walker forcing
+    (the converged solution does not depend on them).  ilu_ordering -1
+    chooses the node order by size: the multicoloured one up to 16^3 (few
+    dependency levels, cheap iterations), the reference's above (its
+    iteration count grows far more slowly: 2,441 against 24,600 Krylov
+    iterations for one 24^3 solve).  With reference_solver the plain FP64
+    run is repeated with the reference's settings (ILU(0) in its node
+    order, GMRES(30), every linear solve to 1e-8).  `modes` selects runs;
+    `budget_s` ends each run's sweep after that many seconds (reported as
+    steps done).  Returns a dict with the times, Newton/Krylov counts,
+    per-phase splits and the relative difference of the converged
+    solutions."""
+    if ilu_ordering < 0:
+        ilu_ordering = 1 if nel <= 16 else 0
     import torch
     from goma_gb300 import problem as pb
     from goma_gb300.continuation import continuation
@@ -178,7 +185,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=1, kr
     torch.cuda.synchronize()
     del warm, xw, tw
     sols = {}
-    modes = ["plain_fp64", "learned_fp64", "learned_fp32"] + (
+    modes = list(modes) if modes else ["plain_fp64", "learned_fp64", "learned_fp32"] + (
         ["plain_fp64_reference_solver"] if reference_solver else [])
     for mode in modes:
         prob = pb.boussinesq_cube_3d(nel, ra0, PR)
@@ -194,12 +201,14 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=1, kr
         recs, x = continuation(gn, ra0, ra1, nsteps,
                                predictor="learned" if mode.startswith("learned") else "zeroth",
                                set_param=set_ra, newton_opts=opts, spacing="log",
-                               learned_opts=dict(steps=300, batch=4096, lr=2e-3))
+                               learned_opts=dict(steps=300, batch=4096, lr=2e-3),
+                               time_budget_s=budget_s)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t
         sols[mode] = x
         ms = {k: sum(r["newton_ms"][k] for r in recs) for k in recs[0]["newton_ms"]}
-        out[mode] = {"seconds": dt, "newton_its": sum(r["newton_its"] for r in recs),
+        out[mode] = {"seconds": dt, "steps_done": len(recs) - 1, "last_ra": recs[-1]["lam"],
+                     "newton_its": sum(r["newton_its"] for r in recs),
                      "linear_its": sum(r.get("linear_its", 0) for r in recs),
                      "guesses": [r["guess"] for r in recs[1:]],
                      "newton_seconds": {k.replace("_ms", ""): v * 1e-3 for k, v in ms.items()},
@@ -208,15 +217,15 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=1, kr
                      "candidate_residual_seconds": sum(r.get("residuals_s", 0.0) for r in recs),
                      "training_seconds": sum(r.get("train_s", 0.0) for r in recs)}
         del gn
-    a, b = sols["plain_fp64"], sols["learned_fp32"]
-    out["solution_rel_diff"] = float(np.abs(a - b).max() / np.abs(a).max())
-    out["solution_rel_diff_learned_fp64"] = float(np.abs(a - sols["learned_fp64"]).max() /
-                                                  np.abs(a).max())
-    if reference_solver:
-        c = sols["plain_fp64_reference_solver"]
-        out["solution_rel_diff_reference_solver"] = float(np.abs(a - c).max() / np.abs(a).max())
-    out["speedup"] = out["plain_fp64"]["seconds"] / out["learned_fp32"]["seconds"]
-    out["speedup_learned_fp64"] = out["plain_fp64"]["seconds"] / out["learned_fp64"]["seconds"]
+    a = sols.get("plain_fp64")
+    complete = {m for m in sols if out[m]["steps_done"] == nsteps}
+    for m in sols:
+        if m != "plain_fp64" and a is not None and {m, "plain_fp64"} <= complete:
+            out["solution_rel_diff_" + m] = float(np.abs(a - sols[m]).max() / np.abs(a).max())
+            out["speedup_" + m] = out["plain_fp64"]["seconds"] / out[m]["seconds"]
+    if "speedup_learned_fp32" in out:
+        out["speedup"] = out["speedup_learned_fp32"]
+        out["solution_rel_diff"] = out["solution_rel_diff_learned_fp32"]
     return out
 
 
@@ -509,9 +518,15 @@ def main():
                          "operand tables, 4 sum factorisation")
     ap.add_argument("--solve-nel", type=int, default=8,
                     help="cube size of the time-to-solve leg (0 skips it)")
-    ap.add_argument("--solve-ilu", type=int, default=1,
+    ap.add_argument("--solve-ilu", type=int, default=-1,
                     help="ILU(0) node order of the time-to-solve leg: 0 the reference's, "
-                         "1 multicoloured")
+                         "1 multicoloured, -1 by size (multicoloured up to 16^3)")
+    ap.add_argument("--solve-modes", default="",
+                    help="comma-separated runs of the time-to-solve leg: plain_fp64, "
+                         "learned_fp64, learned_fp32, plain_fp64_reference_solver "
+                         "(default: all)")
+    ap.add_argument("--solve-budget", type=float, default=0.0,
+                    help="seconds per run of the time-to-solve leg (0: no limit)")
     ap.add_argument("--workloads", default="",
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
@@ -674,8 +689,10 @@ def main():
         gn.close()
         torch.cuda.empty_cache()
         try:
-            line["time_to_solve"] = time_to_solve(args.solve_nel, ilu_ordering=args.solve_ilu,
-                                                  reference_solver=args.solve_nel <= 8)
+            line["time_to_solve"] = time_to_solve(
+                args.solve_nel, ilu_ordering=args.solve_ilu, reference_solver=args.solve_nel <= 8,
+                modes=[m for m in args.solve_modes.split(",") if m] or None,
+                budget_s=args.solve_budget or None)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:

@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(256)
 //      rows spread over the warps), and the node's own diagonal-block
 //      entries into shared memory;
 //   B  one thread: the small in-node triangular solve from shared memory.
-// The node's values are then published (fence + release store of the
+// The node's values are then published (a release store of the
 // epoch).  A node depends only on nodes of lower levels, which hold earlier
 // tickets, and every CTA of the grid is resident, so a node a CTA waits on is
 // always held by a CTA that is running or done.  Every wait is bounded:
@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(256)
 // before it, and those above are the next nr-1-r entries (nvn-1-r for the
 // energy row).
 static constexpr long long kSpinLimit = 1LL << 22;
+static constexpr int kPrefetch = 16;  // row entries per lane loaded before the wait
 static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
@@ -576,6 +577,26 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
     __syncthreads();
     const int n = s_node;
     if (n < 0) return;
+    const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+    // before waiting: this warp's first row -- its factor entries and their
+    // column indices do not depend on the sweep, so their loads overlap the
+    // wait and only the gather of z stays on the critical path
+    A pv[kPrefetch];
+    int pc[kPrefetch];
+    int64_t pr0 = 0, pr1 = 0;
+    if (warp < nr) {
+      const int r = warp, i = f0 + r;
+      const int64_t di = g.diag[i];
+      const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
+      pr0 = LOWER ? g.rowptr[i] : di + 1 + na;
+      pr1 = LOWER ? di - r : g.rowptr[i + 1];
+#pragma unroll
+      for (int k = 0; k < kPrefetch; k++) {
+        const int64_t p = pr0 + lane + 32 * k;
+        pv[k] = p < pr1 ? (A)lu[p] : (A)0;
+        pc[k] = p < pr1 ? g.colidx[p] : -1;
+      }
+    }
     // wait for the dependencies
     bool gave_up = false;
     for (int q = g.nbr_ptr[n] + tid; q < g.nbr_ptr[n + 1]; q += kTrsvThreads) {
@@ -593,7 +614,6 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
     }
     if (__syncthreads_or(gave_up) && tid == 0) atomicExch(g.error, 1);
     // stage A
-    const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
     for (int r = warp; r < nr; r += NW) {
       const int i = f0 + r;
       const int64_t di = g.diag[i];
@@ -611,6 +631,12 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
       }
       A s0 = 0, s1 = 0;
       int64_t p = p0 + lane;
+      if (r == warp) {  // the prefetched row
+#pragma unroll
+        for (int k = 0; k < kPrefetch; k++)
+          if (pc[k] >= 0) s0 = fmx(pv[k], (A)__ldcg(z + pc[k]), s0);
+        p += 32 * kPrefetch;
+      }
       for (; p + 32 < p1; p += 64) {
         s0 = fmx((A)lu[p], (A)__ldcg(z + g.colidx[p]), s0);
         s1 = fmx((A)lu[p + 32], (A)__ldcg(z + g.colidx[p + 32]), s1);
@@ -642,7 +668,7 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
           __stcg(z + f0 + r, (T)v);
         }
       }
-      __threadfence();
+      // the release store orders this thread's z stores before the flag
       st_release(g.flags + n, epoch);
     }
     __syncthreads();
