@@ -147,10 +147,10 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
     with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement.  All use the same
     linear-solver settings: ILU(0), GMRES(krylov), Eisenstat-Walker forcing
     (the converged solution does not depend on them).  ilu_ordering -1
-    chooses the node order by size: the multicoloured one up to 16^3 (few
+    chooses the node order by size: the multicoloured one up to 12^3 (few
     dependency levels, cheap iterations), the reference's above (its
-    iteration count grows far more slowly: 2,441 against 24,600 Krylov
-    iterations for one 24^3 solve).  With reference_solver the plain FP64
+    iteration count grows far more slowly: 801 against 4,198 Krylov
+    iterations for one 16^3 solve, 2,441 against 24,600 at 24^3).  With reference_solver the plain FP64
     run is repeated with the reference's settings (ILU(0) in its node
     order, GMRES(30), every linear solve to 1e-8).  `modes` selects runs;
     `budget_s` ends each run's sweep after that many seconds (reported as
@@ -158,7 +158,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
     per-phase splits and the relative difference of the converged
     solutions."""
     if ilu_ordering < 0:
-        ilu_ordering = 1 if nel <= 16 else 0
+        ilu_ordering = 1 if nel <= 12 else 0
     import torch
     from goma_gb300 import problem as pb
     from goma_gb300.continuation import continuation
@@ -433,6 +433,45 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
     return out
 
 
+def ilu_orders(sizes=(8, 16, 24), ra=1e4, tol=1e-10):
+    """One Newton solve of the Boussinesq cube from rest (Ra `ra`, scaled
+    |R| < tol, GMRES(60), forcing rule) per cube size, ILU(0) node order
+    (the reference's, multicoloured) and inner precision (FP64, FP32 up to
+    16^3): wall time, Newton and Krylov counts and the Krylov phase's time per
+    iteration (CUDA-event phase timers of the Newton driver)."""
+    import time as _time
+
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    rows = []
+    for nel in sizes:
+        prob = pb.boussinesq_cube_3d(nel, ra, PR)
+        for ordering in (0, 1):
+            for fp32 in ((False, True) if nel <= 16 else (False,)):
+                gn = GomaNewton(prob)
+                gn.set_ilu_ordering(ordering)
+                torch.cuda.synchronize()
+                t = _time.perf_counter()
+                x, conv, st = gn.solve_nonlinear_problem(
+                    residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
+                    krylov_dim=60, forcing=1, forcing_max=1e-2, fp32_inner=fp32)
+                torch.cuda.synchronize()
+                dt = _time.perf_counter() - t
+                rows.append({"cube": nel, "ilu_order": "multicoloured" if ordering else
+                             "the reference's", "fp32_inner": fp32, "converged": conv,
+                             "seconds": dt, "newton_its": st["newton_its"],
+                             "linear_its": st["linear_its"],
+                             "ms_per_krylov_it": st["solve_ms"] / max(1, st["linear_its"]),
+                             "factor_seconds": st["factor_ms"] * 1e-3})
+                print("ilu_orders:", rows[-1], file=sys.stderr, flush=True)
+                gn.close()
+                del gn
+                torch.cuda.empty_cache()
+    return {"workload": "Boussinesq cube Newton solve from rest, Ra %g, scaled |R| < %g, "
+                        "GMRES(60), Eisenstat-Walker forcing" % (ra, tol), "runs": rows}
+
+
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
                      predictors=("zeroth", "secant", "learned")):
     """The learned-predictor configuration: backward-facing step, nx x ny
@@ -520,7 +559,7 @@ def main():
                     help="cube size of the time-to-solve leg (0 skips it)")
     ap.add_argument("--solve-ilu", type=int, default=-1,
                     help="ILU(0) node order of the time-to-solve leg: 0 the reference's, "
-                         "1 multicoloured, -1 by size (multicoloured up to 16^3)")
+                         "1 multicoloured, -1 by size (multicoloured up to 12^3)")
     ap.add_argument("--solve-modes", default="",
                     help="comma-separated runs of the time-to-solve leg: plain_fp64, "
                          "learned_fp64, learned_fp32, plain_fp64_reference_solver "
@@ -531,7 +570,9 @@ def main():
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
                          "(assembly of the 512-problem sweep), batch64_solve (Newton solve of "
-                         "64 such problems, n in [16, 32], Re in [10, 100])")
+                         "64 such problems, n in [16, 32], Re in [10, 100]), bfs (the 96x32 "
+                         "Carreau step continuation), ilu_orders (cube solves in both ILU(0) "
+                         "node orders, 8^3 to 24^3)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -708,6 +749,8 @@ def main():
                 extra[w] = batch_sweep_solve(64)
             elif w == "bfs":
                 extra[w] = bfs_continuation()
+            elif w == "ilu_orders":
+                extra[w] = ilu_orders()
         line["workloads"] = extra
     if rank == 0:
         print(json.dumps(line))

@@ -505,23 +505,31 @@ __global__ void __launch_bounds__(256)
 // Sync-free triangular solves: one launch per sweep, one CTA per node at a
 // time.  CTAs take nodes from an atomic ticket in the order of their
 // dependency levels (the level schedule of the sweep: all of level 0, then
-// level 1, ...; independent problems in one matrix interleave), wait until
-// every node they depend on
-// (lower / higher neighbours) has published this solve's epoch in its flag,
-// then solve the node in two stages:
+// level 1, ...; independent problems in one matrix interleave).  A sweep
+// reads its right-hand side from one vector and writes its solution into
+// another that was filled beforehand with an "unpublished" sentinel (a
+// signalling NaN: arithmetic never produces one, so every computed value,
+// NaNs included, differs from it).  A node needs exactly the solution
+// values its rows reference, so it polls those values themselves until none
+// is the sentinel -- no per-node flag, no fence: each value is published by
+// one single-copy-atomic store.  The node is solved in two stages:
 //   A  all warps: for every row of the node, the dot product with the
-//      unknowns of OTHER nodes (the long part of the row: independent loads,
-//      rows spread over the warps), and the node's own diagonal-block
-//      entries into shared memory;
-//   B  one thread: the small in-node triangular solve from shared memory.
-// The node's values are then published (a release store of the
-// epoch).  A node depends only on nodes of lower levels, which hold earlier
-// tickets, and every CTA of the grid is resident, so a node a CTA waits on is
-// always held by a CTA that is running or done.  Every wait is bounded:
-// past kSpinLimit polls the CTA records an error, publishes anyway (so no
-// other CTA can wait forever), every later wait of the sweep stops within
-// 1024 polls, and the host reports the failure after the sweep.  A
-// legitimate wait lasts microseconds; the limit is ~0.3 s.
+//      solution values of OTHER nodes (the long part of the row, rows spread
+//      over the warps; each lane keeps its polled values in registers and
+//      adds them in a fixed order, so the result does not depend on arrival
+//      order);
+//   B  warp 0, lane r for row r: the small in-node triangular solve, one
+//      shuffle per column, from the diagonal block held in shared memory.
+// A warp loads its first row's factor values, column indices, in-node
+// entries and the node's right-hand side before it polls, so only the
+// gather of the solution values stays on the critical path.  A node depends
+// only on nodes of lower levels, which hold earlier tickets, and every CTA of
+// the grid is resident, so a value a CTA waits for is always owed by a CTA
+// that is running or done.  Every wait is bounded: past kSpinLimit polls the
+// CTA records an error, computes and publishes anyway (so no other CTA can
+// wait forever), every later wait of the sweep stops within 1024 polls, and
+// the host reports the failure after the sweep.  A legitimate wait lasts
+// microseconds; the limit is ~0.3 s.
 //
 // Row structure used by the split: a node's unknowns are contiguous and
 // every row of the node holds every own-node column except the energy row,
@@ -530,7 +538,7 @@ __global__ void __launch_bounds__(256)
 // before it, and those above are the next nr-1-r entries (nvn-1-r for the
 // energy row).
 static constexpr long long kSpinLimit = 1LL << 22;
-static constexpr int kPrefetch = 16;  // row entries per lane loaded before the wait
+static constexpr int kPrefetch = 10;  // row entries per lane loaded before the wait (320 a row)
 static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
@@ -539,33 +547,100 @@ struct TrsvArgs {
   const int64_t *rowptr;
   const int *colidx;
   const int64_t *diag;
-  const int *nbr_ptr;
-  const int *nbr_node;
   int num_nodes;
   int Tr;              // local index of the energy row, -1 without energy
   int nvn;             // nodal fields per node
-  unsigned *flags;     // per node: epoch of the last sweep that finished it
   unsigned *tickets;   // [0] L sweep, [1] U sweep (reset before each sweep)
   int *error;          // set when a wait gave up
 };
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+// the "unpublished" sentinels: signalling NaNs (exponent all ones, quiet bit
+// clear, non-zero payload)
+static constexpr unsigned long long kUnpub64 = 0xFFF5DEAD5EEDF00DULL;
+static constexpr unsigned kUnpub32 = 0xFFA5EED5u;
+__device__ __forceinline__ bool unpublished(double v) {
+  return (unsigned long long)__double_as_longlong(v) == kUnpub64;
+}
+__device__ __forceinline__ bool unpublished(float v) { return __float_as_uint(v) == kUnpub32; }
+__device__ __forceinline__ void set_unpublished(double *p) {
+  *p = __longlong_as_double((long long)kUnpub64);
+}
+__device__ __forceinline__ void set_unpublished(float *p) { *p = __uint_as_float(kUnpub32); }
+
+__device__ __forceinline__ double ld_relaxed(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ float ld_relaxed(const float *p) {
+  float v;
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(double *p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(float *p, float v) {
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+// fill a sweep's output with the sentinel and reset its ticket counter
+template <class T>
+__global__ void trsv_prepare_kernel(int64_t n, T *x, unsigned *ticket) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ticket = 0u;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    set_unpublished(x + i);
+}
+
+// one solution value, polled until published (bounded; 0 once given up)
+template <class T>
+__device__ __forceinline__ T poll_value(const T *p, bool &gave_up, const int *error) {
+  T v = ld_relaxed(p);
+  long long polls = 0;
+  while (unpublished(v)) {
+    if (gave_up || ++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile const int *)error)) {
+      gave_up = true;
+      return (T)0;
+    }
+    __nanosleep(32);
+    v = ld_relaxed(p);
+  }
+  return v;
+}
+
+// Stage B, shared by both sweeps: lane r of the calling warp solves row r of
+// the node's diagonal block.  L: unit lower triangle, own[r][c] = L(r, c)
+// for c < r.  U: own[r][j] = U(r, r+1+j) for j < na(r), rdg[r] = 1 / U(r, r).
+// v holds rhs - (off-node part) on entry; returns the solution of row r.
+template <class A, bool LOWER>
+__device__ __forceinline__ A node_block_solve(A v, int lane, int nr, int Tr, int nvn,
+                                              const A (*own)[kMaxNodeDofs], const A *rdg) {
+  if (LOWER) {
+    for (int c = 0; c < nr - 1; c++) {
+      const A zc = __shfl_sync(0xffffffffu, v, c);
+      if (lane > c && lane < nr) v = fmx(-own[lane][c], zc, v);
+    }
+  } else {
+    const int na = (lane == Tr ? nvn : nr) - 1 - lane;
+    for (int c = nr - 1; c >= 0; c--) {
+      if (lane == c) v *= rdg[c];
+      const A zc = __shfl_sync(0xffffffffu, v, c);
+      const int j = c - lane - 1;
+      if (j >= 0 && j < na) v = fmx(-own[lane][j], zc, v);
+    }
+  }
+  return v;
 }
 
 template <class T, bool LOWER>
-__global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g,
-                                                                      const T *__restrict__ lu,
-                                                                      T *z, unsigned epoch) {
+__global__ void __launch_bounds__(kTrsvThreads, 3)
+    trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu, const T *__restrict__ b, T *x) {
   using A = acc_t<T>;
   __shared__ A part[kMaxNodeDofs];               // off-node sums per row
   __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];  // own-node entries of the sweep's factor
-  __shared__ A dg[kMaxNodeDofs];                 // U diagonal
+  __shared__ A rdg[kMaxNodeDofs];                // reciprocal U diagonal
+  __shared__ A rhs[kMaxNodeDofs];                // the node's right-hand side
   __shared__ int s_node;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
@@ -578,12 +653,12 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
     const int n = s_node;
     if (n < 0) return;
     const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
-    // before waiting: this warp's first row -- its factor entries and their
-    // column indices do not depend on the sweep, so their loads overlap the
-    // wait and only the gather of z stays on the critical path
+    // before polling: everything that does not depend on the sweep
     A pv[kPrefetch];
     int pc[kPrefetch];
     int64_t pr0 = 0, pr1 = 0;
+    A rv = 0, ov = 0, dv = 1;
+    if (tid < nr) rv = (A)__ldcg(b + f0 + tid);
     if (warp < nr) {
       const int r = warp, i = f0 + r;
       const int64_t di = g.diag[i];
@@ -596,80 +671,79 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
         pv[k] = p < pr1 ? (A)lu[p] : (A)0;
         pc[k] = p < pr1 ? g.colidx[p] : -1;
       }
+      if (LOWER ? lane < r : lane < na) ov = (A)lu[LOWER ? di - r + lane : di + 1 + lane];
+      if (!LOWER && lane == 0) dv = (A)lu[di];
     }
-    // wait for the dependencies
-    bool gave_up = false;
-    for (int q = g.nbr_ptr[n] + tid; q < g.nbr_ptr[n + 1]; q += kTrsvThreads) {
-      const int m = g.nbr_node[q];
-      if (LOWER ? m >= n : m <= n) continue;
-      long long polls = 0;
-      while (ld_acquire(g.flags + m) != epoch) {
-        // past the limit, or once any CTA of the sweep has given up
-        if (++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile int *)g.error)) {
-          gave_up = true;
-          break;
-        }
-        __nanosleep(64);
-      }
+    if (tid < nr) rhs[tid] = rv;
+    if (warp < nr) {
+      const int r = warp;
+      if (LOWER ? lane < r : lane < (r == g.Tr ? g.nvn : nr) - 1 - r) own[r][lane] = ov;
+      if (!LOWER && lane == 0) rdg[r] = (A)1 / dv;
     }
-    if (__syncthreads_or(gave_up) && tid == 0) atomicExch(g.error, 1);
     // stage A
+    bool gave_up = false;
     for (int r = warp; r < nr; r += NW) {
-      const int i = f0 + r;
-      const int64_t di = g.diag[i];
-      const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
-      int64_t p0, p1;
-      if (LOWER) {
-        p0 = g.rowptr[i];
-        p1 = di - r;
-        if (lane < r) own[r][lane] = (A)lu[di - r + lane];
-      } else {
-        p0 = di + 1 + na;
-        p1 = g.rowptr[i + 1];
-        if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
-        if (lane == 0) dg[r] = (A)lu[di];
-      }
-      A s0 = 0, s1 = 0;
-      int64_t p = p0 + lane;
-      if (r == warp) {  // the prefetched row
+      A s0 = 0;
+      int64_t p, p1;
+      if (r == warp) {  // the prefetched row: poll its values, then add in order
+        A zv[kPrefetch];
+        unsigned pending = 0;
+#pragma unroll
+        for (int k = 0; k < kPrefetch; k++) {
+          zv[k] = 0;
+          if (pc[k] >= 0) {
+            const T v = ld_relaxed(x + pc[k]);
+            if (unpublished(v)) pending |= 1u << k; else zv[k] = (A)v;
+          }
+        }
+        long long polls = 0;
+        while (pending) {
+          if (++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
+            gave_up = true;
+            break;
+          }
+          __nanosleep(32);
+#pragma unroll
+          for (int k = 0; k < kPrefetch; k++) {
+            if (pending & (1u << k)) {
+              const T v = ld_relaxed(x + pc[k]);
+              if (!unpublished(v)) {
+                zv[k] = (A)v;
+                pending &= ~(1u << k);
+              }
+            }
+          }
+        }
 #pragma unroll
         for (int k = 0; k < kPrefetch; k++)
-          if (pc[k] >= 0) s0 = fmx(pv[k], (A)__ldcg(z + pc[k]), s0);
-        p += 32 * kPrefetch;
+          if (pc[k] >= 0) s0 = fmx(pv[k], zv[k], s0);
+        p = pr0 + lane + 32 * kPrefetch;
+        p1 = pr1;
+      } else {
+        const int i = f0 + r;
+        const int64_t di = g.diag[i];
+        const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
+        if (LOWER) {
+          p = g.rowptr[i] + lane;
+          p1 = di - r;
+          if (lane < r) own[r][lane] = (A)lu[di - r + lane];
+        } else {
+          p = di + 1 + na + lane;
+          p1 = g.rowptr[i + 1];
+          if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
+          if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
+        }
       }
-      for (; p + 32 < p1; p += 64) {
-        s0 = fmx((A)lu[p], (A)__ldcg(z + g.colidx[p]), s0);
-        s1 = fmx((A)lu[p + 32], (A)__ldcg(z + g.colidx[p + 32]), s1);
-      }
-      if (p < p1) s0 = fmx((A)lu[p], (A)__ldcg(z + g.colidx[p]), s0);
-      const A sum = wsum(s0 + s1);
+      for (; p < p1; p += 32) s0 = fmx((A)lu[p], (A)poll_value(x + g.colidx[p], gave_up, g.error), s0);
+      const A sum = wsum(s0);
       if (lane == 0) part[r] = sum;
     }
-    __syncthreads();
-    // stage B: the in-node solve, one thread
-    if (tid == 0) {
-      A zl[kMaxNodeDofs];
-      if (LOWER) {
-#pragma unroll 1
-        for (int r = 0; r < nr; r++) {
-          A v = (A)__ldcg(z + f0 + r) - part[r];
-          for (int c = 0; c < r; c++) v = fmx(-own[r][c], zl[c], v);
-          zl[r] = v;
-          __stcg(z + f0 + r, (T)v);
-        }
-      } else {
-#pragma unroll 1
-        for (int r = nr - 1; r >= 0; r--) {
-          const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
-          A v = (A)__ldcg(z + f0 + r) - part[r];
-          for (int c = 0; c < na; c++) v = fmx(-own[r][c], zl[r + 1 + c], v);
-          v /= dg[r];
-          zl[r] = v;
-          __stcg(z + f0 + r, (T)v);
-        }
-      }
-      // the release store orders this thread's z stores before the flag
-      st_release(g.flags + n, epoch);
+    if (__syncthreads_or(gave_up) && tid == 0) atomicExch(g.error, 1);
+    // stage B
+    if (warp == 0) {
+      A v = lane < nr ? rhs[lane] - part[lane] : (A)0;
+      v = node_block_solve<A, LOWER>(v, lane, nr, g.Tr, g.nvn, own, rdg);
+      if (lane < nr) st_relaxed(x + f0 + lane, (T)v);
     }
     __syncthreads();
   }
@@ -678,8 +752,9 @@ __global__ void __launch_bounds__(kTrsvThreads) trsv_sync_free_kernel(TrsvArgs g
 // One dependency level of a triangular sweep, one CTA per node: the nodes of
 // a level do not depend on each other, so the launch boundary is the only
 // synchronisation.  Same two stages as the sync-free sweep (rows over the
-// warps, then the in-node solve); used for short level schedules (the
-// multicoloured order), launched level after level from a captured graph.
+// warps, then the in-node solve over the lanes of warp 0), in place on z;
+// used for short level schedules (the multicoloured order), launched level
+// after level from a captured graph.
 template <class T, bool LOWER>
 __global__ void __launch_bounds__(kTrsvThreads)
     trsv_level_cta_kernel(const int *__restrict__ nodes, TrsvArgs g, const T *__restrict__ lu,
@@ -687,11 +762,14 @@ __global__ void __launch_bounds__(kTrsvThreads)
   using A = acc_t<T>;
   __shared__ A part[kMaxNodeDofs];
   __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];
-  __shared__ A dg[kMaxNodeDofs];
+  __shared__ A rdg[kMaxNodeDofs];
+  __shared__ A rhs[kMaxNodeDofs];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
   const int n = nodes[blockIdx.x];
   const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+  // the node's own right-hand side, all rows at once (only this CTA writes it)
+  if (tid < nr) rhs[tid] = (A)z[f0 + tid];
   for (int r = warp; r < nr; r += NW) {
     const int i = f0 + r;
     const int64_t di = g.diag[i];
@@ -705,7 +783,7 @@ __global__ void __launch_bounds__(kTrsvThreads)
       p0 = di + 1 + na;
       p1 = g.rowptr[i + 1];
       if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
-      if (lane == 0) dg[r] = (A)lu[di];
+      if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
     }
     A s0 = 0, s1 = 0;
     int64_t p = p0 + lane;
@@ -718,32 +796,15 @@ __global__ void __launch_bounds__(kTrsvThreads)
     if (lane == 0) part[r] = sum;
   }
   __syncthreads();
-  if (tid == 0) {
-    A zl[kMaxNodeDofs];
-    if (LOWER) {
-#pragma unroll 1
-      for (int r = 0; r < nr; r++) {
-        A v = (A)z[f0 + r] - part[r];
-        for (int c = 0; c < r; c++) v = fmx(-own[r][c], zl[c], v);
-        zl[r] = v;
-        z[f0 + r] = (T)v;
-      }
-    } else {
-#pragma unroll 1
-      for (int r = nr - 1; r >= 0; r--) {
-        const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
-        A v = (A)z[f0 + r] - part[r];
-        for (int c = 0; c < na; c++) v = fmx(-own[r][c], zl[r + 1 + c], v);
-        v /= dg[r];
-        zl[r] = v;
-        z[f0 + r] = (T)v;
-      }
-    }
+  if (warp == 0) {
+    A v = lane < nr ? rhs[lane] - part[lane] : (A)0;
+    v = node_block_solve<A, LOWER>(v, lane, nr, g.Tr, g.nvn, own, rdg);
+    if (lane < nr) z[f0 + lane] = (T)v;
   }
 }
 
-// the sweeps' view of the preconditioner layout (flags, tickets and the
-// order are set by the sync-free sweep)
+// the sweeps' view of the preconditioner layout (tickets and the order are
+// set by the sync-free sweep)
 static TrsvArgs trsv_args(const Solver *S) {
   TrsvArgs g;
   g.order = nullptr;
@@ -751,12 +812,9 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.rowptr = S->P.rowptr;
   g.colidx = S->P.colidx;
   g.diag = S->P.diag;
-  g.nbr_ptr = S->P.nbr_ptr;
-  g.nbr_node = S->P.nbr_node;
   g.num_nodes = S->C->L.num_nodes;
   g.Tr = S->C->L.energy ? S->C->L.dim : -1;
   g.nvn = S->C->L.nvn;
-  g.flags = nullptr;
   g.tickets = nullptr;
   g.error = nullptr;
   return g;
@@ -812,7 +870,7 @@ Solver::~Solver() {
   if (prec64) cudaGraphExecDestroy(prec64);
   if (prec32) cudaGraphExecDestroy(prec32);
   void *p[] = {d_lu, d_lu32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
-               d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
+               d_sweep_y, d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
   for (void *q : owned)
@@ -1099,12 +1157,10 @@ int Solver::copy_factors(double *host, bool fp32, cudaStream_t st) {
 
 template <class T>
 static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
-  Context *C = S->C;
   if (!S->d_flags) {
-    GB_CU(cudaMalloc(&S->d_flags, sizeof(unsigned) * C->L.num_nodes + 16 * sizeof(unsigned)),
-          "trsv flags");
-    GB_CU(cudaMemsetAsync(S->d_flags, 0, sizeof(unsigned) * C->L.num_nodes + 16 * sizeof(unsigned),
-                          st), "trsv flags");
+    GB_CU(cudaMalloc(&S->d_flags, 16 * sizeof(unsigned)), "trsv tickets");
+    GB_CU(cudaMemsetAsync(S->d_flags, 0, 16 * sizeof(unsigned), st), "trsv tickets");
+    GB_CU(cudaMalloc(&S->d_sweep_y, sizeof(double) * (size_t)S->N), "trsv scratch");
     int per_sm = 1 << 30, dev = 0, sms = 0;
     const void *fns[4] = {(const void *)trsv_sync_free_kernel<double, true>,
                           (const void *)trsv_sync_free_kernel<double, false>,
@@ -1118,21 +1174,20 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     S->trsv_grid = std::max(1, per_sm) * sms;
+    S->prep_grid = 2 * sms;
   }
   TrsvArgs g = trsv_args(S);  // the order is set per sweep below
-  g.flags = S->d_flags;
-  g.tickets = S->d_flags + C->L.num_nodes;
-  g.error = (int *)(S->d_flags + C->L.num_nodes + 4);
-  for (int pass = 0; pass < 2; pass++) {
-    const unsigned epoch = ++S->epoch;
-    GB_CU(cudaMemsetAsync(g.tickets, 0, 2 * sizeof(unsigned), st), "tickets");
-    g.order = pass == 0 ? S->d_lo_nodes : S->d_up_nodes;
-    if (pass == 0)
-      trsv_sync_free_kernel<T, true><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, epoch);
-    else
-      trsv_sync_free_kernel<T, false><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, epoch);
-    GB_CU(cudaGetLastError(), "trsv");
-  }
+  g.tickets = S->d_flags;
+  g.error = (int *)(S->d_flags + 4);
+  T *y = static_cast<T *>(S->d_sweep_y);
+  // L: z -> y, then U: y -> z; each output starts all unpublished
+  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y, g.tickets + 0);
+  g.order = S->d_lo_nodes;
+  trsv_sync_free_kernel<T, true><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, y);
+  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z, g.tickets + 1);
+  g.order = S->d_up_nodes;
+  trsv_sync_free_kernel<T, false><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, y, z);
+  GB_CU(cudaGetLastError(), "trsv");
   return 0;
 }
 
@@ -1143,10 +1198,9 @@ bool Solver::use_level_graph() const {
 int Solver::check_trsv_error() {
   if (!d_flags) return 0;
   int h = 0;
-  GB_CU(cudaMemcpy(&h, d_flags + C->L.num_nodes + 4, sizeof(int), cudaMemcpyDeviceToHost),
-        "trsv error");
+  GB_CU(cudaMemcpy(&h, d_flags + 4, sizeof(int), cudaMemcpyDeviceToHost), "trsv error");
   if (h) {
-    cudaMemset(d_flags + C->L.num_nodes + 4, 0, sizeof(int));
+    cudaMemset(d_flags + 4, 0, sizeof(int));
     return fail("triangular solve: a dependency wait gave up");
   }
   return 0;

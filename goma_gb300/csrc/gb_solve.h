@@ -79,9 +79,9 @@ struct Solver {
   double *d_t = nullptr, *d_w = nullptr, *d_r = nullptr, *d_xs = nullptr;
   float *d_t32 = nullptr, *d_w32 = nullptr;
   cudaGraphExec_t prec64 = nullptr, prec32 = nullptr;  // captured ILU solves on d_t / d_t32
-  unsigned *d_flags = nullptr;  // per-node epochs, tickets, error word
-  unsigned epoch = 0;
-  int trsv_grid = 0;
+  unsigned *d_flags = nullptr;  // sync-free sweeps: [0..1] tickets, [4] error word
+  void *d_sweep_y = nullptr;    // sync-free sweeps: the L sweep's output (N values)
+  int trsv_grid = 0, prep_grid = 0;
   int check_trsv_error();
   // level-scheduled sweeps from a captured graph (else the sync-free ones)
   bool use_level_graph() const;
