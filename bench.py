@@ -555,8 +555,9 @@ def main():
                     help="element kernel: 0 automatic (4), 1 scalar FP64, 2 FP64 tensor pipe "
                          "with per-fragment coefficients, 3 FP64 tensor-pipe products over "
                          "operand tables, 4 sum factorisation")
-    ap.add_argument("--solve-nel", type=int, default=8,
-                    help="cube size of the time-to-solve leg (0 skips it)")
+    ap.add_argument("--solve-nel", type=int, default=16,
+                    help="cube size of the time-to-solve leg (0 skips it; the run with the "
+                         "reference's solver settings is added up to 8^3)")
     ap.add_argument("--solve-ilu", type=int, default=-1,
                     help="ILU(0) node order of the time-to-solve leg: 0 the reference's, "
                          "1 multicoloured, -1 by size (multicoloured up to 12^3)")
