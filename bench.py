@@ -433,6 +433,46 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
     return out
 
 
+def cpu_time_to_solve(nel=8, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, krylov=30, linear_tol=1e-8):
+    """The time-to-solve continuation of `time_to_solve` (Ra ra0 -> ra1 in
+    nsteps log-uniform steps from rest, zeroth-order predictor, scaled
+    |R| < tol) on one host core: the CPU oracle's assembly (restatement of
+    the reference's matrix_fill), row-sum scaling and Newton loop with its
+    ILU(0)-GMRES(krylov) restatement at the reference's solver settings
+    (natural node order, every linear solve to linear_tol).  The reference's
+    own Krylov solver (AztecOO) is third-party and not built here, so this
+    is labelled "not AztecOO"; it pairs with the GPU's
+    plain_fp64_reference_solver run of the same sweep."""
+    import dataclasses
+
+    import oracle
+    from goma_gb300 import problem as pb
+    prob = pb.boussinesq_cube_3d(nel, ra0, PR)
+    x = None
+    recs = []
+    t0 = time.perf_counter()
+    for k, ra in enumerate(np.geomspace(ra0, ra1, nsteps + 1)):
+        mat = dataclasses.replace(prob.material, momentum_source=(0.0, 0.0, -ra * PR))
+        o = oracle.Oracle(dataclasses.replace(prob, material=mat))
+        if x is None:
+            x = o.dirichlet_init(np.zeros(o.N))
+        ts = time.perf_counter()
+        x, it, lin, _ = o.newton_gmres(x, 40, tol, linear_tol=linear_tol, krylov=krylov,
+                                       max_linear_its=4000)
+        recs.append({"ra": float(ra), "newton_its": int(it), "linear_its": int(lin),
+                     "seconds": time.perf_counter() - ts})
+        if it < 0:
+            break
+    return {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
+                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
+            "solver": "CPU oracle: ILU(0) (natural order) + GMRES(%d) restatement, not AztecOO, "
+                      "every linear solve to %g, 1 thread" % (krylov, linear_tol),
+            "seconds": time.perf_counter() - t0, "cores": 1,
+            "converged": all(r["newton_its"] >= 0 for r in recs) and len(recs) == nsteps + 1,
+            "newton_its": sum(max(r["newton_its"], 0) for r in recs),
+            "linear_its": sum(r["linear_its"] for r in recs), "steps": recs}
+
+
 def ilu_orders(sizes=(8, 16, 24), ra=1e4, tol=1e-10):
     """One Newton solve of the Boussinesq cube from rest (Ra `ra`, scaled
     |R| < tol, GMRES(60), forcing rule) per cube size, ILU(0) node order
@@ -573,7 +613,8 @@ def main():
                          "(assembly of the 512-problem sweep), batch64_solve (Newton solve of "
                          "64 such problems, n in [16, 32], Re in [10, 100]), bfs (the 96x32 "
                          "Carreau step continuation), ilu_orders (cube solves in both ILU(0) "
-                         "node orders, 8^3 to 24^3)")
+                         "node orders, 8^3 to 24^3), cpu_solve (the 8^3 time-to-solve sweep on "
+                         "one host core with the oracle's ILU(0)-GMRES(30))")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -752,6 +793,8 @@ def main():
                 extra[w] = bfs_continuation()
             elif w == "ilu_orders":
                 extra[w] = ilu_orders()
+            elif w == "cpu_solve":
+                extra[w] = cpu_time_to_solve(8)
         line["workloads"] = extra
     if rank == 0:
         print(json.dumps(line))

@@ -54,6 +54,10 @@ def lib():
         L.orc_row_sum_scale.argtypes = [vp, dp, dp, dp]
         L.orc_newton.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp]
         L.orc_ilu0.argtypes = [vp, dp, ctypes.c_double, dp]
+        L.orc_gmres_ilu0.argtypes = [vp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, ip, dp]
+        L.orc_newton_gmres.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, ip, dp]
         L.orc_mesh_sizes.argtypes = [ctypes.c_char_p, ip, ip, ip]
         L.orc_mesh_fill.argtypes = [ctypes.c_char_p, dp, ip, ip, ip]
         _lib = L
@@ -145,6 +149,35 @@ class Oracle:
         it = lib().orc_newton(self.h, _p(x, ctypes.c_double), max_it, tol,
                               _p(norms, ctypes.c_double))
         return x, it, norms[:max(it + 1, 0)] if it >= 0 else norms
+
+    def gmres_ilu0(self, a, lu, b, krylov=30, maxit=500, tol=1e-8):
+        """ILU(0)-preconditioned GMRES(krylov) on the MSR system a x = b from
+        x = 0: (x, converged, iterations, relative residual)."""
+        a = np.ascontiguousarray(a, np.float64)
+        lu = np.ascontiguousarray(lu, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.empty(self.N)
+        its = ctypes.c_int()
+        rel = ctypes.c_double()
+        st = lib().orc_gmres_ilu0(self.h, _p(a, ctypes.c_double), _p(lu, ctypes.c_double),
+                                  _p(b, ctypes.c_double), _p(x, ctypes.c_double), krylov, maxit,
+                                  tol, ctypes.byref(its), ctypes.byref(rel))
+        if st < 0:
+            raise MemoryError("orc_gmres_ilu0")
+        return x, st == 0, its.value, rel.value
+
+    def newton_gmres(self, x0, max_it=40, tol=1e-10, linear_tol=1e-8, krylov=30,
+                     max_linear_its=4000, tau=1e-4):
+        """Newton with ILU(0)-GMRES(krylov) linear solves (the reference's
+        solver settings): (x, Newton iterations or -1, total Krylov
+        iterations, scaled-residual L2 norms)."""
+        x = np.ascontiguousarray(x0, np.float64).copy()
+        norms = np.full(max_it, np.nan)
+        lin = ctypes.c_int()
+        it = lib().orc_newton_gmres(self.h, _p(x, ctypes.c_double), max_it, tol, linear_tol,
+                                    krylov, max_linear_its, tau, ctypes.byref(lin),
+                                    _p(norms, ctypes.c_double))
+        return x, it, lin.value, norms[:max(it + 1, 0)] if it >= 0 else norms
 
 
 def mesh_from_spec(spec):

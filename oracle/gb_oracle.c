@@ -786,6 +786,191 @@ int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *
   return result;
 }
 
+/* y = A x for an MSR matrix (src/sl_auxutil.c:373, MV_MSR). */
+static void msr_matvec(int N, const int *ija, const double *a, const double *x, double *y) {
+  for (int i = 0; i < N; i++) {
+    double s = a[i] * x[i];
+    for (int k = ija[i]; k < ija[i + 1]; k++) s += a[k] * x[ija[k]];
+    y[i] = s;
+  }
+}
+
+/* z = (LU)^-1 z in place with ILU(0) factors in the MSR layout: unit lower
+ * triangle below the diagonal, U on and above it. */
+static void ilu0_apply(int N, const int *ija, const double *lu, double *z) {
+  for (int i = 0; i < N; i++) {
+    double s = z[i];
+    for (int k = ija[i]; k < ija[i + 1] && ija[k] < i; k++) s -= lu[k] * z[ija[k]];
+    z[i] = s;
+  }
+  for (int i = N - 1; i >= 0; i--) {
+    double s = z[i];
+    for (int k = ija[i + 1] - 1; k >= ija[i] && ija[k] > i; k--) s -= lu[k] * z[ija[k]];
+    z[i] = s / lu[i];
+  }
+}
+
+static double dot(int N, const double *x, const double *y) {
+  double s = 0.0;
+  for (int i = 0; i < N; i++) s += x[i] * y[i];
+  return s;
+}
+
+/* Restarted GMRES(m), right-preconditioned, modified Gram-Schmidt and
+ * Givens rotations (Saad, Iterative Methods for Sparse Linear Systems, 2nd
+ * ed., Alg. 9.5).  The reference's Krylov solver is AztecOO's GMRES with
+ * ILU(0) on one subdomain (third-party, Trilinos, not in the reference
+ * tree; options from src/sl_util.c:417,556); this restates the published
+ * algorithm so a CPU Krylov solve can be timed next to the GPU's. */
+int orc_gmres_ilu0(const orc_problem *p, const double *a, const double *lu, const double *b,
+                   double *x, int m, int maxit, double tol, int *its, double *relres) {
+  const int N = p->N;
+  const int *ija = p->ija;
+  double *V = (double *)malloc(sizeof(double) * (size_t)N * (size_t)(m + 1));
+  double *z = (double *)malloc(sizeof(double) * (size_t)N);
+  double *w = (double *)malloc(sizeof(double) * (size_t)N);
+  double *H = (double *)calloc((size_t)(m + 1) * (size_t)m, sizeof(double));
+  double *cs = (double *)malloc(sizeof(double) * (size_t)m);
+  double *sn = (double *)malloc(sizeof(double) * (size_t)m);
+  double *g = (double *)malloc(sizeof(double) * (size_t)(m + 1));
+  double *yv = (double *)malloc(sizeof(double) * (size_t)m);
+  int result = -1, k_total = 0;
+  double rel = 1.0;
+  if (!V || !z || !w || !H || !cs || !sn || !g || !yv) goto done;
+  for (int i = 0; i < N; i++) x[i] = 0.0;
+  const double bnorm = sqrt(dot(N, b, b));
+  if (bnorm == 0.0) {
+    result = 0;
+    rel = 0.0;
+    goto done;
+  }
+  memcpy(w, b, sizeof(double) * (size_t)N); /* r0 = b - A 0 */
+  result = 1;
+  while (k_total < maxit) {
+    const double beta = sqrt(dot(N, w, w));
+    rel = beta / bnorm;
+    if (rel <= tol) {
+      result = 0;
+      break;
+    }
+    for (int i = 0; i < N; i++) V[i] = w[i] / beta;
+    for (int i = 0; i <= m; i++) g[i] = 0.0;
+    g[0] = beta;
+    int j = 0;
+    for (; j < m && k_total < maxit; j++) {
+      double *vj = V + (size_t)j * N, *vn = V + (size_t)(j + 1) * N;
+      memcpy(z, vj, sizeof(double) * (size_t)N);
+      ilu0_apply(N, ija, lu, z);
+      msr_matvec(N, ija, a, z, vn);
+      for (int i = 0; i <= j; i++) {
+        const double *vi = V + (size_t)i * N;
+        const double h = dot(N, vn, vi);
+        H[i * m + j] = h;
+        for (int q = 0; q < N; q++) vn[q] -= h * vi[q];
+      }
+      const double hn = sqrt(dot(N, vn, vn));
+      H[(j + 1) * m + j] = hn;
+      if (hn > 0.0)
+        for (int q = 0; q < N; q++) vn[q] /= hn;
+      for (int i = 0; i < j; i++) { /* earlier rotations on column j */
+        const double t = cs[i] * H[i * m + j] + sn[i] * H[(i + 1) * m + j];
+        H[(i + 1) * m + j] = -sn[i] * H[i * m + j] + cs[i] * H[(i + 1) * m + j];
+        H[i * m + j] = t;
+      }
+      const double hd = H[j * m + j], hs = H[(j + 1) * m + j];
+      const double r = sqrt(hd * hd + hs * hs);
+      cs[j] = r > 0.0 ? hd / r : 1.0;
+      sn[j] = r > 0.0 ? hs / r : 0.0;
+      H[j * m + j] = r;
+      H[(j + 1) * m + j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      k_total++;
+      if (fabs(g[j + 1]) <= tol * bnorm) {
+        j++;
+        break;
+      }
+    }
+    /* y = H^-1 g (upper triangular, j columns), x += M^-1 V y */
+    for (int i = j - 1; i >= 0; i--) {
+      double s = g[i];
+      for (int c = i + 1; c < j; c++) s -= H[i * m + c] * yv[c];
+      yv[i] = H[i * m + i] != 0.0 ? s / H[i * m + i] : 0.0;
+    }
+    for (int q = 0; q < N; q++) z[q] = 0.0;
+    for (int i = 0; i < j; i++) {
+      const double *vi = V + (size_t)i * N;
+      for (int q = 0; q < N; q++) z[q] += yv[i] * vi[q];
+    }
+    ilu0_apply(N, ija, lu, z);
+    for (int q = 0; q < N; q++) x[q] += z[q];
+    msr_matvec(N, ija, a, x, w); /* true residual for the restart */
+    for (int q = 0; q < N; q++) w[q] = b[q] - w[q];
+  }
+  if (result == 1) {
+    rel = sqrt(dot(N, w, w)) / bnorm;
+    if (rel <= tol) result = 0;
+  }
+done:
+  if (its) *its = k_total;
+  if (relres) *relres = rel;
+  free(V);
+  free(z);
+  free(w);
+  free(H);
+  free(cs);
+  free(sn);
+  free(g);
+  free(yv);
+  return result;
+}
+
+/* Newton loop of solve_nonlinear_problem (src/mm_sol_nonlinear.c:1108) as in
+ * orc_newton, with the linear solve done by ILU(0)-GMRES(m) on the row-sum
+ * scaled system (the reference's AZTECOO case, :1805). */
+int orc_newton_gmres(const orc_problem *p, double *x, int max_it, double tol, double lin_tol,
+                     int m, int lin_maxit, double tau, int *linear_its, double *norms) {
+  const int N = p->N;
+  double *R = (double *)malloc(sizeof(double) * (size_t)N);
+  double *dx = (double *)malloc(sizeof(double) * (size_t)N);
+  double *a = (double *)malloc(sizeof(double) * (size_t)p->msr_len);
+  double *lu = (double *)malloc(sizeof(double) * (size_t)p->msr_len);
+  double *sc = (double *)malloc(sizeof(double) * (size_t)N);
+  int result = -1, lin_total = 0;
+  if (!R || !dx || !a || !lu || !sc) goto done;
+  for (int it = 0; it < max_it; it++) {
+    memset(R, 0, sizeof(double) * (size_t)N);
+    memset(a, 0, sizeof(double) * (size_t)p->msr_len);
+    if (orc_matrix_fill(p, x, R, a, 0, p->d.num_elems) != 0) break;
+    orc_row_sum_scale(p, a, R, sc);
+    double l2 = 0.0, loo = 0.0;
+    for (int i = 0; i < N; i++) {
+      l2 += R[i] * R[i];
+      if (fabs(R[i]) > loo) loo = fabs(R[i]);
+    }
+    l2 = sqrt(l2);
+    if (norms) norms[it] = l2;
+    if (!isfinite(l2)) break;
+    if (it > 0 && l2 < tol && loo < tol) {
+      result = it;
+      break;
+    }
+    if (orc_ilu0(p, a, tau, lu) != 0) break;
+    int its = 0;
+    if (orc_gmres_ilu0(p, a, lu, R, dx, m, lin_maxit, lin_tol, &its, NULL) < 0) break;
+    lin_total += its;
+    for (int i = 0; i < N; i++) x[i] -= dx[i];
+  }
+done:
+  if (linear_its) *linear_its = lin_total;
+  free(R);
+  free(dx);
+  free(a);
+  free(lu);
+  free(sc);
+  return result;
+}
+
 /* ------------------------------------------------- mesh generator access */
 #include "mesh_gen.h"
 

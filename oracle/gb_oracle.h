@@ -59,6 +59,18 @@ int orc_ilu0(const orc_problem *p, const double *a, double tau, double *lu);
  * iterations (>= 0) on convergence, -1 on failure.  norms (optional) gets
  * the scaled-residual L2 norm of every iteration (max_it entries). */
 int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *norms);
+/* Restarted right-preconditioned GMRES(m) with the ILU(0) factors lu (from
+ * orc_ilu0) on the MSR system a x = b, from x = 0, until the residual is
+ * below tol * |b| or maxit iterations.  Returns 0 when converged, 1 when
+ * not, -1 on allocation failure; *its and *relres (optional) report. */
+int orc_gmres_ilu0(const orc_problem *p, const double *a, const double *lu, const double *b,
+                   double *x, int m, int maxit, double tol, int *its, double *relres);
+/* Newton as orc_newton with ILU(0)-GMRES(m) (pivot floor tau, linear
+ * tolerance lin_tol, at most lin_maxit iterations per solve) instead of the
+ * direct solve.  Returns the Newton iterations on convergence, -1 on
+ * failure; *linear_its (optional) gets the total Krylov iterations. */
+int orc_newton_gmres(const orc_problem *p, double *x, int max_it, double tol, double lin_tol,
+                     int m, int lin_maxit, double tau, int *linear_its, double *norms);
 
 #ifdef __cplusplus
 }
