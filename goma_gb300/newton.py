@@ -146,13 +146,19 @@ class GomaNewton:
 
     # --- solve_nonlinear_problem
     def newton_opts(self, **kw):
+        """gb_newton_opts with the defaults of gb_newton_opts_default and the
+        given fields (fp32_inner sets linear_precision); an unknown name is an
+        error rather than a silently ignored attribute."""
         o = _lib.NewtonOpts()
         self._L.gb_newton_opts_default(ctypes.byref(o))
+        fields = {f[0] for f in o._fields_}
         for k, v in kw.items():
             if k == "fp32_inner":
                 o.linear_precision = 1 if v else 0
-            else:
+            elif k in fields:
                 setattr(o, k, v)
+            else:
+                raise TypeError("unknown Newton option %r" % k)
         return o
 
     def solve_nonlinear_problem(self, x0=None, **opts):

@@ -54,3 +54,18 @@ def test_host_layout_rejects_bad_connectivity(lib):
     prob.mesh.conn[1, 3] = prob.mesh.num_nodes + 5
     with pytest.raises(_lib.GbError, match="outside"):
         msr_pattern_host(prob)
+
+
+def test_newton_options_fill_the_abi_struct(lib):
+    """gb_newton_opts_default needs no device; named options land in the C
+    struct (fp32_inner as linear_precision) and an unknown name is an error."""
+    import types
+
+    from goma_gb300.newton import GomaNewton
+    host = types.SimpleNamespace(_L=lib)
+    o = GomaNewton.newton_opts(host, krylov_dim=45, forcing=1, fp32_inner=True, linear_tol=1e-9)
+    assert (o.krylov_dim, o.forcing, o.linear_precision, o.linear_tol) == (45, 1, 1, 1e-9)
+    d = GomaNewton.newton_opts(host)
+    assert d.linear_precision == 0 and d.max_newton > 0
+    with pytest.raises(TypeError, match="krylov"):
+        GomaNewton.newton_opts(host, krylov=30)

@@ -123,3 +123,26 @@ def test_multicolour_ilu_solves_the_cube(trsv):
         sols.append(x)
         gn.close()
     assert np.abs(sols[0] - sols[1]).max() <= TOL_X * np.abs(sols[0]).max()
+
+
+def test_gpu_krylov_counts_match_oracle_gmres():
+    """With the reference's solver settings (ILU(0) in its node order,
+    GMRES(30), every linear solve to 1e-8) the GPU Newton loop takes the
+    same Newton steps as the oracle's Newton with its restated
+    ILU(0)-GMRES(30), the same Krylov iterations up to the rounding of the
+    two Gram-Schmidt variants (classical with one reorthogonalisation on the
+    GPU, modified in the oracle), and reaches the same fields."""
+    prob = pb.boussinesq_cube_3d(3, 1e4, 0.71)
+    o = oracle.Oracle(prob)
+    x0 = o.dirichlet_init(np.zeros(o.N))
+    xo, ito, lino, _ = o.newton_gmres(x0, 40, 1e-10, linear_tol=1e-8, krylov=30,
+                                      max_linear_its=4000)
+    assert ito > 0
+    gn = GomaNewton(prob)
+    x, conv, st = gn.solve_nonlinear_problem(x0, residual_tol=1e-10, linear_tol=1e-8,
+                                             krylov_dim=30, forcing=0, max_newton=40,
+                                             max_linear_its=4000)
+    assert conv
+    assert abs(st["newton_its"] - ito) <= 1
+    assert abs(st["linear_its"] - lino) <= max(3, 0.1 * lino)
+    assert np.abs(x - xo).max() <= TOL_X * np.abs(xo).max()
