@@ -216,6 +216,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
                      "candidate_seconds": sum(r.get("candidates_s", 0.0) for r in recs),
                      "candidate_residual_seconds": sum(r.get("residuals_s", 0.0) for r in recs),
                      "training_seconds": sum(r.get("train_s", 0.0) for r in recs)}
+        out[mode]["newton_steps_per_s"] = out[mode]["newton_its"] / dt
         del gn
     a = sols.get("plain_fp64")
     complete = {m for m in sols if out[m]["steps_done"] == nsteps}
@@ -463,14 +464,16 @@ def cpu_time_to_solve(nel=8, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, krylov=30, l
                      "seconds": time.perf_counter() - ts})
         if it < 0:
             break
-    return {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
-                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
-            "solver": "CPU oracle: ILU(0) (natural order) + GMRES(%d) restatement, not AztecOO, "
-                      "every linear solve to %g, 1 thread" % (krylov, linear_tol),
-            "seconds": time.perf_counter() - t0, "cores": 1,
-            "converged": all(r["newton_its"] >= 0 for r in recs) and len(recs) == nsteps + 1,
-            "newton_its": sum(max(r["newton_its"], 0) for r in recs),
-            "linear_its": sum(r["linear_its"] for r in recs), "steps": recs}
+    out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
+                       "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
+           "solver": "CPU oracle: ILU(0) (natural order) + GMRES(%d) restatement, not AztecOO, "
+                     "every linear solve to %g, 1 thread" % (krylov, linear_tol),
+           "seconds": time.perf_counter() - t0, "cores": 1,
+           "converged": all(r["newton_its"] >= 0 for r in recs) and len(recs) == nsteps + 1,
+           "newton_its": sum(max(r["newton_its"], 0) for r in recs),
+           "linear_its": sum(r["linear_its"] for r in recs), "steps": recs}
+    out["newton_steps_per_s"] = out["newton_its"] / out["seconds"]
+    return out
 
 
 def ilu_orders(sizes=(8, 16, 24), ra=1e4, tol=1e-10):
