@@ -351,14 +351,19 @@ def batch_sweep_assembly(num=512, seed=0, steps=3, warmup=2):
 
 
 def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, check=2,
-                      ilu_ordering=0, budget_s=240.0, nmin=16, nmax=32, re_max=100.0):
+                      ilu_ordering=0, budget_s=240.0, nmin=16, nmax=32, re_max=100.0,
+                      max_ratio=None, max_linear_its=600):
     """The 512-problem sweep: unit-square QUAD9 Q2/P1 cavities and channels,
     meshes n x n with n uniform in [16, 64], Re log-uniform in [10, 1000]
     (seeded), all held in one context as a disjoint union with per-element
     Reynolds numbers, so one assembly launch per colour and one Krylov solve
     serve every problem.  Newton from rest to the scaled residual `tol`,
     through `stages` geometric Reynolds ramps (Re_p 10^(k/stages) ... up to
-    each problem's own Re).  The Krylov solve is the batched GMRES (one
+    each problem's own Re).  With max_ratio the number of stages is chosen
+    so that no problem's Re grows by more than that factor from one stage to
+    the next (Newton from the previous stage's solution converges in 4-5
+    steps for ratios up to ~1.7 on cavities up to Re 1000; a 10x step from
+    Re 100 diverges).  The Krylov solve is the batched GMRES (one
     Arnoldi process per problem).  `check` of the smallest members are solved
     again, on their own, by the CPU oracle, and compared.  Stages stop once
     `budget_s` seconds have passed (reported as not converged)."""
@@ -369,6 +374,8 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
     from goma_gb300.newton import GomaNewton
     t0 = _time.perf_counter()
     b = pb.batch_sweep_2d(num, seed=seed, nmin=nmin, nmax=nmax, re_max=re_max)
+    if max_ratio is not None:
+        stages = max(1, int(np.ceil(np.log(b.elem_re.max() / 10.0) / np.log(max_ratio))))
     gn = GomaNewton(b.problem)
     gn.set_ilu_ordering(ilu_ordering)
     setup_s = _time.perf_counter() - t0
@@ -385,7 +392,7 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
             break
         ts = _time.perf_counter()
         x, conv, st = gn.solve_nonlinear_problem(
-            x, residual_tol=tol, linear_tol=1e-8, max_newton=15, max_linear_its=600,
+            x, residual_tol=tol, linear_tol=1e-8, max_newton=15, max_linear_its=max_linear_its,
             fp32_inner=fp32_inner, inner_tol=1e-3, forcing=1, forcing_max=1e-2)
         print("batch stage %d: converged %s, %d Newton, %d Krylov, %.1f s, |R| %s" % (
             k, conv, st["newton_its"], st["linear_its"], _time.perf_counter() - ts,
@@ -614,7 +621,9 @@ def main():
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
                          "(assembly of the 512-problem sweep), batch64_solve (Newton solve of "
-                         "64 such problems, n in [16, 32], Re in [10, 100]), bfs (the 96x32 "
+                         "64 such problems, n in [16, 32], Re in [10, 100]), batch512_solve "
+                         "(the full sweep: 512 problems, n in [16, 64], Re in [10, 1000], Re "
+                         "stages of at most 1.6x), bfs (the 96x32 "
                          "Carreau step continuation), ilu_orders (cube solves in both ILU(0) "
                          "node orders, 8^3 to 24^3), cpu_solve (the 8^3 time-to-solve sweep on "
                          "one host core with the oracle's ILU(0)-GMRES(30))")
@@ -799,6 +808,10 @@ def main():
                 extra[w] = batch_sweep_assembly(512)
             elif w == "batch64_solve":
                 extra[w] = batch_sweep_solve(64)
+            elif w == "batch512_solve":
+                extra[w] = batch_sweep_solve(512, nmin=16, nmax=64, re_max=1000.0,
+                                             max_ratio=1.6, budget_s=900.0, check=1,
+                                             max_linear_its=2500)
             elif w == "bfs":
                 extra[w] = bfs_continuation()
             elif w == "ilu_orders":
