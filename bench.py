@@ -139,7 +139,8 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
 
 
 def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=60,
-                  forcing=1, reference_solver=True, modes=None, budget_s=None):
+                  forcing=1, reference_solver=True, modes=None, budget_s=None,
+                  factorization_reuse=0):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
@@ -154,7 +155,8 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
     run is repeated with the reference's settings (ILU(0) in its node
     order, GMRES(30), every linear solve to 1e-8).  `modes` selects runs;
     `budget_s` ends each run's sweep after that many seconds (reported as
-    steps done).  Returns a dict with the times, Newton/Krylov counts,
+    steps done).  factorization_reuse (GB_FACTOR_*) applies to every run
+    but the one with the reference's settings.  Returns a dict with the times, Newton/Krylov counts,
     per-phase splits and the relative difference of the converged
     solutions."""
     if ilu_ordering < 0:
@@ -171,9 +173,11 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
 
     out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
-           "linear_solver": "ILU(0) in the %s node order, GMRES(%d), %s" % (
+           "linear_solver": "ILU(0) in the %s node order, GMRES(%d), %s, factors %s" % (
                "reference's" if ilu_ordering == 0 else "multicoloured", krylov,
-               "Eisenstat-Walker forcing (1e-8 .. 1e-2)" if forcing else "linear tol 1e-8")}
+               "Eisenstat-Walker forcing (1e-8 .. 1e-2)" if forcing else "linear tol 1e-8",
+               ["at every Newton step", "once per Newton solve", "reused across solves"][
+                   factorization_reuse])}
     # first-use costs of the process (CUDA module loading of the network and
     # copy kernels) are paid once here, outside both timed runs
     from goma_gb300.mlp import GpuMLP
@@ -195,7 +199,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
         opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
                     fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3,
                     krylov_dim=30 if refs else krylov, forcing=0 if refs else forcing,
-                    forcing_max=1e-2)
+                    forcing_max=1e-2, factorization_reuse=0 if refs else factorization_reuse)
         torch.cuda.synchronize()
         t = time.perf_counter()
         recs, x = continuation(gn, ra0, ra1, nsteps,
@@ -210,6 +214,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
         out[mode] = {"seconds": dt, "steps_done": len(recs) - 1, "last_ra": recs[-1]["lam"],
                      "newton_its": sum(r["newton_its"] for r in recs),
                      "linear_its": sum(r.get("linear_its", 0) for r in recs),
+                     "factorizations": sum(r.get("factorizations", 0) for r in recs),
                      "guesses": [r["guess"] for r in recs[1:]],
                      "newton_seconds": {k.replace("_ms", ""): v * 1e-3 for k, v in ms.items()},
                      "predictor_seconds": sum(r.get("predictor_s", 0.0) for r in recs),
@@ -617,6 +622,9 @@ def main():
                          "(default: all)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
                     help="seconds per run of the time-to-solve leg (0: no limit)")
+    ap.add_argument("--solve-reuse", type=int, default=0,
+                    help="ILU(0) factorisation reuse of the time-to-solve leg: 0 every Newton "
+                         "step, 1 once per Newton solve, 2 across solves")
     ap.add_argument("--workloads", default="",
                     help="extra timed workloads, comma separated: reacting (the 64x64x32 "
                          "reacting channel), reacting_small (its 16x16x8 version), batch512 "
@@ -794,7 +802,7 @@ def main():
             line["time_to_solve"] = time_to_solve(
                 args.solve_nel, ilu_ordering=args.solve_ilu, reference_solver=args.solve_nel <= 8,
                 modes=[m for m in args.solve_modes.split(",") if m] or None,
-                budget_s=args.solve_budget or None)
+                budget_s=args.solve_budget or None, factorization_reuse=args.solve_reuse)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:

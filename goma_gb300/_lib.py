@@ -19,7 +19,8 @@ class NewtonOpts(ctypes.Structure):
                 ("max_linear_its", ctypes.c_int), ("linear_tol", ctypes.c_double),
                 ("linear_precision", ctypes.c_int), ("inner_tol", ctypes.c_double),
                 ("max_refinements", ctypes.c_int), ("verbose", ctypes.c_int),
-                ("forcing", ctypes.c_int), ("forcing_max", ctypes.c_double)]
+                ("forcing", ctypes.c_int), ("forcing_max", ctypes.c_double),
+                ("factorization_reuse", ctypes.c_int)]
 
 
 class NewtonStats(ctypes.Structure):
@@ -28,7 +29,8 @@ class NewtonStats(ctypes.Structure):
                 ("refinements", ctypes.c_int), ("residual_l2", ctypes.c_double * 64),
                 ("residual_loo", ctypes.c_double), ("assemble_ms", ctypes.c_double),
                 ("scale_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
-                ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+                ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("factorizations", ctypes.c_int)]
 
 
 MLP_NOALLOC_MAX_ACT = 1 << 20  # GB_MLP_NOALLOC_MAX_ACT of include/gb_newton.h
@@ -71,6 +73,7 @@ def load():
         "gb_stream": (vp, [vp]),
         "gb_csr_to_msr_host": (ctypes.c_int, [vp, vp, dp]),
         "gb_newton_opts_default": (None, [ctypes.POINTER(NewtonOpts)]),
+        "gb_abi_struct_size": (ctypes.c_longlong, [ctypes.c_int]),
         "gb_solve_nonlinear_problem": (ctypes.c_int, [vp, dp, ctypes.POINTER(NewtonOpts), ip,
                                                       ctypes.POINTER(NewtonStats)]),
         "gb_solve_nonlinear_problem_device": (ctypes.c_int, [vp, vp, ctypes.POINTER(NewtonOpts),

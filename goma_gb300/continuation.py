@@ -238,7 +238,8 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
     if not conv:
         raise RuntimeError("first continuation step did not converge")
     records = [{"lam": float(lams[0]), "guess": "initial", "newton_its": st["newton_its"],
-                "linear_its": st["linear_its"], "guess_residual": None,
+                "linear_its": st["linear_its"], "factorizations": st["factorizations"],
+                "guess_residual": None,
                 "wall_s": time.perf_counter() - t0,
                 "newton_ms": {k2: st[k2] for k2 in ("assemble_ms", "scale_ms", "factor_ms",
                                                     "solve_ms", "total_ms")}}]
@@ -312,7 +313,8 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
             train_s = time.perf_counter() - tt
         wall = time.perf_counter() - t0
         records.append({"lam": float(lam), "guess": choice, "newton_its": st["newton_its"],
-                        "linear_its": st["linear_its"], "guess_residual": res.get(choice),
+                        "linear_its": st["linear_its"], "factorizations": st["factorizations"],
+                        "guess_residual": res.get(choice),
                         "candidates": res, "halvings": halvings, "wall_s": wall,
                         "predictor_s": pred_s, "candidates_s": cand_s, "residuals_s": res_s,
                         "train_s": train_s,

@@ -80,6 +80,13 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
   cudaEventRecord(ev[0], s);
   int rc = 0;
   const int maxit = o.max_newton > 0 ? o.max_newton : 20;
+  const int reuse = o.factorization_reuse;
+  if (reuse < GB_FACTOR_CALC || reuse > GB_FACTOR_REUSE) {
+    cudaFree(d_dx);
+    for (auto &e : ev) cudaEventDestroy(e);
+    return fail("unknown factorization_reuse");
+  }
+  bool factored = false;  // in this call
   for (int it = 0; it < maxit; it++) {
     cudaEventRecord(ev[1], s);
     if (C->assemble(d_x, C->d_R, C->d_vals, s)) {
@@ -128,9 +135,17 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
       lo.tol = eta;
       prev_norm = n3[0];
     }
-    if (S.factor(C->d_vals, lo.fp32_inner, s)) {
+    // the preconditioner: new factors, or the last ones (factorization_reuse)
+    const bool refactor = reuse == GB_FACTOR_CALC || !S.has_factors(lo.fp32_inner) ||
+                          (reuse == GB_FACTOR_PER_SOLVE && !factored);
+    if (refactor ? S.factor(C->d_vals, lo.fp32_inner, s)
+                 : S.refresh(C->d_vals, lo.fp32_inner, s)) {
       rc = -1;
       break;
+    }
+    if (refactor) {
+      factored = true;
+      S_.factorizations++;
     }
     cudaEventRecord(ev[4], s);
     LinearStats ls;
@@ -181,6 +196,17 @@ void gb_newton_opts_default(gb_newton_opts *o) {
   o->max_refinements = 20;
   o->forcing = 0;
   o->forcing_max = 1e-2;
+  o->factorization_reuse = GB_FACTOR_CALC;
+}
+
+long long gb_abi_struct_size(int which) {
+  switch (which) {
+    case 0: return (long long)sizeof(gb_newton_opts);
+    case 1: return (long long)sizeof(gb_newton_stats);
+    case 2: return (long long)sizeof(gb_problem_desc);
+    case 3: return (long long)sizeof(gb_material);
+    default: return 0;
+  }
 }
 
 int gb_solve_nonlinear_problem_device(gb_ctx *ctx, double *d_x, const gb_newton_opts *opts,

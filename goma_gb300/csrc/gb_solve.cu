@@ -1133,9 +1133,21 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
     if (!prec32 && use_level_graph())
       GB_CU(capture_prec<float>(this, d_lu32, ordering ? d_tp32 : d_t32, st, &prec32),
             "ILU32 graph");
+    have_lu32 = true;
   } else {
     if (!prec64 && use_level_graph())
       GB_CU(capture_prec<double>(this, d_lu, ordering ? d_tp : d_t, st, &prec64), "ILU graph");
+    have_lu64 = true;
+  }
+  return 0;
+}
+
+int Solver::refresh(const double *vals, bool fp32, cudaStream_t st) {
+  if (!has_factors(fp32)) return fail("no ILU(0) factors to reuse");
+  d_A = vals;
+  if (fp32) {
+    to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
+    GB_CU(cudaGetLastError(), "FP32 matrix copy");
   }
   return 0;
 }

@@ -88,7 +88,13 @@ struct Solver {
   static constexpr int kMaxGraphLevels = 64;  // automatic mode: graph up to this depth
   ~Solver();
   int init(Context *c, int krylov);
+  // ILU(0) factors of the scaled matrix vals (FP64, or FP32 with the FP32
+  // matrix copy); refresh() only points the solve at a new matrix (and
+  // refreshes the FP32 copy), keeping the last factors as preconditioner
   int factor(const double *vals, bool fp32, cudaStream_t st);
+  int refresh(const double *vals, bool fp32, cudaStream_t st);
+  bool has_factors(bool fp32) const { return fp32 ? have_lu32 : have_lu64; }
+  bool have_lu64 = false, have_lu32 = false;
   // the last factors (CSR order, FP64 or FP32 ones widened) to host memory
   int copy_factors(double *host, bool fp32, cudaStream_t st);
   int apply_prec64(cudaStream_t st);  // in place on d_t

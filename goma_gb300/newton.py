@@ -221,4 +221,4 @@ def _stats_dict(st):
             "residual_l2": [st.residual_l2[i] for i in range(min(n + 1, 64))],
             "residual_loo": st.residual_loo, "assemble_ms": st.assemble_ms,
             "scale_ms": st.scale_ms, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
-            "total_ms": st.total_ms}
+            "total_ms": st.total_ms, "factorizations": st.factorizations}

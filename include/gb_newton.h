@@ -156,6 +156,19 @@ int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
 #define GB_LINEAR_FP64 0
 #define GB_LINEAR_FP32_REFINED 1
 
+/* ILU(0) factorisation reuse, the reference's "Matrix Factorization Reuse"
+ * card (src/mm_sol_nonlinear.c:1688-1709, src/sl_util.c:721-734):
+ * CALC factors at every Newton step ("calc", the default; "recalc" does the
+ * same numeric work here, the pattern being fixed); PER_SOLVE factors at
+ * the first Newton step of each gb_solve_nonlinear_problem call and reuses
+ * those factors for its later steps; REUSE keeps the last factors of this
+ * context across calls ("reuse", AztecOO's AZ_reuse) and factors only when
+ * there are none for the precision in use.  The matrix of every linear
+ * solve is always the current one; only the preconditioner lags. */
+#define GB_FACTOR_CALC 0
+#define GB_FACTOR_PER_SOLVE 1
+#define GB_FACTOR_REUSE 2
+
 /* Solver cards of the input deck (src/mm_input.c rd_solver_specs). */
 typedef struct gb_newton_opts {
   int max_newton;          /* "Number of Newton Iterations" */
@@ -175,6 +188,7 @@ typedef struct gb_newton_opts {
    * solution is decided by residual_tol either way. */
   int forcing;
   double forcing_max;
+  int factorization_reuse; /* GB_FACTOR_CALC, _PER_SOLVE or _REUSE */
 } gb_newton_opts;
 
 typedef struct gb_newton_stats {
@@ -184,7 +198,13 @@ typedef struct gb_newton_stats {
   double residual_l2[64];  /* scaled-residual L2 norm per Newton step */
   double residual_loo;     /* final scaled-residual L-infinity norm */
   double assemble_ms, scale_ms, factor_ms, solve_ms, total_ms;
+  int factorizations;      /* ILU(0) factorisations done, all steps */
 } gb_newton_stats;
+
+/* sizeof of the ABI structs, for bindings that mirror them: 0
+ * gb_newton_opts, 1 gb_newton_stats, 2 gb_problem_desc, 3 gb_material;
+ * 0 for any other value.  Needs no device. */
+long long gb_abi_struct_size(int which);
 
 void gb_newton_opts_default(gb_newton_opts *o);
 

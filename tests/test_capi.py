@@ -69,3 +69,20 @@ def test_newton_options_fill_the_abi_struct(lib):
     assert d.linear_precision == 0 and d.max_newton > 0
     with pytest.raises(TypeError, match="krylov"):
         GomaNewton.newton_opts(host, krylov=30)
+
+
+def test_abi_struct_mirrors_match_the_library(lib):
+    """The ctypes mirrors of the ABI structs have the library's sizes, and
+    the Newton options' defaults land in the right fields."""
+    import ctypes
+
+    from goma_gb300 import problem as pb
+    assert lib.gb_abi_struct_size(0) == ctypes.sizeof(_lib.NewtonOpts)
+    assert lib.gb_abi_struct_size(1) == ctypes.sizeof(_lib.NewtonStats)
+    assert lib.gb_abi_struct_size(2) == ctypes.sizeof(pb.CProblemDesc)
+    assert lib.gb_abi_struct_size(3) == ctypes.sizeof(pb.CMaterial)
+    assert lib.gb_abi_struct_size(99) == 0
+    o = _lib.NewtonOpts()
+    lib.gb_newton_opts_default(ctypes.byref(o))
+    assert (o.max_newton, o.krylov_dim, o.max_refinements, o.forcing) == (20, 30, 20, 0)
+    assert (o.inner_tol, o.forcing_max, o.factorization_reuse) == (1e-3, 1e-2, 0)

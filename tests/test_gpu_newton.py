@@ -146,3 +146,34 @@ def test_gpu_krylov_counts_match_oracle_gmres():
     assert abs(st["newton_its"] - ito) <= 1
     assert abs(st["linear_its"] - lino) <= max(3, 0.1 * lino)
     assert np.abs(x - xo).max() <= TOL_X * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
+def test_gpu_factorization_reuse(fp32):
+    """The reference's "Matrix Factorization Reuse" choices: CALC factors at
+    every Newton step, REUSE keeps the last factors across calls (here a
+    continuation-like call at a nearby Rayleigh number factors nothing),
+    PER_SOLVE factors once per call.  Every mode converges to the fields of
+    the CALC solve."""
+    def solve(ra, x0, reuse, gn=None):
+        if gn is None:
+            gn = GomaNewton(pb.boussinesq_cube_3d(3, ra, 0.71))
+        x, conv, st = gn.solve_nonlinear_problem(
+            x0, residual_tol=1e-10, linear_tol=1e-9, krylov_dim=60, max_newton=30,
+            max_linear_its=4000, fp32_inner=fp32, factorization_reuse=reuse)
+        assert conv, (ra, reuse, st)
+        return gn, x, st
+
+    gn, xc, st = solve(1e4, None, 0)
+    assert st["factorizations"] == st["newton_its"] > 0
+    # the next parameter value with the last factors of the converged solve
+    m = gn.problem.material
+    m.momentum_source = (0.0, 0.0, -1.2e4 * 0.71)
+    gn.set_material(m)
+    _, xr, st = solve(1.2e4, xc, 2, gn)
+    assert st["factorizations"] == 0 and st["newton_its"] > 0
+    _, xref, _ = solve(1.2e4, xc, 0)
+    assert np.abs(xr - xref).max() <= TOL_X * np.abs(xref).max()
+    _, xp, st = solve(1e4, None, 1)
+    assert st["factorizations"] == 1
+    assert np.abs(xp - xc).max() <= TOL_X * np.abs(xc).max()
