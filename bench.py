@@ -488,6 +488,39 @@ def cpu_time_to_solve(nel=8, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, krylov=30, l
     return out
 
 
+def factorization_reuse_solves(nel=16, ra=1e4, tol=1e-10, fp32=False):
+    """One Newton solve of the Boussinesq cube from rest (Ra `ra`, GMRES(60),
+    forcing rule, the reference's node order) with each factorisation reuse
+    mode (0 every Newton step, 1 once per solve, 2 across solves, after a
+    first solve): wall time, Newton and Krylov counts and factorisations."""
+    import time as _time
+
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    rows = []
+    gn = GomaNewton(pb.boussinesq_cube_3d(nel, ra, PR))
+    gn.set_ilu_ordering(0)
+    for reuse in (0, 1, 2):
+        torch.cuda.synchronize()
+        t = _time.perf_counter()
+        x, conv, st = gn.solve_nonlinear_problem(
+            residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
+            krylov_dim=60, forcing=1, forcing_max=1e-2, fp32_inner=fp32,
+            factorization_reuse=reuse)
+        torch.cuda.synchronize()
+        rows.append({"factorization_reuse": reuse, "converged": conv,
+                     "seconds": _time.perf_counter() - t, "newton_its": st["newton_its"],
+                     "linear_its": st["linear_its"], "factorizations": st["factorizations"],
+                     "factor_seconds": st["factor_ms"] * 1e-3,
+                     "solve_seconds": st["solve_ms"] * 1e-3})
+        print("reuse:", rows[-1], file=sys.stderr, flush=True)
+    gn.close()
+    return {"workload": "%d^3 Boussinesq cube Newton solve from rest, Ra %g, GMRES(60), "
+                        "forcing rule, %s" % (nel, ra, "FP32 inner" if fp32 else "FP64"),
+            "runs": rows}
+
+
 def ilu_orders(sizes=(8, 16, 24), ra=1e4, tol=1e-10):
     """One Newton solve of the Boussinesq cube from rest (Ra `ra`, scaled
     |R| < tol, GMRES(60), forcing rule) per cube size, ILU(0) node order
@@ -824,6 +857,8 @@ def main():
                 extra[w] = bfs_continuation()
             elif w == "ilu_orders":
                 extra[w] = ilu_orders()
+            elif w == "reuse":
+                extra[w] = factorization_reuse_solves(16)
             elif w == "cpu_solve":
                 extra[w] = cpu_time_to_solve(8)
         line["workloads"] = extra
