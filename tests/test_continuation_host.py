@@ -95,8 +95,10 @@ def test_a_failed_step_is_halved_and_the_sweep_goes_on():
 def test_too_many_halvings_raise():
     gn = CubicNewton()
     gn.reach = 1e-6
-    with pytest.raises(RuntimeError, match="did not converge"):
-        continuation(gn, 0.5, 4.0, 1, predictor="zeroth", set_param=set_lam, max_halvings=2)
+    with pytest.raises(RuntimeError, match="continuation step at lambda"):
+        continuation(gn, 0.5, 4.0, 1, predictor="zeroth", x0=gn.exact(0.5), set_param=set_lam,
+                     max_halvings=2)
+    assert len(gn.guess_errors) == 1 + 3  # the start, the step and its two halvings
 
 
 def test_time_budget_and_bad_predictor():
