@@ -145,6 +145,12 @@ class GomaNewton:
         return its.value, rr.value
 
     # --- solve_nonlinear_problem
+    def write_exodus(self, path, solutions, times=None, title="goma_gb300 solution"):
+        """Exodus II results file of host solution vectors of this problem
+        (the reference's variable names; goma_gb300.exodus)."""
+        from .exodus import write_exodus
+        write_exodus(path, self.problem, solutions, times, title)
+
     def newton_opts(self, **kw):
         """gb_newton_opts with the defaults of gb_newton_opts_default and the
         given fields (fp32_inner sets linear_precision); an unknown name is an
