@@ -140,12 +140,14 @@ def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
 
 def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=60,
                   forcing=1, reference_solver=True, modes=None, budget_s=None,
-                  factorization_reuse=0):
+                  factorization_reuse=0, max_linear_its=4000):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
     reference's ALC_ZEROTH) against the learned predictor (secant fallback)
-    with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement.  All use the same
+    with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement; the
+    secant_fp32 run is the learned_fp32 run without the network (the plain
+    secant guess), so the two isolate what the network gains.  All use the same
     linear-solver settings: ILU(0), GMRES(krylov), Eisenstat-Walker forcing
     (the converged solution does not depend on them).  ilu_ordering -1
     chooses the node order by size: the multicoloured one up to 12^3 (few
@@ -196,14 +198,16 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
         gn = GomaNewton(prob)
         refs = mode == "plain_fp64_reference_solver"
         gn.set_ilu_ordering(0 if refs else ilu_ordering)
-        opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30, max_linear_its=4000,
-                    fp32_inner=(mode == "learned_fp32"), inner_tol=1e-3,
+        opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30,
+                    max_linear_its=max_linear_its,
+                    fp32_inner=mode.endswith("_fp32"), inner_tol=1e-3,
                     krylov_dim=30 if refs else krylov, forcing=0 if refs else forcing,
                     forcing_max=1e-2, factorization_reuse=0 if refs else factorization_reuse)
         torch.cuda.synchronize()
         t = time.perf_counter()
         recs, x = continuation(gn, ra0, ra1, nsteps,
-                               predictor="learned" if mode.startswith("learned") else "zeroth",
+                               predictor={"plain": "zeroth", "secant": "secant",
+                                          "learned": "learned"}[mode.split("_")[0]],
                                set_param=set_ra, newton_opts=opts, spacing="log",
                                learned_opts=dict(steps=300, batch=4096, lr=2e-3),
                                time_budget_s=budget_s)
@@ -229,6 +233,11 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
         if m != "plain_fp64" and a is not None and {m, "plain_fp64"} <= complete:
             out["solution_rel_diff_" + m] = float(np.abs(a - sols[m]).max() / np.abs(a).max())
             out["speedup_" + m] = out["plain_fp64"]["seconds"] / out[m]["seconds"]
+    # the network's own gain: the same FP32-inner solve with the plain secant
+    # guess in its place
+    if {"secant_fp32", "learned_fp32"} <= complete:
+        out["learned_over_secant_seconds"] = (out["learned_fp32"]["seconds"] /
+                                              out["secant_fp32"]["seconds"])
     if "speedup_learned_fp32" in out:
         out["speedup"] = out["speedup_learned_fp32"]
         out["solution_rel_diff"] = out["solution_rel_diff_learned_fp32"]
@@ -651,10 +660,13 @@ def main():
                          "1 multicoloured, -1 by size (multicoloured up to 12^3)")
     ap.add_argument("--solve-modes", default="",
                     help="comma-separated runs of the time-to-solve leg: plain_fp64, "
-                         "learned_fp64, learned_fp32, plain_fp64_reference_solver "
+                         "learned_fp64, learned_fp32, secant_fp32, secant_fp64, "
+                         "plain_fp64_reference_solver "
                          "(default: all)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
                     help="seconds per run of the time-to-solve leg (0: no limit)")
+    ap.add_argument("--solve-max-linear", type=int, default=4000,
+                    help="Krylov iteration limit of one linear solve in the time-to-solve leg")
     ap.add_argument("--solve-reuse", type=int, default=0,
                     help="ILU(0) factorisation reuse of the time-to-solve leg: 0 every Newton "
                          "step, 1 once per Newton solve, 2 across solves")
@@ -835,7 +847,8 @@ def main():
             line["time_to_solve"] = time_to_solve(
                 args.solve_nel, ilu_ordering=args.solve_ilu, reference_solver=args.solve_nel <= 8,
                 modes=[m for m in args.solve_modes.split(",") if m] or None,
-                budget_s=args.solve_budget or None, factorization_reuse=args.solve_reuse)
+                budget_s=args.solve_budget or None, factorization_reuse=args.solve_reuse,
+                max_linear_its=args.solve_max_linear)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:
