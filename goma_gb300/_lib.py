@@ -91,7 +91,7 @@ def load():
         "gb_mlp_set_params": (ctypes.c_int, [vp, fp]),
         "gb_mlp_get_grads": (ctypes.c_int, [vp, fp]),
         "gb_mlp_forward_device": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
-        "gb_mlp_forward_noalloc": (ctypes.c_int, [vp, vp, ctypes.c_int, vp]),
+        "gb_mlp_forward_noalloc": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, vp]),
         "gb_mlp_loss_grad_device": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, fp]),
         "gb_mlp_adam_step": (ctypes.c_int, [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_float]),

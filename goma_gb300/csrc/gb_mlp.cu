@@ -259,7 +259,10 @@ struct Mlp {
   float *d_split = nullptr;          // weight-gradient partial sums [kMaxSplit][maxw][maxw]
   int *d_idx = nullptr;
   int adam_t = 0;
+  int dev = 0;                       // the device the network lives on
   cudaStream_t st = nullptr;
+  // orders a caller's stream after the network's own stream and back
+  cudaEvent_t ev_own = nullptr, ev_caller = nullptr;
   ~Mlp() {
     cudaFree(d_w);
     cudaFree(d_g);
@@ -275,6 +278,8 @@ struct Mlp {
     cudaFree(d_idx);
     cudaFree(d_split);
     if (h_part) cudaFreeHost(h_part);
+    if (ev_own) cudaEventDestroy(ev_own);
+    if (ev_caller) cudaEventDestroy(ev_caller);
     if (st) cudaStreamDestroy(st);
   }
   int maxw() const {
@@ -411,7 +416,10 @@ int gb_mlp_create(int n_in, int width, int hidden_layers, int n_out, unsigned lo
     const double a = std::sqrt(6.0 / (fi + fo));
     for (int i = 0; i < fi * fo; i++) w[M.woff[l] + i] = (float)((2.0 * next() - 1.0) * a);
   }
-  cudaError_t e = cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking);
+  cudaError_t e = cudaGetDevice(&M.dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&M.ev_own, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&M.ev_caller, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&M.d_w, sizeof(float) * off);
   if (e == cudaSuccess) e = cudaMalloc(&M.d_g, sizeof(float) * off);
   if (e == cudaSuccess) e = cudaMalloc(&M.d_m, sizeof(float) * off);
@@ -574,10 +582,23 @@ static int noalloc_scratch(float **out) {
 
 }  // namespace gb
 
-extern "C" int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y) {
+extern "C" int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y,
+                                      void *stream) {
   if (!m || !d_x || !d_y) return gb::fail("NULL argument");
   if (B <= 0) return gb::fail("batch size must be positive");
   gb::Mlp &M = m->m;
+  {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return gb::cuda_fail(e, "cudaGetDevice");
+    if (dev != M.dev) {
+      char msg[160];
+      snprintf(msg, sizeof msg,
+               "current device %d is not the network's device %d; make device %d current", dev,
+               M.dev, M.dev);
+      return gb::fail(msg);
+    }
+  }
   int widest = 0;
   for (int l = 1; l + 1 < (int)M.width.size(); l++) widest = M.width[l] > widest ? M.width[l] : widest;
   if ((long long)B * widest > (long long)GB_MLP_NOALLOC_MAX_ACT) {
@@ -591,17 +612,24 @@ extern "C" int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float 
   float *base = nullptr;
   if (gb::noalloc_scratch(&base)) return -1;
   float *buf[2] = {base, base + (size_t)GB_MLP_NOALLOC_MAX_ACT};
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  // after the network's own queued work (training, parameter updates) ...
+  cudaError_t e = cudaEventRecord(M.ev_own, M.st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, M.ev_own, 0);
+  if (e != cudaSuccess) return gb::cuda_fail(e, "MLP forward (no allocation): ordering");
   const float *in = d_x;
   const int L = M.layers();
   for (int l = 0; l < L; l++) {
     const int K = M.width[l], N = M.width[l + 1];
     float *out = l + 1 == L ? d_y : buf[l & 1];
     dim3 grid((N + gb::TN - 1) / gb::TN, (B + gb::TM - 1) / gb::TM);
-    gb::gemm_xwT_kernel<<<grid, 256, 0, M.st>>>(B, N, K, in, M.d_w + M.woff[l], M.d_w + M.boff[l],
-                                                out, l + 1 < L ? 1 : 0);
+    gb::gemm_xwT_kernel<<<grid, 256, 0, cs>>>(B, N, K, in, M.d_w + M.woff[l], M.d_w + M.boff[l],
+                                              out, l + 1 < L ? 1 : 0);
     in = out;
   }
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaStreamSynchronize(M.st);
+  e = cudaGetLastError();
+  // ... and the network's later work after this pass
+  if (e == cudaSuccess) e = cudaEventRecord(M.ev_caller, cs);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(M.st, M.ev_caller, 0);
   return e == cudaSuccess ? 0 : gb::cuda_fail(e, "MLP forward (no allocation)");
 }

@@ -47,22 +47,37 @@ class GpuMLP:
         _lib.check(self._L.gb_mlp_get_grads(self.h, _fp(g)))
         return g
 
-    # device tensors (torch) in, device tensors out
+    # device tensors (torch) in, device tensors out.  The library's network
+    # entry points run on the network's own stream, which does not wait for
+    # torch's: the current stream is synchronised first so that the inputs
+    # are complete on the device.
+    @staticmethod
+    def _inputs_ready(t):
+        import torch
+        torch.cuda.current_stream(t.device).synchronize()
+
     def forward(self, x):
         import torch
         x = x.contiguous().float()
         y = torch.empty((x.shape[0], self.widths[-1]), dtype=torch.float32, device=x.device)
+        self._inputs_ready(x)
         _lib.check(self._L.gb_mlp_forward_device(self.h, x.data_ptr(), x.shape[0], y.data_ptr()))
         return y
 
-    def forward_noalloc(self, x, y):
+    def forward_noalloc(self, x, y, stream=None):
         """Forward pass into the caller's y without any device allocation
         (gb_mlp_forward_noalloc): x [B, n_in] and y [B, n_out] are FP32 device
-        tensors the caller owns; B x hidden width <= MLP_NOALLOC_MAX_ACT."""
-        _lib.check(self._L.gb_mlp_forward_noalloc(self.h, x.data_ptr(), x.shape[0], y.data_ptr()))
+        tensors the caller owns; B x hidden width <= MLP_NOALLOC_MAX_ACT.  The
+        pass is queued on `stream` (a torch.cuda.Stream; default: torch's
+        current stream) in order with the work already queued there."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(x.device)
+        _lib.check(self._L.gb_mlp_forward_noalloc(self.h, x.data_ptr(), x.shape[0], y.data_ptr(),
+                                                  ctypes.c_void_p(s.cuda_stream)))
         return y
 
     def loss_grad(self, x, t, mask):
+        self._inputs_ready(x)
         loss = ctypes.c_float()
         _lib.check(self._L.gb_mlp_loss_grad_device(self.h, x.data_ptr(), t.data_ptr(),
                                                    mask.data_ptr(), x.shape[0],
@@ -73,6 +88,7 @@ class GpuMLP:
         _lib.check(self._L.gb_mlp_adam_step(self.h, lr, b1, b2, eps))
 
     def train(self, x, t, mask, steps, batch=4096, lr=1e-3, seed=0):
+        self._inputs_ready(x)
         loss = ctypes.c_float()
         _lib.check(self._L.gb_mlp_train_device(self.h, x.data_ptr(), t.data_ptr(), mask.data_ptr(),
                                                x.shape[0], steps, batch, lr, seed,

@@ -264,6 +264,11 @@ int gb_mlp_num_params(const gb_mlp *m);
 int gb_mlp_get_params(const gb_mlp *m, float *host);
 int gb_mlp_set_params(gb_mlp *m, const float *host);
 int gb_mlp_get_grads(const gb_mlp *m, float *host);
+/* The network's device entry points below (forward, loss and gradients,
+ * training) run on the network's own stream and return once their work is
+ * done.  That stream does not wait for the caller's streams: the device
+ * arrays passed in must be complete on the device before the call (for
+ * example, synchronise the stream that wrote them). */
 /* y[B][n_out] = net(x[B][n_in]); device arrays */
 int gb_mlp_forward_device(gb_mlp *m, const float *d_x, int B, float *d_y);
 /* loss = sum mask (net(x) - t)^2 / sum mask, gradients kept inside (read
@@ -281,14 +286,24 @@ int gb_mlp_adam_step(gb_mlp *m, float lr, float beta1, float beta2, float eps);
  * array compiled into the library: two buffers of GB_MLP_NOALLOC_MAX_ACT
  * floats, so B times the hidden width may not exceed GB_MLP_NOALLOC_MAX_ACT
  * (larger batches are rejected with an error; split them).  Every GPU that
- * loads the library holds that 8 MB until the process exits.  The first call
+ * loads the library holds that 8 MB until the process exits.
+ *
+ * The pass is queued on `stream` (a cudaStream_t; NULL is CUDA's default
+ * stream) and the call returns without waiting for it: x is read, and y
+ * written, in that stream's order, so work the caller queued on `stream`
+ * before the call is seen and work queued after it sees y.  The pass also
+ * waits for the network's own queued work (training, parameter updates),
+ * and the network's later work waits for the pass.  The network's device
+ * must be current; another device is refused with an error.  The first call
  * on a device looks the array's device address up (once per device); make
- * that first call before any stream capture.  All calls share the array,
- * so calls that overlap on the GPU (other threads, other streams) race; it
- * keeps the last call's activations, and nothing in it needs to start at
- * zero because every activation is written before it is read. */
+ * that first call before any stream capture.  The address is kept for the
+ * life of the process: after cudaDeviceReset this entry point may no longer
+ * be called.  All calls share the array, so calls that overlap on the GPU
+ * (other threads, other streams) race; it keeps the last call's
+ * activations, and nothing in it needs to start at zero because every
+ * activation is written before it is read. */
 #define GB_MLP_NOALLOC_MAX_ACT (1 << 20)
-int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y);
+int gb_mlp_forward_noalloc(gb_mlp *m, const float *d_x, int B, float *d_y, void *stream);
 /* steps Adam steps on minibatches of `batch` points drawn from n_points
  * (fixed integer-hash sampling from seed) */
 int gb_mlp_train_device(gb_mlp *m, const float *d_x, const float *d_t, const float *d_mask,
