@@ -15,8 +15,9 @@ scatter, at a seeded synthetic state.
          GPU's FP64 throughput measured in-process (scalar FMA and mma.sync
          f64 run at the same rate); the dense-equivalent rate and the HBM
          view of the same launch alongside
-  cpu_baseline  the CPU oracle (a restatement of the reference's
-         matrix_fill) on an 8^3-element block of the same problem
+  cpu_baseline  the CPU oracle (the golden-pinned restatement of the
+         reference's matrix_fill_full) assembling the same 32^3 workload on
+         all host threads
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -101,41 +102,53 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def cpu_baseline(nel_block=8, threads=1, budget_s=20.0):
-    """The CPU oracle's matrix_fill on an nel_block^3 block of the same
-    problem; elements/s over `threads` threads (disjoint element ranges,
-    private output arrays)."""
-    import concurrent.futures
+class CpuAssembly:
+    """The reference's CPU assembly of the whole nel^3 workload, timed: the
+    CPU oracle (the golden-pinned restatement of the reference's
+    matrix_fill_full, not Goma itself) over `threads` host threads, each
+    step the caller's zeroing of R and the 2.5 GB of MSR values and all
+    nel^3 elements, colour by colour, into one shared MSR array
+    (oracle.ParallelFill)."""
 
-    import oracle
-    from goma_gb300 import problem as pb
-    prob = pb.boussinesq_cube_3d(nel_block, RA, PR)
-    o = oracle.Oracle(prob)
-    x = np.random.default_rng(7).uniform(-1, 1, o.N)
-    ne = prob.mesh.num_elems
-    # time one element first to size the sample to the budget
-    t = time.perf_counter()
-    o.matrix_fill(x, True, 0, 1)
-    per = max(time.perf_counter() - t, 1e-6)
-    n = int(min(ne, max(threads, budget_s / per)))
-    chunks = np.array_split(np.arange(n), threads)
+    def __init__(self, nel, threads):
+        import oracle
+        from goma_gb300 import problem as pb
+        t = time.perf_counter()
+        self.nel = nel
+        self.o = oracle.Oracle(pb.boussinesq_cube_3d(nel, RA, PR))
+        self.fill = oracle.ParallelFill(self.o, threads)
+        self.x = self.o.dirichlet_init(np.random.default_rng(11).uniform(-1.0, 1.0, self.o.N))
+        self.setup_s = time.perf_counter() - t
 
-    def work(c):
-        R = np.zeros(o.N)
-        a = np.zeros(o.msr_len)
-        lib = oracle.lib()
-        P = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
-        lib.orc_matrix_fill(o.h, P(x), P(R), P(a), int(c[0]), int(c[-1]) + 1)
-        return len(c)
+    def step(self):
+        t = time.perf_counter()
+        if self.fill(self.x) != 0:
+            raise RuntimeError("CPU assembly: non-positive Jacobian determinant")
+        return time.perf_counter() - t
 
-    t = time.perf_counter()
-    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
-        done = sum(ex.map(work, [c for c in chunks if len(c)]))
-    dt = time.perf_counter() - t
-    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "CPU oracle matrix_fill (restatement of the reference's), %d elements of an "
-                      "%d^3-element block of the same HEX27 Boussinesq problem, %.1f s"
-                      % (done, nel_block, dt)}
+    def describe(self, steps, dt):
+        return ("CPU oracle matrix_fill_full (golden-pinned restatement of the reference's, "
+                "not Goma itself) over the whole %d^3 HEX27 Boussinesq workload (%d elements, "
+                "zeroing of R and the MSR values included), %d colours, element chunks over %d "
+                "host threads into one MSR array; %d step(s), %.2f s each"
+                % (self.nel, self.nel ** 3, self.fill.num_colors, self.fill.threads, steps, dt))
+
+    def close(self):
+        self.fill.close()
+
+
+def cpu_baseline(nel=NEL, threads=None, steps=1):
+    """The reference's CPU assembly of the same workload on the host cores:
+    one untimed pass (pages the arrays in), then `steps` timed passes."""
+    threads = threads or os.cpu_count() or 1
+    ca = CpuAssembly(nel, threads)
+    ca.step()
+    dts = [ca.step() for _ in range(steps)]
+    dt = float(np.median(dts))
+    out = {"value": nel ** 3 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": ca.describe(steps, dt), "setup_s": ca.setup_s}
+    ca.close()
+    return out
 
 
 def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=60,
@@ -615,26 +628,32 @@ def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path.  The reference C compiles
-    only where its source tree is (oracle/_ref, not on the GPU machine), so
-    the oracle port stands in, on all host threads."""
+    """--impl reference: the reference's CPU assembly of the workload on all
+    host threads.  The reference C compiles only where its source tree is
+    (oracle/_ref, not on the GPU machine), so the golden-pinned oracle port
+    stands in.  Every step is one full nel^3 assembly (zeroing included);
+    W untimed steps, then K timed ones; ms_per_step is their mean."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(max(args.warmup, 0)):
-        cpu_baseline(8, threads, budget_s=2.0)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(8, threads, budget_s=max(60.0 / max(args.steps, 1), 5.0)))
-    v = float(np.median([c["value"] for c in vals]))
-    cb = dict(vals[-1])
-    cb["value"] = v
+    ca = CpuAssembly(args.nel, threads)
+    for _ in range(max(args.warmup, 1)):
+        ca.step()
+    t = time.perf_counter()
+    dts = [ca.step() for _ in range(args.steps)]
+    total = time.perf_counter() - t
+    ms = 1e3 * total / max(args.steps, 1)
+    v = args.nel ** 3 / (ms * 1e-3)
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": ca.describe(args.steps, ms * 1e-3),
+          "step_seconds": {"min": min(dts), "max": max(dts)}, "setup_s": ca.setup_s}
+    ca.close()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * NEL ** 3 / v, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(NEL), "cpu_baseline": cb,
+            "config": workload_config(args.nel), "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -838,7 +857,7 @@ def main():
             "clocks": clk.summary(), "e2e": e2e, "roofline": roofline,
             "gpu_launches": int(gn.num_colors * args.steps)}
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(8, 1, budget_s=15.0)
+        line["cpu_baseline"] = cpu_baseline(nel)
     if rank == 0 and args.solve_nel > 0:
         del dv, dx, dR, xh, Rh, ah
         gn.close()

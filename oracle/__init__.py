@@ -48,6 +48,8 @@ def lib():
         L.orc_dirichlet_mask.argtypes = [vp, ip]
         L.orc_dirichlet_init.argtypes = [vp, dp]
         L.orc_matrix_fill.argtypes = [vp, dp, dp, dp, ctypes.c_int, ctypes.c_int]
+        L.orc_matrix_fill_list.argtypes = [vp, dp, dp, dp, ip, ctypes.c_int]
+        L.orc_element_colors.argtypes = [vp, ip]
         L.orc_element.argtypes = [vp, ctypes.c_int, dp, dp, dp, ctypes.c_int]
         L.orc_local_size.argtypes = [vp]
         L.orc_element_dofs.argtypes = [vp, ctypes.c_int, ip]
@@ -178,6 +180,65 @@ class Oracle:
                                     krylov, max_linear_its, tau, ctypes.byref(lin),
                                     _p(norms, ctypes.c_double))
         return x, it, lin.value, norms[:max(it + 1, 0)] if it >= 0 else norms
+
+
+class ParallelFill:
+    """The oracle's matrix_fill_full over many host threads, for timing the
+    reference's CPU assembly of a whole problem: per call, the caller's
+    zeroing of R and of the MSR values (src/mm_sol_nonlinear.c:1114-1120),
+    then the element loop (src/mm_fill.c:158-312) colour by colour.  Each
+    colour's elements (no two share a node, so they touch disjoint rows) are
+    split into `threads` chunks that add into one shared R and one shared
+    MSR array; a colour starts when the previous one is done.  The sums of a
+    row are taken in colour order rather than element order, so results
+    match the serial fill to rounding, not bitwise."""
+
+    def __init__(self, o, threads):
+        import concurrent.futures
+        self.o = o
+        self.threads = max(1, int(threads))
+        color = np.empty(o.num_elems, np.int32)
+        nc = lib().orc_element_colors(o.h, _p(color, ctypes.c_int))
+        if nc < 0:
+            raise RuntimeError("orc_element_colors failed")
+        self.num_colors = nc
+        self.chunks = []
+        for k in range(nc):
+            els = np.flatnonzero(color == k).astype(np.int32)
+            self.chunks.append([np.ascontiguousarray(c) for c in
+                                np.array_split(els, self.threads) if len(c)])
+        self.R = np.zeros(o.N)
+        self.a = np.zeros(o.msr_len)
+        self.pool = concurrent.futures.ThreadPoolExecutor(self.threads)
+
+    def close(self):
+        self.pool.shutdown()
+
+    def _zero(self, arr):
+        n = arr.size
+        bounds = np.linspace(0, n, self.threads + 1).astype(np.int64)
+        base = arr.ctypes.data
+
+        def z(i):
+            ctypes.memset(base + 8 * int(bounds[i]), 0, 8 * int(bounds[i + 1] - bounds[i]))
+
+        list(self.pool.map(z, range(self.threads)))
+
+    def __call__(self, x):
+        """R and the MSR values of the state x (into self.R, self.a);
+        returns 0, or -1 on a non-positive Jacobian determinant."""
+        L = lib()
+        x = np.ascontiguousarray(x, np.float64)
+        self._zero(self.R)
+        self._zero(self.a)
+        xp, Rp, ap = (_p(v, ctypes.c_double) for v in (x, self.R, self.a))
+        status = 0
+        for col in self.chunks:
+            sts = list(self.pool.map(
+                lambda c: L.orc_matrix_fill_list(self.o.h, xp, Rp, ap, _p(c, ctypes.c_int),
+                                                 len(c)), col))
+            status = min([status] + sts)
+        return status
 
 
 def mesh_from_spec(spec):

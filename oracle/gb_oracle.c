@@ -595,13 +595,17 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
 
 /* Scatter of load_lec (src/mm_fill.c:5241): a[diag] / a[off-diag slot]
  * += element entries, elements in order. */
-int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1) {
+/* The element loop of matrix_fill_full (src/mm_fill.c:158-312) over either
+ * the range [e0, e1) (elems == NULL) or the list elems[e0 .. e1). */
+static int fill_elements(const orc_problem *p, const double *x, double *R, double *a,
+                         const int *elems, int e0, int e1) {
   const int nloc = p->nloc;
   double *Re = (double *)malloc(sizeof(double) * (size_t)nloc);
   double *Je = (double *)malloc(sizeof(double) * (size_t)nloc * nloc);
   int g[27 * (4 + GB_MAX_SPECIES) + 4];
   int status = 0;
-  for (int e = e0; e < e1; e++) {
+  for (int k = e0; k < e1; k++) {
+    const int e = elems ? elems[k] : k;
     if (orc_element(p, e, x, Re, Je, 1) != 0) status = -1;
     orc_element_dofs(p, e, g);
     for (int r = 0; r < nloc; r++) {
@@ -637,6 +641,40 @@ int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a,
   free(Re);
   free(Je);
   return status;
+}
+
+int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1) {
+  return fill_elements(p, x, R, a, NULL, e0, e1);
+}
+
+int orc_matrix_fill_list(const orc_problem *p, const double *x, double *R, double *a,
+                         const int *elems, int n) {
+  return fill_elements(p, x, R, a, elems, 0, n);
+}
+
+/* Greedy element colouring: each element takes the smallest colour that no
+ * element sharing one of its nodes has taken yet, in element order. */
+int orc_element_colors(const orc_problem *p, int *color) {
+  const int ne = p->d.num_elems, nn = p->nn;
+  unsigned long long *used =
+      (unsigned long long *)calloc((size_t)p->d.num_nodes, sizeof(unsigned long long));
+  if (!used) return -1;
+  int ncol = 0;
+  for (int e = 0; e < ne; e++) {
+    unsigned long long m = 0;
+    for (int k = 0; k < nn; k++) m |= used[p->conn[(size_t)e * nn + k]];
+    int c = 0;
+    while (c < 64 && (m >> c) & 1ULL) c++;
+    if (c == 64) {
+      free(used);
+      return -1;
+    }
+    color[e] = c;
+    if (c + 1 > ncol) ncol = c + 1;
+    for (int k = 0; k < nn; k++) used[p->conn[(size_t)e * nn + k]] |= 1ULL << c;
+  }
+  free(used);
+  return ncol;
 }
 
 /* row_sum_scale_MSR (src/sl_matrix_util.c:506) */

@@ -41,6 +41,13 @@ void orc_dirichlet_init(const orc_problem *p, double *x);
  * is not NULL, to the MSR values a (length msr_len).  Returns 0, or -1 when
  * an element has a non-positive Jacobian determinant. */
 int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1);
+/* The same over the n elements listed in elems. */
+int orc_matrix_fill_list(const orc_problem *p, const double *x, double *R, double *a,
+                         const int *elems, int n);
+/* Greedy colouring of the elements (no two elements of a colour share a
+ * node, so their contributions touch disjoint rows); returns the number of
+ * colours, or -1. */
+int orc_element_colors(const orc_problem *p, int *color);
 /* Element-level residual and Jacobian (before the Dirichlet rows are
  * applied when apply_bc == 0), in the oracle's local DOF order:
  * velocity component a of local node k at a*nn + k, temperature at
