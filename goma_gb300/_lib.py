@@ -30,7 +30,8 @@ class NewtonStats(ctypes.Structure):
                 ("residual_loo", ctypes.c_double), ("assemble_ms", ctypes.c_double),
                 ("scale_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
                 ("solve_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
-                ("factorizations", ctypes.c_int)]
+                ("factorizations", ctypes.c_int), ("residual_l1", ctypes.c_double * 64),
+                ("residual_loo_steps", ctypes.c_double * 64)]
 
 
 MLP_NOALLOC_MAX_ACT = 1 << 20  # GB_MLP_NOALLOC_MAX_ACT of include/gb_newton.h
@@ -105,6 +106,7 @@ def load():
         "gb_ilu_permutation_host": (ctypes.c_int, [vp, ip, ip, ip, ctypes.POINTER(ctypes.c_longlong),
                                                    ip, ctypes.POINTER(ctypes.c_longlong)]),
         "gb_set_triangular_solve": (ctypes.c_int, [vp, ctypes.c_int]),
+        "gb_set_sweep_fault": (ctypes.c_int, [vp, ctypes.c_longlong, ctypes.c_int]),
         "gb_ilu0_factors": (ctypes.c_int, [vp, dp, ctypes.c_int, dp]),
         "gb_kernel_timing": (ctypes.c_int, [vp, ctypes.c_int, dp, llp]),
         "gb_linear_solve": (ctypes.c_int, [vp, dp, dp, dp, ctypes.POINTER(NewtonOpts), ip, dp]),

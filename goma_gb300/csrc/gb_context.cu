@@ -491,6 +491,13 @@ int gb_set_triangular_solve(gb_ctx *ctx, int mode) {
   return 0;
 }
 
+int gb_set_sweep_fault(gb_ctx *ctx, long long spin_limit, int reverse_lower) {
+  if (!ctx) return fail("NULL argument");
+  ctx->c.sweep_spin_limit = spin_limit > 0 ? spin_limit : 0;
+  ctx->c.sweep_reverse_lower = reverse_lower != 0;
+  return 0;
+}
+
 int gb_set_material(gb_ctx *ctx, const gb_material *mat) {
   if (!ctx || !mat) return fail("NULL argument");
   return ctx->c.set_material(*mat);

@@ -29,6 +29,9 @@ struct Context {
   // ILU triangular solves: 0 sync-free sweeps, 1 level-scheduled graph,
   // 2 automatic (the graph for short level schedules)
   int trsv = 2;
+  // host-injected fault of the sync-free sweeps (gb_set_sweep_fault)
+  long long sweep_spin_limit = 0;  // polls per wait; <= 0: the default
+  int sweep_reverse_lower = 0;
   int ilu_ordering = 0;  // ILU(0) node order: 0 the reference's, 1 multicoloured
   cudaStream_t stream = nullptr;
   double *d_coords = nullptr;

@@ -111,7 +111,11 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
     cudaEventRecord(ev[3], s);
     cudaEventSynchronize(ev[3]);
     S_.scale_ms += elapsed(ev[2], ev[3]);
-    if (it < 64) S_.residual_l2[it] = n3[0];
+    if (it < 64) {
+      S_.residual_l2[it] = n3[0];
+      S_.residual_l1[it] = n3[1];
+      S_.residual_loo_steps[it] = n3[2];
+    }
     S_.residual_loo = n3[2];
     if (o.verbose) printf("  newton [%d] |R|_2 %.3e |R|_inf %.3e\n", it, n3[0], n3[2]);
     if (!std::isfinite(n3[0]) || !std::isfinite(n3[1]) || !std::isfinite(n3[2])) {

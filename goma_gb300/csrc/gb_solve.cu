@@ -525,11 +525,11 @@ __global__ void __launch_bounds__(256)
 // gather of the solution values stays on the critical path.  A node depends
 // only on nodes of lower levels, which hold earlier tickets, and every CTA of
 // the grid is resident, so a value a CTA waits for is always owed by a CTA
-// that is running or done.  Every wait is bounded: past kSpinLimit polls the
+// that is running or done.  Every wait is bounded: past spin_limit polls the
 // CTA records an error, computes and publishes anyway (so no other CTA can
 // wait forever), every later wait of the sweep stops within 1024 polls, and
 // the host reports the failure after the sweep.  A legitimate wait lasts
-// microseconds; the limit is ~0.3 s.
+// microseconds; the default limit (kSpinLimit) is ~0.3 s.
 //
 // Row structure used by the split: a node's unknowns are contiguous and
 // every row of the node holds every own-node column except the energy row,
@@ -552,6 +552,7 @@ struct TrsvArgs {
   int nvn;             // nodal fields per node
   unsigned *tickets;   // [0] L sweep, [1] U sweep (reset before each sweep)
   int *error;          // set when a wait gave up
+  long long spin_limit;  // polls before a wait gives up
 };
 
 // the "unpublished" sentinels: signalling NaNs (exponent all ones, quiet bit
@@ -595,11 +596,12 @@ __global__ void trsv_prepare_kernel(int64_t n, T *x, unsigned *ticket) {
 
 // one solution value, polled until published (bounded; 0 once given up)
 template <class T>
-__device__ __forceinline__ T poll_value(const T *p, bool &gave_up, const int *error) {
+__device__ __forceinline__ T poll_value(const T *p, bool &gave_up, const int *error,
+                                        long long spin_limit) {
   T v = ld_relaxed(p);
   long long polls = 0;
   while (unpublished(v)) {
-    if (gave_up || ++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile const int *)error)) {
+    if (gave_up || ++polls > spin_limit || ((polls & 1023) == 0 && *(volatile const int *)error)) {
       gave_up = true;
       return (T)0;
     }
@@ -698,7 +700,7 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
         }
         long long polls = 0;
         while (pending) {
-          if (++polls > kSpinLimit || ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
+          if (++polls > g.spin_limit || ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
             gave_up = true;
             break;
           }
@@ -734,7 +736,8 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
           if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
         }
       }
-      for (; p < p1; p += 32) s0 = fmx((A)lu[p], (A)poll_value(x + g.colidx[p], gave_up, g.error), s0);
+      for (; p < p1; p += 32) s0 = fmx((A)lu[p], (A)poll_value(x + g.colidx[p], gave_up, g.error, g.spin_limit),
+                                       s0);
       const A sum = wsum(s0);
       if (lane == 0) part[r] = sum;
     }
@@ -817,6 +820,7 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.nvn = S->C->L.nvn;
   g.tickets = nullptr;
   g.error = nullptr;
+  g.spin_limit = S->C->sweep_spin_limit > 0 ? S->C->sweep_spin_limit : kSpinLimit;
   return g;
 }
 
@@ -955,6 +959,7 @@ int Solver::init(Context *c, int krylov) {
   lo_ptr = S.lo_ptr;
   up_ptr = S.up_ptr;
   num_levels = (int)lo_ptr.size() - 1;
+  lo_nodes_host = S.lo_nodes;
   GB_CU(cudaMalloc(&d_lo_nodes, sizeof(int) * S.lo_nodes.size()), "sched");
   GB_CU(cudaMemcpy(d_lo_nodes, S.lo_nodes.data(), sizeof(int) * S.lo_nodes.size(),
                    cudaMemcpyHostToDevice), "sched");
@@ -1192,13 +1197,29 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
   g.tickets = S->d_flags;
   g.error = (int *)(S->d_flags + 4);
   T *y = static_cast<T *>(S->d_sweep_y);
+  // the host-injected fault of gb_set_sweep_fault: the lower sweep's nodes in
+  // reverse order (every dependency after its dependant) on one CTA, whose
+  // first wait can then only end by running out
+  const int *lo_order = S->d_lo_nodes;
+  int grid = S->trsv_grid;
+  if (S->C->sweep_reverse_lower) {
+    if (!S->d_lo_nodes_rev) {
+      std::vector<int> rev(S->lo_nodes_host.rbegin(), S->lo_nodes_host.rend());
+      GB_CU(cudaMalloc(&S->d_lo_nodes_rev, sizeof(int) * rev.size()), "reversed order");
+      S->owned.push_back(S->d_lo_nodes_rev);
+      GB_CU(cudaMemcpy(S->d_lo_nodes_rev, rev.data(), sizeof(int) * rev.size(),
+                       cudaMemcpyHostToDevice), "reversed order");
+    }
+    lo_order = S->d_lo_nodes_rev;
+    grid = 1;
+  }
   // L: z -> y, then U: y -> z; each output starts all unpublished
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y, g.tickets + 0);
-  g.order = S->d_lo_nodes;
-  trsv_sync_free_kernel<T, true><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, z, y);
+  g.order = lo_order;
+  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lu, z, y);
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z, g.tickets + 1);
   g.order = S->d_up_nodes;
-  trsv_sync_free_kernel<T, false><<<S->trsv_grid, kTrsvThreads, 0, st>>>(g, lu, y, z);
+  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lu, y, z);
   GB_CU(cudaGetLastError(), "trsv");
   return 0;
 }

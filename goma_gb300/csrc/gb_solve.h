@@ -67,6 +67,8 @@ struct Solver {
   int *d_fu = nullptr;          // first unknown per node (shared with C)
   int *d_lo_nodes = nullptr, *d_up_nodes = nullptr;
   std::vector<int> lo_ptr, up_ptr;
+  std::vector<int> lo_nodes_host;  // the lower sweep's order (host copy)
+  int *d_lo_nodes_rev = nullptr;   // it reversed, for the injected sweep fault
   const double *d_A = nullptr;  // scaled FP64 matrix the factors were built from
   double pivot_tau = 1e-4;      // ILU(0) pivot floor on the row-scaled matrix
   int maxnb = 0, lmax = 0;      // largest node neighbourhood / block-row length

@@ -132,6 +132,13 @@ class GomaNewton:
         2 automatic (the default)."""
         _lib.check(self._L.gb_set_triangular_solve(self.h, int(mode)))
 
+    def set_sweep_fault(self, spin_limit=0, reverse_lower=False):
+        """Host-injected fault of the sync-free ILU(0) sweeps
+        (gb_set_sweep_fault): polls per wait before it gives up (0: the
+        default) and a reversed lower-sweep order on one CTA, whose waits can
+        only end by giving up.  set_sweep_fault() restores the normal sweeps."""
+        _lib.check(self._L.gb_set_sweep_fault(self.h, int(spin_limit), 1 if reverse_lower else 0))
+
     def scale_device(self, d_vals, d_R, d_scale=None):
         """row_sum_scaling_scale on device arrays (in place)."""
         _lib.check(self._L.gb_row_sum_scale_device(self.h, d_vals, d_R, d_scale))
@@ -225,6 +232,8 @@ def _stats_dict(st):
     n = st.newton_its
     return {"newton_its": n, "linear_its": st.linear_its, "refinements": st.refinements,
             "residual_l2": [st.residual_l2[i] for i in range(min(n + 1, 64))],
+            "residual_l1": [st.residual_l1[i] for i in range(min(n + 1, 64))],
+            "residual_loo_steps": [st.residual_loo_steps[i] for i in range(min(n + 1, 64))],
             "residual_loo": st.residual_loo, "assemble_ms": st.assemble_ms,
             "scale_ms": st.scale_ms, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
             "total_ms": st.total_ms, "factorizations": st.factorizations}

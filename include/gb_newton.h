@@ -136,6 +136,19 @@ int gb_set_element_density(gb_ctx *ctx, const double *rho);
  * solves are sequential). */
 int gb_set_triangular_solve(gb_ctx *ctx, int mode);
 
+/* Host-side fault injection for the sync-free sweeps' bounded waits; no
+ * counterpart in the reference.  spin_limit sets the polls a wait makes
+ * before it gives up (<= 0: the default, 2^22, about 0.3 s).  With
+ * reverse_lower != 0 the lower sweep hands its nodes out in reverse order
+ * (every dependency after the node that needs it) on a grid of one CTA,
+ * so its first wait can only end by running out: the sweep then finishes
+ * with the error word set, later waits of the solve stop within 1024 polls,
+ * and the linear solve returns -1 ("a dependency wait gave up") with the
+ * context still usable.  (0, 0) restores the normal sweeps.  Applies to
+ * the sync-free sweeps only (gb_set_triangular_solve mode 0, or 2 with a
+ * deep schedule). */
+int gb_set_sweep_fault(gb_ctx *ctx, long long spin_limit, int reverse_lower);
+
 /* Replaces the material of a context (same mesh, DOF map and pattern), as
  * update_parameterC does during continuation (src/ac_conti.c:755,
  * src/ac_update_parameter.c). */
@@ -199,6 +212,11 @@ typedef struct gb_newton_stats {
   double residual_loo;     /* final scaled-residual L-infinity norm */
   double assemble_ms, scale_ms, factor_ms, solve_ms, total_ms;
   int factorizations;      /* ILU(0) factorisations done, all steps */
+  /* the other two norms the reference prints per Newton step
+   * (src/mm_sol_nonlinear.c:1451-1453: L_oo, L_1, L_2 of the scaled
+   * residual) */
+  double residual_l1[64];
+  double residual_loo_steps[64];
 } gb_newton_stats;
 
 /* sizeof of the ABI structs, for bindings that mirror them: 0
