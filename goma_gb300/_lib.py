@@ -63,6 +63,7 @@ def load():
         "gb_msr_pattern": (ctypes.c_int, [vp, ip]),
         "gb_msr_pattern_host": (ctypes.c_int, [vp, ip, llp]),
         "gb_csr_pattern": (ctypes.c_int, [vp, llp, ip]),
+        "gb_csr_row": (ctypes.c_longlong, [vp, vp, ctypes.c_int, llp, ip, dp, ctypes.c_longlong]),
         "gb_first_unknown": (ctypes.c_int, [vp, ip]),
         "gb_dirichlet_init": (ctypes.c_int, [vp, dp]),
         "gb_matrix_fill_full": (ctypes.c_int, [vp, dp, dp, dp]),

@@ -398,6 +398,26 @@ int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx) {
   return 0;
 }
 
+long long gb_csr_row(gb_ctx *ctx, const double *d_vals, int row, long long *start, int *cols,
+                     double *vals, long long capacity) {
+  if (!ctx) return fail("NULL argument");
+  const gb::Layout &L = ctx->c.L;
+  if (row < 0 || row >= L.N) return fail("row out of range");
+  const int64_t b = L.rowptr[row], len = L.rowptr[row + 1] - b;
+  if (start) *start = b;
+  if (!cols && !vals) return len;
+  if (len > capacity) return fail("row longer than the capacity given");
+  if (cols) memcpy(cols, L.colidx.data() + b, sizeof(int) * (size_t)len);
+  if (vals) {
+    if (!d_vals) return fail("NULL device values");
+    cudaError_t e = cudaMemcpyAsync(vals, d_vals + b, sizeof(double) * (size_t)len,
+                                    cudaMemcpyDeviceToHost, ctx->c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->c.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "row copy");
+  }
+  return len;
+}
+
 int gb_first_unknown(const gb_ctx *ctx, int *fu) {
   if (!ctx || !fu) return fail("NULL argument");
   memcpy(fu, ctx->c.L.fu.data(), sizeof(int) * ctx->c.L.fu.size());

@@ -78,6 +78,20 @@ class GomaNewton:
             ctypes.POINTER(ctypes.c_longlong)), ci.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return rp, ci
 
+    def csr_row(self, d_vals, row):
+        """(64-bit start offset, columns, values) of one CSR row of the device
+        values d_vals (gb_csr_row)."""
+        start = ctypes.c_longlong()
+        n = self._L.gb_csr_row(self.h, None, int(row), ctypes.byref(start), None, None, 0)
+        if n < 0:
+            _lib.check(-1)
+        cols = np.empty(n, np.int32)
+        vals = np.empty(n)
+        if self._L.gb_csr_row(self.h, d_vals, int(row), ctypes.byref(start),
+                              cols.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(vals), n) != n:
+            _lib.check(-1)
+        return start.value, cols, vals
+
     def dirichlet_init(self, x):
         x = np.ascontiguousarray(x, np.float64).copy()
         _lib.check(self._L.gb_dirichlet_init(self.h, _dp(x)))

@@ -59,6 +59,14 @@ int gb_ilu_permutation_host(const gb_problem_desc *desc, int *perm, int *num_col
                             long long *rowptr, int *colidx, long long *vmap);
 /* CSR pattern used on the device: rowptr (N+1, int64), colidx (nnz). */
 int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx);
+/* One row of the CSR matrix: its 64-bit start offset in the CSR arrays, its
+ * columns (from the layout) and its values (copied from d_vals, this
+ * context's CSR values on the device; the library stream is synchronised).
+ * Returns the row's length (cols and vals may be NULL to ask for it), or -1
+ * when it exceeds capacity.  For inspecting rows of matrices too large to
+ * copy out whole; no counterpart in the reference. */
+long long gb_csr_row(gb_ctx *ctx, const double *d_vals, int row, long long *start, int *cols,
+                     double *vals, long long capacity);
 /* First unknown of every node (num_nodes + 1 ints), as
  * Nodes[i]->First_Unknown (src/mm_unknown_map.c:758). */
 int gb_first_unknown(const gb_ctx *ctx, int *fu);

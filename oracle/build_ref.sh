@@ -5,9 +5,10 @@
 # shims under oracle/ref_shim/ stand in for MPI (one rank), Exodus II (an
 # in-memory structured mesh), NetCDF/LAPACK/Trilinos (unreached) and the
 # Sparse 1.3 direct solver.  Outputs go only to oracle/_ref/.
-#   usage: oracle/build_ref.sh [reference root, default /root/reference]
+#   usage: oracle/build_ref.sh [reference root; default $GOMA_REFERENCE,
+#          else /root/reference]
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${GOMA_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/_ref
 SHIM=$HERE/ref_shim

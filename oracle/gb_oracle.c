@@ -4,6 +4,7 @@
  * against vectors the reference produced (tests/golden/make_golden.py). */
 #include "gb_oracle.h"
 
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -222,6 +223,12 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
     if (!pass) {
       off = pos - (p->N + 1);
       p->msr_len = (long)p->N + 1 + off;
+      /* beyond the reference's 32-bit MSR indexing: no pattern, element-level
+       * use only (orc_element, orc_element_dofs, residual-only fills) */
+      if (p->msr_len > INT_MAX) {
+        p->ija = NULL;
+        break;
+      }
       p->ija = (int *)malloc(sizeof(int) * (size_t)p->msr_len);
     } else {
       p->ija[p->N] = (int)pos;
@@ -286,6 +293,7 @@ void orc_destroy(orc_problem *p) {
 int orc_num_unknowns(const orc_problem *p) { return p->N; }
 long orc_msr_len(const orc_problem *p) { return p->msr_len; }
 void orc_msr_pattern(const orc_problem *p, int *ija) {
+  if (!p->ija) return;
   memcpy(ija, p->ija, sizeof(int) * (size_t)p->msr_len);
 }
 void orc_first_unknown(const orc_problem *p, int *fu) {
@@ -644,11 +652,13 @@ static int fill_elements(const orc_problem *p, const double *x, double *R, doubl
 }
 
 int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1) {
+  if (a && !p->ija) return -2;
   return fill_elements(p, x, R, a, NULL, e0, e1);
 }
 
 int orc_matrix_fill_list(const orc_problem *p, const double *x, double *R, double *a,
                          const int *elems, int n) {
+  if (a && !p->ija) return -2;
   return fill_elements(p, x, R, a, elems, 0, n);
 }
 

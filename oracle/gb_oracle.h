@@ -25,6 +25,9 @@ extern "C" {
 
 typedef struct orc_problem orc_problem;
 
+/* Builds the DOF map, Dirichlet marks and MSR pattern.  A problem whose MSR
+ * would exceed the reference's 32-bit indexing gets no pattern: only the
+ * element-level calls and residual-only fills (a == NULL) work on it. */
 orc_problem *orc_create(const gb_problem_desc *desc);
 void orc_destroy(orc_problem *p);
 int orc_num_unknowns(const orc_problem *p);

@@ -67,7 +67,17 @@ CASES = {
     "box3d_3x3x3_bouss_solve": dict(mesh="hex27 3 3 3 1 1 1", phys="nst", rho=1.0,
                                     visc=("newtonian", 0.71), bc="cube_heated", datum=True,
                                     mode="solve", tol=1e-12, ra_pr=7100.0),
+    # the lid-driven cavity at its benchmark size (32 x 32 QUAD9, Re 100,
+    # N = 11,522): compact records (every residual entry, a seeded sample of
+    # Jacobian rows and a hash of the whole pattern; the converged solution)
+    "cav2d_32x32": dict(mesh="quad9 32 32 1 1", phys="ns", rho=100.0, visc=("newtonian", 1.0),
+                        bc="cavity2d", datum=True, mode="assemble", seed=8, compact=True),
+    "cav2d_32x32_solve": dict(mesh="quad9 32 32 1 1", phys="ns", rho=100.0,
+                              visc=("newtonian", 1.0), bc="cavity2d", datum=True, mode="solve",
+                              tol=1e-10, compact=True),
 }
+
+COMPACT_ROWS = 300  # Jacobian rows kept by a compact record
 
 # Dirichlet sets: (variable, node set id, value), applied in this order
 BCS = {
@@ -268,16 +278,45 @@ def run_case(name, case, outdir):
             rec["x_converged"] = np.array(vals)
             rec["newton_log"] = "\n".join(l for l in p.stdout.splitlines() if "]" in l[:14])
             rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
-        rec["ija"] = np.fromfile(os.path.join(tmp, "d.ija"), dtype="<i4")
-        rec["a"] = np.fromfile(os.path.join(tmp, "d.a"))
-        rec["R"] = np.fromfile(os.path.join(tmp, "d.R"))
+        ija = np.fromfile(os.path.join(tmp, "d.ija"), dtype="<i4")
+        a = np.fromfile(os.path.join(tmp, "d.a"))
+        R = np.fromfile(os.path.join(tmp, "d.R"))
+        if not case.get("compact"):
+            rec["ija"], rec["a"], rec["R"] = ija, a, R
+        else:
+            rec.update(compact_record(case, ija, a, R))
     np.savez_compressed(os.path.join(outdir, name + ".npz"), **rec)
     return rec
 
 
+def compact_record(case, ija, a, R):
+    """What a large case keeps: N, the msr length, a SHA-256 of the whole
+    pattern, and -- for assembly cases -- every residual entry and a seeded
+    sample of Jacobian rows (diagonal first, then the off-diagonal columns
+    in MSR order)."""
+    import hashlib
+    n = R.size
+    out = {"N": np.int64(n), "msr_len": np.int64(ija[n]),
+           "ija_sha256": hashlib.sha256(ija.astype("<i4").tobytes()).hexdigest()}
+    if case["mode"] != "assemble":
+        return out
+    rng = np.random.default_rng(case["seed"] + 1000)
+    rows = np.unique(np.concatenate([np.arange(8), np.arange(n - 8, n),
+                                     rng.choice(n, COMPACT_ROWS, replace=False)]))
+    ptr, cols, vals = [0], [], []
+    for i in rows:
+        cols += [i] + list(ija[ija[i]:ija[i + 1]])
+        vals += [a[i]] + list(a[ija[i]:ija[i + 1]])
+        ptr.append(len(cols))
+    out.update(R=R, rows=rows.astype(np.int32), row_ptr=np.array(ptr, np.int32),
+               row_cols=np.array(cols, np.int32), row_vals=np.array(vals))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GOMA_REFERENCE", "/root/reference"),
+                    help="reference source root (default: $GOMA_REFERENCE)")
     ap.add_argument("cases", nargs="*")
     args = ap.parse_args()
     if not os.path.exists(GOMA):
@@ -285,8 +324,12 @@ def main():
     names = args.cases or list(CASES)
     for name in names:
         rec = run_case(name, CASES[name], HERE)
-        n = rec["R"].size
-        print("%-28s N=%6d msr_len=%8d %s" % (name, n, rec["ija"][n], CASES[name]["mode"]))
+        if "ija" in rec:
+            n = rec["R"].size
+            ml = rec["ija"][n]
+        else:
+            n, ml = int(rec["N"]), int(rec["msr_len"])
+        print("%-28s N=%6d msr_len=%8d %s" % (name, n, ml, CASES[name]["mode"]))
 
 
 if __name__ == "__main__":

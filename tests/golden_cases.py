@@ -11,14 +11,38 @@ from goma_gb300 import problem as pb
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names(mode=None):
+def names(mode=None, compact=False):
+    """Golden case names (of one mode); compact=True lists the compact
+    records of large cases (sampled Jacobian rows, pattern hash) instead of
+    the full ones."""
     out = []
     for f in sorted(os.listdir(GOLDEN)):
         if f.endswith(".npz"):
             n = f[:-4]
-            if mode is None or load(n)[1]["mode"] == mode:
+            case = load(n)[1]
+            if (mode is None or case["mode"] == mode) and bool(case.get("compact")) == compact:
                 out.append(n)
     return out
+
+
+def compact_rows_check(g, ija, a, R):
+    """Row-scaled error of the sampled Jacobian rows and of R of a compact
+    record against an assembly (MSR ija / a, residual R), after checking the
+    pattern's hash."""
+    import hashlib
+    n = int(g["N"])
+    assert R.size == n and int(ija[n]) == int(g["msr_len"])
+    assert hashlib.sha256(np.asarray(ija, "<i4").tobytes()).hexdigest() == str(g["ija_sha256"])
+    worst = 0.0
+    rows, ptr, cols, vals = g["rows"], g["row_ptr"], g["row_cols"], g["row_vals"]
+    for k, i in enumerate(rows):
+        c = cols[ptr[k]:ptr[k + 1]]
+        v = vals[ptr[k]:ptr[k + 1]]
+        assert c[0] == i and np.array_equal(c[1:], ija[ija[i]:ija[i + 1]])
+        got = np.concatenate([[a[i]], a[ija[i]:ija[i + 1]]])
+        worst = max(worst, np.abs(got - v).max() / max(np.abs(v).max(), 1e-300))
+    rerr = np.abs(R - g["R"]).max() / np.abs(g["R"]).max()
+    return worst, rerr
 
 
 def load(name):
@@ -65,3 +89,17 @@ def msr_row_scaled_error(ija, a, ref):
         d = max(abs(a[i] - ref[i]), np.abs(a[lo:hi] - ref[lo:hi]).max() if hi > lo else 0.0)
         worst = max(worst, d / scale)
     return worst
+
+
+def msr_row_scaled_error_fast(ija, a, ref):
+    """msr_row_scaled_error, vectorised for large matrices (every row must
+    have off-diagonal entries)."""
+    N = int(ija[0]) - 1
+    lens = np.diff(np.asarray(ija[:N + 1], np.int64))
+    assert (lens > 0).all()
+    starts = np.asarray(ija[:N], np.int64) - (N + 1)
+    dm = np.maximum.reduceat(np.abs(a[N + 1:] - ref[N + 1:]), starts)
+    rm = np.maximum.reduceat(np.abs(ref[N + 1:]), starts)
+    dm = np.maximum(dm, np.abs(a[:N] - ref[:N]))
+    rm = np.maximum(rm, np.abs(ref[:N]))
+    return float((dm / np.maximum(rm, 1e-300)).max())

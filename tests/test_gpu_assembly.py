@@ -190,3 +190,110 @@ def test_3d_element_kernels_agree(prob_fn, path):
     assert np.abs(R_tc - R_sc).max() <= TOL * np.abs(Ro).max()
     if path in (3, 4):
         assert np.array_equal(R_res, R_tc)
+
+
+@pytest.mark.parametrize("name", gc.names("assemble", compact=True))
+def test_gpu_assembly_matches_reference_at_benchmark_size(name):
+    """The 32 x 32 lid-driven cavity at the benchmark size: the whole pattern
+    (hash), every residual entry and a seeded sample of Jacobian rows of the
+    reference's own assembly."""
+    g, case = gc.load(name)
+    gn = GomaNewton(gc.problem_from_case(case))
+    R, a = gn.matrix_fill_full(g["x"])
+    jerr, rerr = gc.compact_rows_check(g, gn.msr_pattern(), a, R)
+    assert jerr < TOL and rerr <= TOL
+
+
+def test_gpu_assembly_matches_oracle_on_the_32_cube():
+    """The benchmark workload itself: the 32^3 HEX27 Boussinesq cube
+    (1,229,572 unknowns, 308 M nonzeros), every residual entry and every
+    Jacobian entry against the oracle's assembly (colour-parallel on the
+    host cores), so every colour's persistent element loop runs its full
+    4,096 elements."""
+    import os
+    prob = pb.boussinesq_cube_3d(32, 1e5, 0.71)
+    o = oracle.Oracle(prob)
+    x = o.dirichlet_init(np.random.default_rng(23).uniform(-1.0, 1.0, o.N))
+    pf = oracle.ParallelFill(o, os.cpu_count() or 1)
+    try:
+        assert pf(x) == 0
+        Ro, ao = pf.R, pf.a
+        gn = GomaNewton(prob)
+        ija = o.ija()
+        assert np.array_equal(gn.msr_pattern(), ija)
+        R, a = gn.matrix_fill_full(x)
+        assert gc.msr_row_scaled_error_fast(ija, a, ao) < TOL
+        assert np.abs(R - Ro).max() <= TOL * np.abs(Ro).max()
+    finally:
+        pf.close()
+
+
+def test_gpu_reacting_channel_rows_beyond_32bit_offsets_match_oracle():
+    """The 64 x 64 x 32 reacting channel (7.0 M unknowns, 2.6e9 nonzeros:
+    CSR offsets past 2^31, which the reference's 32-bit MSR cannot hold).
+    Rows whose CSR start lies beyond 2^31 -- the last row, the first row
+    past the boundary, a pressure row and seeded random ones -- against the
+    oracle's element-level assembly of the elements around the row's node,
+    and the residual entries of those rows."""
+    import ctypes
+
+    import torch
+    prob = pb.reacting_channel_3d(64, 64, 32, seed=0)
+    gn = GomaNewton(prob)
+    assert gn.nnz > 2 ** 31
+    x = gn.dirichlet_init(np.random.default_rng(5).uniform(0.5, 1.5, gn.N))
+    dx = torch.tensor(x, dtype=torch.float64, device="cuda")
+    dR = torch.empty(gn.N, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    gn.matrix_fill_full_device(dx.data_ptr(), dR.data_ptr(), gn.d_vals)
+    gn.status()
+    R = dR.cpu().numpy()
+    fu = np.empty(prob.mesh.num_nodes + 1, np.int32)
+    from goma_gb300 import _lib
+    _lib.check(gn._L.gb_first_unknown(gn.h, fu.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    # first row whose CSR start is past 2^31 (starts ascend)
+    lo, hi = 0, gn.N - 1
+    while lo < hi:
+        mid = (lo + hi) // 2
+        if _row_start(gn, mid) >= 2 ** 31:
+            hi = mid
+        else:
+            lo = mid + 1
+    r0 = lo
+    assert _row_start(gn, r0) >= 2 ** 31 > _row_start(gn, r0 - 1)
+    conn = np.asarray(prob.mesh.conn)
+    centroids = conn[:, 20]
+    nvn = 6
+    p_rows = fu[centroids] + nvn
+    rows = {r0, gn.N - 1, int(p_rows[p_rows >= r0][0])}
+    rows |= set(np.random.default_rng(9).integers(r0, gn.N, 6).tolist())
+    o = oracle.Oracle(prob)
+    for r in sorted(rows):
+        start, cols, vals = gn.csr_row(gn.d_vals, r)
+        assert start >= 2 ** 31
+        node = int(np.searchsorted(fu, r, side="right") - 1)
+        els = np.flatnonzero((conn == node).any(axis=1))
+        exp, Rr, Rabs = {}, 0.0, 0.0
+        for e in els:
+            Re, Je, g, st = o.element(int(e), x)
+            assert st == 0
+            lr = int(np.flatnonzero(g == r)[0])
+            Rr += Re[lr]
+            Rabs += abs(Re[lr])
+            for c, v in zip(g, Je[lr]):
+                exp[int(c)] = exp.get(int(c), 0.0) + v
+        ref = np.array([exp.get(int(c), 0.0) for c in cols])
+        missing = [c for c, v in exp.items() if v != 0.0 and c not in set(cols.tolist())]
+        assert not missing, (r, missing[:5])
+        assert np.abs(vals - ref).max() <= TOL * np.abs(ref).max(), r
+        assert abs(R[r] - Rr) <= TOL * max(Rabs, 1e-300), r
+    del dx, dR
+    gn.close()
+    torch.cuda.empty_cache()
+
+
+def _row_start(gn, row):
+    import ctypes
+    s = ctypes.c_longlong()
+    gn._L.gb_csr_row(gn.h, None, int(row), ctypes.byref(s), None, None, 0)
+    return s.value

@@ -30,6 +30,24 @@ def test_gpu_newton_matches_reference_solution(name, fp32_inner, ordering):
     assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
 
 
+@pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
+@pytest.mark.parametrize("name", gc.names("solve", compact=True))
+def test_gpu_newton_matches_reference_solution_at_benchmark_size(name, fp32_inner):
+    """The 32 x 32 lid-driven cavity at Re 100 (the benchmark size, 11,522
+    unknowns) from rest to the scaled residual 1e-10, against the reference's
+    converged fields, with the reference's solver settings (ILU(0) in its
+    node order, GMRES(30))."""
+    g, case = gc.load(name)
+    gn = GomaNewton(gc.problem_from_case(case))
+    gn.set_ilu_ordering(0)
+    x, conv, st = gn.solve_nonlinear_problem(None, residual_tol=case["tol"], linear_tol=1e-10,
+                                             fp32_inner=fp32_inner, max_newton=30,
+                                             krylov_dim=30, max_linear_its=3000)
+    assert conv, st
+    xc = g["x_converged"]
+    assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
+
+
 def test_gpu_linear_solve_drop_in():
     """gb_linear_solve on the reference-scaled MSR system matches a direct
     solve of the same system (oracle band LU via one Newton correction)."""

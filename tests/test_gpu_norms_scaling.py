@@ -75,7 +75,7 @@ def _printed_close(value, printed):
     return abs(value - printed) <= 0.5 * 10.0 ** (e - 1) * 1.001
 
 
-@pytest.mark.parametrize("name", gc.names("solve"))
+@pytest.mark.parametrize("name", gc.names("solve") + gc.names("solve", compact=True))
 def test_newton_residual_norms_match_the_reference_log(name):
     g, case = gc.load(name)
     gn = GomaNewton(gc.problem_from_case(case))

@@ -36,6 +36,31 @@ def test_oracle_newton_matches_reference(name):
     assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
 
 
+@pytest.mark.parametrize("name", gc.names("assemble", compact=True))
+def test_oracle_assembly_matches_reference_at_benchmark_size(name):
+    """The 32 x 32 lid-driven cavity (the benchmark size): the whole pattern
+    (hash), every residual entry and a seeded sample of Jacobian rows."""
+    g, case = gc.load(name)
+    o = oracle.Oracle(gc.problem_from_case(case))
+    R, a, st = o.matrix_fill(g["x"])
+    assert st == 0
+    jerr, rerr = gc.compact_rows_check(g, o.ija(), a, R)
+    assert jerr < TOL_RJ and rerr <= TOL_RJ
+
+
+@pytest.mark.parametrize("name", gc.names("solve", compact=True))
+def test_oracle_newton_matches_reference_at_benchmark_size(name):
+    import hashlib
+    g, case = gc.load(name)
+    o = oracle.Oracle(gc.problem_from_case(case))
+    ija = o.ija()
+    assert hashlib.sha256(ija.astype("<i4").tobytes()).hexdigest() == str(g["ija_sha256"])
+    x, it, _ = o.newton(o.dirichlet_init(np.zeros(o.N)), 40, case["tol"])
+    assert it > 0
+    xc = g["x_converged"]
+    assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
+
+
 def test_oracle_mesh_generator_matches_package():
     from goma_gb300.problem import mesh_from_spec
     for spec in ["quad9 3 2 1.5 1 0.15 7", "hex27 2 1 3 1 0.5 1.5 0.12 9", "quad9 5 4 2 1"]:
