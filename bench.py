@@ -582,6 +582,45 @@ def ilu_orders(sizes=(8, 16, 24), ra=1e4, tol=1e-10):
                         "GMRES(60), Eisenstat-Walker forcing" % (ra, tol), "runs": rows}
 
 
+def krylov_kernels(nel, iters=30, ra=1e4):
+    """The linear-solver kernels on one Newton system of the nel^3
+    Boussinesq cube (the state at rest, Ra `ra`), in the reference's node
+    order with the sync-free sweeps: one Newton step each in FP64 and in
+    FP32-inner mode, each a factorisation plus exactly `iters` GMRES(iters)
+    iterations (tolerance out of reach), timed by the Newton driver's CUDA
+    events.  Algorithmic bytes per launch, for the rooflines of the launch
+    list: SpMV 12 nnz + 24 N (FP64) / 8 nnz + 12 N (FP32); one triangular
+    sweep reads its factor's half of the values and column indices, the
+    right-hand side and writes the solution (about (8 + 4) nnz / 2 + 16 N
+    in FP64, (4 + 4) nnz / 2 + 8 N in FP32)."""
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    gn = GomaNewton(pb.boussinesq_cube_3d(nel, ra, PR))
+    gn.set_ilu_ordering(0)
+    gn.set_triangular_solve(0)
+    N, nnz = gn.N, gn.nnz
+    out = {"workload": "%d^3 Boussinesq cube, one Newton step from rest (Ra %g): ILU(0) in the "
+                       "reference's node order, sync-free sweeps, %d GMRES(%d) iterations"
+                       % (nel, ra, iters, iters),
+           "unknowns": N, "csr_nnz": nnz,
+           "bytes": {"spmv_fp64": 12 * nnz + 24 * N, "spmv_fp32": 8 * nnz + 12 * N,
+                     "sweep_fp64": 6 * nnz + 16 * N, "sweep_fp32": 4 * nnz + 8 * N}}
+    for fp32 in (False, True):
+        torch.cuda.synchronize()
+        x, conv, st = gn.solve_nonlinear_problem(
+            None, residual_tol=1e-300, linear_tol=1e-300, max_newton=1, max_linear_its=iters,
+            krylov_dim=iters, fp32_inner=fp32, max_refinements=1, inner_tol=1e-300)
+        torch.cuda.synchronize()
+        out["fp32" if fp32 else "fp64"] = {
+            "linear_its": st["linear_its"], "factor_ms": st["factor_ms"],
+            "solve_ms": st["solve_ms"], "ms_per_iteration": st["solve_ms"] / max(1, st["linear_its"])}
+        print("krylov:", out["fp32" if fp32 else "fp64"], file=sys.stderr, flush=True)
+    gn.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
                      predictors=("zeroth", "secant", "learned")):
     """The learned-predictor configuration: backward-facing step, nx x ny
@@ -698,7 +737,9 @@ def main():
                          "stages of at most 1.6x), bfs (the 96x32 "
                          "Carreau step continuation), ilu_orders (cube solves in both ILU(0) "
                          "node orders, 8^3 to 24^3), cpu_solve (the 8^3 time-to-solve sweep on "
-                         "one host core with the oracle's ILU(0)-GMRES(30))")
+                         "one host core with the oracle's ILU(0)-GMRES(30)), krylovN (the "
+                         "linear-solver kernels on one N^3 cube system: factorisation + 30 "
+                         "GMRES iterations, FP64 and FP32)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -893,6 +934,8 @@ def main():
                 extra[w] = factorization_reuse_solves(16)
             elif w == "cpu_solve":
                 extra[w] = cpu_time_to_solve(8)
+            elif w.startswith("krylov"):
+                extra[w] = krylov_kernels(int(w[len("krylov"):] or 16))
         line["workloads"] = extra
     if rank == 0:
         print(json.dumps(line))
