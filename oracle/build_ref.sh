@@ -47,5 +47,5 @@ gcc $SHIMC -c "$SHIM/ref_main.c" -o "$OUT/ref_main.o"
 OBJS=$(ls "$OUT"/obj/*.o | grep -v '/main\.o$')
 gcc -o "$OUT/goma_ref" "$OUT/ref_main.o" $OBJS "$OUT"/exo_mem.o "$OUT"/mpi_serial.o \
   "$OUT"/band_lu.o "$OUT"/tpl_stubs.o "$OUT"/mesh_gen.o "$OUT"/harness.o "$OUT"/user_species.o \
-  -Wl,--wrap=matrix_fill_full -Wl,--wrap=usr_species_source -lm
+  -Wl,--wrap=matrix_fill_full -Wl,--wrap=numerical_jacobian -Wl,--wrap=usr_species_source -lm
 echo "build_ref: built $OUT/goma_ref"

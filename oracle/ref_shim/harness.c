@@ -10,6 +10,10 @@
  *                 (int32, MSR bindx), <prefix>.a (float64, MSR values),
  *                 <prefix>.R and <prefix>.x (float64, length N)
  *   GB_REF_EXIT   when set, exit(0) right after that first dump
+ * With -Wl,--wrap=numerical_jacobian the reference's Jacobian checker
+ * (src/mm_numjac.c:716, run when the deck sets Debug = -1/-2/-3) also gets
+ * the GB_REF_X_IN state before it copies x, so its perturbed states are
+ * taken around that state.
  * Everything else runs the unmodified reference code. */
 #include <stdio.h>
 #include <stdlib.h>
@@ -29,6 +33,38 @@ int __real_matrix_fill_full(struct GomaLinearSolverData *ams, double x[], double
                             dbl *estifm);
 
 static int g_calls = 0;
+
+/* x[] <- the GB_REF_X_IN file (N doubles) */
+static void read_x_in(const char *xin, double *x, int N) {
+  FILE *f = fopen(xin, "rb");
+  if (!f || fread(x, sizeof(double), (size_t)N, f) != (size_t)N) {
+    fprintf(stderr, "harness: cannot read %d doubles from %s\n", N, xin);
+    exit(3);
+  }
+  fclose(f);
+}
+
+void __real_numerical_jacobian(struct GomaLinearSolverData *ams, double x[],
+                               double resid_vector[], double delta_t, double theta,
+                               double x_old[], double x_older[], double xdot[],
+                               double xdot_old[], double x_update[], int num_total_nodes,
+                               struct elem_side_bc_struct *first_elem_side_BC_array[],
+                               int Debug_Flag, double time_value, Exo_DB *exo, Dpi *dpi,
+                               double *h_elem_avg, double *U_norm);
+
+void __wrap_numerical_jacobian(struct GomaLinearSolverData *ams, double x[],
+                               double resid_vector[], double delta_t, double theta,
+                               double x_old[], double x_older[], double xdot[],
+                               double xdot_old[], double x_update[], int num_total_nodes,
+                               struct elem_side_bc_struct *first_elem_side_BC_array[],
+                               int Debug_Flag, double time_value, Exo_DB *exo, Dpi *dpi,
+                               double *h_elem_avg, double *U_norm) {
+  const char *xin = getenv("GB_REF_X_IN");
+  if (xin) read_x_in(xin, x, ams->npu);
+  __real_numerical_jacobian(ams, x, resid_vector, delta_t, theta, x_old, x_older, xdot, xdot_old,
+                            x_update, num_total_nodes, first_elem_side_BC_array, Debug_Flag,
+                            time_value, exo, dpi, h_elem_avg, U_norm);
+}
 
 static void dump(const char *prefix, const char *ext, const void *p, size_t sz, size_t n) {
   char path[4096];
@@ -50,14 +86,7 @@ int __wrap_matrix_fill_full(struct GomaLinearSolverData *ams, double x[], double
                             dbl *estifm) {
   const int N = ams->npu;
   const char *xin = getenv("GB_REF_X_IN");
-  if (xin && g_calls == 0) {
-    FILE *f = fopen(xin, "rb");
-    if (!f || fread(x, sizeof(double), (size_t)N, f) != (size_t)N) {
-      fprintf(stderr, "harness: cannot read %d doubles from %s\n", N, xin);
-      exit(3);
-    }
-    fclose(f);
-  }
+  if (xin && g_calls == 0) read_x_in(xin, x, N);
   int err = __real_matrix_fill_full(ams, x, resid_vector, x_old, x_older, xdot, xdot_old,
                                     x_update, ptr_delta_t, ptr_theta, first_elem_side_BC_array,
                                     ptr_time_value, exo, dpi, ptr_num_total_nodes,

@@ -313,14 +313,59 @@ def compact_record(case, ija, a, R):
     return out
 
 
+NUMJAC = os.path.join(HERE, "numjac_reference.json")
+
+
+def run_numjac(name, case):
+    """The reference's own analytic-Jacobian checker (numerical_jacobian,
+    src/mm_numjac.c:716, its default bracketed form) run by the reference on
+    an assembly case at the case's seeded state: the deck's Debug = -2 makes
+    solve_nonlinear_problem call it on its first step (rows scaled by their
+    row sums; src/mm_sol_nonlinear.c:1194-1216) and exit.  Returns the
+    entries it flags: the lines it prints for a perturbed residual outside
+    the band the analytic Jacobians allow, and its dependency warnings."""
+    g = np.load(os.path.join(HERE, name + ".npz"))
+    with tempfile.TemporaryDirectory() as tmp:
+        with open(os.path.join(tmp, "input"), "w") as f:
+            f.write(deck_text(case).replace("Debug = 0", "Debug = -2"))
+        with open(os.path.join(tmp, "fluid.mat"), "w") as f:
+            f.write(mat_text(case))
+        g["x"].astype("<f8").tofile(os.path.join(tmp, "x.bin"))
+        env = dict(os.environ, GB_REF_MESH=case["mesh"], GB_REF_X_IN=os.path.join(tmp, "x.bin"))
+        p = subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env, check=True,
+                           capture_output=True, text=True)
+    if "numerical Jacobian done" not in p.stdout:
+        raise RuntimeError("%s: the reference's checker did not finish:\n%s" % (name, p.stdout[-2000:]))
+    flagged = [l.strip() for l in p.stderr.splitlines()
+               if "conf=" in l or "Potential dependency error" in l]
+    return {"columns": int(g["x"].size), "debug_flag": -2, "flagged": flagged}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GOMA_REFERENCE", "/root/reference"),
                     help="reference source root (default: $GOMA_REFERENCE)")
+    ap.add_argument("--numjac", action="store_true",
+                    help="run the reference's Jacobian checker on the (non-compact) assembly "
+                         "cases into numjac_reference.json instead")
     ap.add_argument("cases", nargs="*")
     args = ap.parse_args()
     if not os.path.exists(GOMA):
         subprocess.run([os.path.join(REPO, "oracle", "build_ref.sh"), args.ref], check=True)
+    if args.numjac:
+        names = args.cases or [n for n, c in CASES.items()
+                               if c["mode"] == "assemble" and not c.get("compact")]
+        out = {}
+        if os.path.exists(NUMJAC):
+            with open(NUMJAC) as f:
+                out = json.load(f)
+        for name in names:
+            out[name] = run_numjac(name, CASES[name])
+            print("%-28s columns=%5d flagged=%d" % (name, out[name]["columns"],
+                                                     len(out[name]["flagged"])))
+        with open(NUMJAC, "w") as f:
+            json.dump(out, f, indent=1, sort_keys=True)
+        return 0
     names = args.cases or list(CASES)
     for name in names:
         rec = run_case(name, CASES[name], HERE)

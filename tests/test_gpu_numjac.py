@@ -45,3 +45,40 @@ def test_analytic_jacobian_matches_finite_differences(prob_fn):
         mask = np.abs(R0) > 0
         err = np.abs(Jv - fd)[mask].max() / np.abs(Jv[mask]).max()
         assert err < 1e-6, err
+
+
+@pytest.mark.parametrize("name", ["cav2d_2x2", "cav2d_3x2_pert", "bfs2d_4x2_carreau",
+                                  "box3d_2x2x2_bouss", "box3d_2x1x3_carreau_t",
+                                  "box3d_2x2x2_species"])
+def test_gpu_jacobian_passes_the_reference_checker_like_the_reference(name):
+    """The reference's own Jacobian checker (numerical_jacobian with
+    Debug = -2, src/mm_numjac.c:716, restated in tests/numjac_check.py) on
+    the GPU's assembly: every column of every golden assembly problem,
+    perturbed around the golden state, flags exactly what the reference
+    flagged when it checked its own analytic Jacobian on the same problem
+    and state (tests/golden/numjac_reference.json, from running the
+    reference; nothing)."""
+    import json
+    import os
+
+    from tests import golden_cases as gc
+    from tests import numjac_check as nj
+    with open(os.path.join(gc.GOLDEN, "numjac_reference.json")) as f:
+        ref = json.load(f)[name]
+    g, case = gc.load(name)
+    prob = nj.without_dirichlet(gc.problem_from_case(case))
+    gn = GomaNewton(prob)
+    assert gn.N == ref["columns"]
+    ija = gn.msr_pattern()
+
+    def fill(x):
+        R, a = gn.matrix_fill_full(x)
+        return R, nj.msr_to_dense(ija, a)
+
+    fu = np.empty(prob.mesh.num_nodes + 1, np.int32)
+    import ctypes
+
+    from goma_gb300 import _lib
+    _lib.check(gn._L.gb_first_unknown(gn.h, fu.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    flagged = nj.check(nj.Layout(prob, fu), fill, g["x"])
+    assert len(flagged) == len(ref["flagged"]), flagged[:5]
