@@ -55,6 +55,9 @@ def lib():
         L.orc_element_dofs.argtypes = [vp, ctypes.c_int, ip]
         L.orc_row_sum_scale.argtypes = [vp, dp, dp, dp]
         L.orc_newton.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp]
+        L.orc_set_transient.argtypes = [vp, dp, ctypes.c_double]
+        L.orc_newton_transient.argtypes = [vp, dp, dp, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_double, dp]
         L.orc_ilu0.argtypes = [vp, dp, ctypes.c_double, dp]
         L.orc_gmres_ilu0.argtypes = [vp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, ip, dp]
@@ -109,15 +112,80 @@ class Oracle:
         lib().orc_dirichlet_init(self.h, _p(x, ctypes.c_double))
         return x
 
-    def matrix_fill(self, x, jacobian=True, e0=0, e1=None):
-        """Returns (R, a_msr or None, status)."""
+    def matrix_fill(self, x, jacobian=True, e0=0, e1=None, xdot=None, delta_t=None, theta=0.0):
+        """Returns (R, a_msr or None, status).  With xdot (and delta_t,
+        theta) the transient terms: mass terms of xdot, their sensitivity
+        (1 + 2 theta) / delta_t."""
         x = np.ascontiguousarray(x, np.float64)
         R = np.zeros(self.N)
         a = np.zeros(self.msr_len) if jacobian else None
-        st = lib().orc_matrix_fill(self.h, _p(x, ctypes.c_double), _p(R, ctypes.c_double),
-                                   _p(a, ctypes.c_double) if a is not None else None, e0,
-                                   self.num_elems if e1 is None else e1)
+        if xdot is not None:
+            xdot = np.ascontiguousarray(xdot, np.float64)
+            lib().orc_set_transient(self.h, _p(xdot, ctypes.c_double),
+                                    (1.0 + 2.0 * theta) / delta_t)
+        try:
+            st = lib().orc_matrix_fill(self.h, _p(x, ctypes.c_double), _p(R, ctypes.c_double),
+                                       _p(a, ctypes.c_double) if a is not None else None, e0,
+                                       self.num_elems if e1 is None else e1)
+        finally:
+            if xdot is not None:
+                lib().orc_set_transient(self.h, None, 0.0)
         return R, a, st
+
+    def newton_transient(self, x0, xdot0, delta_t, theta, max_it=40, tol=1e-10):
+        """One time step's Newton solve from the predicted (x0, xdot0):
+        (x, xdot, iterations or -1)."""
+        x = np.ascontiguousarray(x0, np.float64).copy()
+        xd = np.ascontiguousarray(xdot0, np.float64).copy()
+        norms = np.full(max_it, np.nan)
+        it = lib().orc_newton_transient(self.h, _p(x, ctypes.c_double), _p(xd, ctypes.c_double),
+                                        (1.0 + 2.0 * theta) / delta_t, max_it, tol,
+                                        _p(norms, ctypes.c_double))
+        return x, xd, it
+
+    def transient_run(self, x0, nsteps, delta_t, theta, tol=1e-10, max_it=40):
+        """The reference's fixed-step transient loop (solve_problem,
+        src/rf_solve.c:1138-2601, with a constant delta_t): histories start
+        at x0 with zero time derivatives; the first three steps are backward
+        Euler (theta = 0, :1378-1386), then the given theta; each step
+        predicts x and xdot (predict_solution, :2767), solves, and shifts
+        the histories (:2359-2366).  Returns the solution after every
+        step."""
+        x = self.dirichlet_init(x0)
+        x_old = x.copy()
+        x_older = x.copy()
+        x_oldest = x.copy()
+        xd_old = np.zeros_like(x)
+        xd_older = np.zeros_like(x)
+        out = []
+        for nt in range(nsteps):
+            th = 0.0 if nt < 3 else theta
+            x, xd = predict(delta_t, delta_t, delta_t, th, x_old, x_older, x_oldest, xd_old,
+                            xd_older)
+            x, xd, it = self.newton_transient(x, xd, delta_t, th, max_it, tol)
+            if it < 0:
+                raise RuntimeError("oracle transient step %d did not converge" % nt)
+            out.append(x.copy())
+            xd_older, xd_old = xd_old, xd
+            x_oldest, x_older, x_old = x_older, x_old, x
+        return out
+
+
+def predict(dt, dt_old, dt_older, theta, x_old, x_older, x_oldest, xd_old, xd_older):
+    """predict_solution (src/rf_solve.c:2767-2834): the trapezoid rule's
+    second-order extrapolation for theta = 0.5, else the first-order one;
+    xdot consistent with the predicted x."""
+    if theta == 0.5:
+        c1 = dt * (dt + dt_old) / dt_older / (dt_older + dt_old)
+        c2 = -dt * (dt + dt_old + dt_older) / (dt_old * dt_older)
+        c3 = (dt + dt_old + dt_older) * (dt + dt_old) / dt_old / (dt_older + dt_old)
+        x = c3 * x_old + c2 * x_older + c1 * x_oldest
+    else:
+        c1 = dt * (1.0 + theta * dt / dt_old)
+        c2 = theta * dt * dt / dt_old
+        x = x_old + c1 * xd_old - c2 * xd_older
+    xd = (1.0 + 2.0 * theta) / dt * (x - x_old) - 2.0 * theta * xd_old
+    return x, xd
 
     def element(self, e, x, apply_bc=True):
         x = np.ascontiguousarray(x, np.float64)

@@ -27,6 +27,10 @@ struct orc_problem {
   long msr_len;
   int *dbc;   /* per unknown: -1, or index of the Dirichlet card (datum: -2) */
   double *dbc_val;
+  /* transient: the time derivative xdot (NULL when steady) and the mass
+   * coefficient (1 + 2 theta) / delta_t of its sensitivity */
+  const double *xdot;
+  double mass_c;
 };
 
 /* ---------------------------------------------------------------- basis */
@@ -352,6 +356,9 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
   const int *cn = p->conn + (size_t)e * nn;
   int status = 0;
   double X[27][3], U[27][3], Tn[27], Pn[4], Yn[GB_MAX_SPECIES][27];
+  /* nodal time derivatives of the transient terms (zero when steady) */
+  double Ud[27][3], Tdn[27], Ydn[GB_MAX_SPECIES][27];
+  const double *xd = p->xdot, mc = p->xdot ? p->mass_c : 0.0;
   int g[27 * (4 + GB_MAX_SPECIES) + 4];
   orc_element_dofs(p, e, g);
   for (int k = 0; k < nn; k++) {
@@ -359,6 +366,9 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
     for (int a = 0; a < dim; a++) U[k][a] = x[g[a * nn + k]];
     Tn[k] = en ? x[g[oT + k]] : 0.0;
     for (int w = 0; w < ns; w++) Yn[w][k] = x[g[oY + w * nn + k]];
+    for (int a = 0; a < dim; a++) Ud[k][a] = xd ? xd[g[a * nn + k]] : 0.0;
+    Tdn[k] = (en && xd) ? xd[g[oT + k]] : 0.0;
+    for (int w = 0; w < ns; w++) Ydn[w][k] = xd ? xd[g[oY + w * nn + k]] : 0.0;
   }
   for (int l = 0; l < npr; l++) Pn[l] = x[g[oP + l]];
   memset(Re, 0, sizeof(double) * (size_t)nloc);
@@ -430,6 +440,13 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         Y[w] += Yn[w][k] * phi[k];
         for (int pp = 0; pp < dim; pp++) gY[w][pp] += Yn[w][k] * gphi[k][pp];
       }
+    /* time derivatives at the point (load_fv: fv_dot, src/load_field_variables.c) */
+    double vd[3] = {0, 0, 0}, Td = 0.0, Yd[GB_MAX_SPECIES] = {0};
+    for (int k = 0; k < nn; k++) {
+      for (int a = 0; a < dim; a++) vd[a] += Ud[k][a] * phi[k];
+      Td += Tdn[k] * phi[k];
+      for (int w = 0; w < ns; w++) Yd[w] += Ydn[w][k] * phi[k];
+    }
     double divv = 0.0;
     for (int a = 0; a < dim; a++) divv += gv[a][a];
     double gam[3][3];
@@ -491,7 +508,12 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * Pi[a][pp];
         dif *= -dA;
         double src = f[a] * (phi[i] * dA);
-        Re[ri] += adv + dif + src;
+        /* mass term -rho v_dot_a phi_i dA (src/mm_fill_momentum.c:471-500) */
+        double mass = -rho * vd[a] * phi[i] * dA;
+        Re[ri] += mass + adv + dif + src;
+        /* its sensitivity -(1 + 2 theta) / dt rho phi_i phi_j dA (:1586-1590) */
+        if (mc != 0.0)
+          for (int j = 0; j < nn; j++) JE(ri, a * nn + j) += -mc * rho * phi[i] * phi[j] * dA;
         /* J_m_v */
         double gi_dot_gam = 0.0;
         for (int pp = 0; pp < dim; pp++) gi_dot_gam += gphi[i][pp] * gam[a][pp];
@@ -532,7 +554,10 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         double dif = 0.0;
         for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * (-kc * gT[pp]);
         dif *= dA;
-        Re[ri] += adv + dif;
+        /* mass term -rho Cp T_dot phi_i dA (src/mm_fill_energy.c:315-381) */
+        Re[ri] += adv + dif - rcp * Td * phi[i] * dA;
+        if (mc != 0.0)
+          for (int j = 0; j < nn; j++) JE(ri, oT + j) += -mc * rcp * phi[i] * phi[j] * dA;
         for (int j = 0; j < nn; j++) {
           double vgj = 0.0, gij = 0.0;
           for (int pp = 0; pp < dim; pp++) {
@@ -569,6 +594,11 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         double dif = 0.0;
         for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * (-D * gY[w][pp]);
         Re[ri] += -vgY * phi[i] * dA + dif * dA + S * phi[i] * dA;
+        /* mass term -Y_dot_w phi_i dA, with the advection term's unit
+         * coefficient (src/mm_fill_species.c:525-551) */
+        Re[ri] += -Yd[w] * phi[i] * dA;
+        if (mc != 0.0)
+          for (int j = 0; j < nn; j++) JE(ri, oY + w * nn + j) += -mc * phi[i] * phi[j] * dA;
         for (int j = 0; j < nn; j++) {
           double vgj = 0.0, gij = 0.0;
           for (int pp = 0; pp < dim; pp++) {
@@ -649,6 +679,11 @@ static int fill_elements(const orc_problem *p, const double *x, double *R, doubl
   free(Re);
   free(Je);
   return status;
+}
+
+void orc_set_transient(orc_problem *p, const double *xdot, double mass_c) {
+  p->xdot = xdot;
+  p->mass_c = mass_c;
 }
 
 int orc_matrix_fill(const orc_problem *p, const double *x, double *R, double *a, int e0, int e1) {
@@ -802,7 +837,11 @@ static int band_solve(int N, const int *ija, const double *a, double *xb) {
  * assemble, row-sum scale, converged when after at least one update the
  * scaled residual has L2 and L-infinity norms below tol (:1482-1486),
  * otherwise solve and take the full step x -= dx (:2553-2557). */
-int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *norms) {
+/* Newton with the banded direct solve; with xdot (transient) the time
+ * derivative follows every update, xdot -= (1 + 2 theta) / dt * dx
+ * (src/mm_sol_nonlinear.c:2553-2562). */
+static int newton_impl(const orc_problem *p, double *x, double *xdot, int max_it, double tol,
+                       double *norms) {
   const int N = p->N;
   double *R = (double *)malloc(sizeof(double) * (size_t)N);
   double *a = (double *)malloc(sizeof(double) * (size_t)p->msr_len);
@@ -827,11 +866,25 @@ int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *
     }
     if (band_solve(N, p->ija, a, R) != 0) break;
     for (int i = 0; i < N; i++) x[i] -= R[i];
+    if (xdot)
+      for (int i = 0; i < N; i++) xdot[i] -= p->mass_c * R[i];
   }
   free(R);
   free(a);
   free(sc);
   return result;
+}
+
+int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *norms) {
+  return newton_impl(p, x, NULL, max_it, tol, norms);
+}
+
+int orc_newton_transient(orc_problem *p, double *x, double *xdot, double mass_c, int max_it,
+                         double tol, double *norms) {
+  orc_set_transient(p, xdot, mass_c);
+  const int r = newton_impl(p, x, xdot, max_it, tol, norms);
+  orc_set_transient(p, NULL, 0.0);
+  return r;
 }
 
 /* y = A x for an MSR matrix (src/sl_auxutil.c:373, MV_MSR). */

@@ -69,6 +69,13 @@ int orc_ilu0(const orc_problem *p, const double *a, double tau, double *lu);
  * iterations (>= 0) on convergence, -1 on failure.  norms (optional) gets
  * the scaled-residual L2 norm of every iteration (max_it entries). */
 int orc_newton(const orc_problem *p, double *x, int max_it, double tol, double *norms);
+/* Transient terms of later fills: the time derivative xdot (N values, NULL
+ * for steady) and the mass coefficient (1 + 2 theta) / delta_t. */
+void orc_set_transient(orc_problem *p, const double *xdot, double mass_c);
+/* orc_newton for one time step: xdot follows every update
+ * (xdot -= mass_c dx); the transient terms are cleared on return. */
+int orc_newton_transient(orc_problem *p, double *x, double *xdot, double mass_c, int max_it,
+                         double tol, double *norms);
 /* Restarted right-preconditioned GMRES(m) with the ILU(0) factors lu (from
  * orc_ilu0) on the MSR system a x = b, from x = 0, until the residual is
  * below tol * |b| or maxit iterations.  Returns 0 when converged, 1 when

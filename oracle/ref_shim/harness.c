@@ -9,7 +9,11 @@
  *   GB_REF_DUMP   path prefix; the first assembly writes <prefix>.ija
  *                 (int32, MSR bindx), <prefix>.a (float64, MSR values),
  *                 <prefix>.R and <prefix>.x (float64, length N)
+ *   GB_REF_XDOT_IN  raw float64 file; when set, xdot[] is replaced by it
+ *                 before the first assembly (a seeded time derivative)
  *   GB_REF_EXIT   when set, exit(0) right after that first dump
+ * A transient first assembly also writes <prefix>.xdot (float64, N) and
+ * <prefix>.dt (float64: delta_t, theta). 
  * With -Wl,--wrap=numerical_jacobian the reference's Jacobian checker
  * (src/mm_numjac.c:716, run when the deck sets Debug = -1/-2/-3) also gets
  * the GB_REF_X_IN state before it copies x, so its perturbed states are
@@ -87,6 +91,8 @@ int __wrap_matrix_fill_full(struct GomaLinearSolverData *ams, double x[], double
   const int N = ams->npu;
   const char *xin = getenv("GB_REF_X_IN");
   if (xin && g_calls == 0) read_x_in(xin, x, N);
+  const char *xdin = getenv("GB_REF_XDOT_IN");
+  if (xdin && g_calls == 0 && xdot) read_x_in(xdin, xdot, N);
   int err = __real_matrix_fill_full(ams, x, resid_vector, x_old, x_older, xdot, xdot_old,
                                     x_update, ptr_delta_t, ptr_theta, first_elem_side_BC_array,
                                     ptr_time_value, exo, dpi, ptr_num_total_nodes,
@@ -98,6 +104,11 @@ int __wrap_matrix_fill_full(struct GomaLinearSolverData *ams, double x[], double
     dump(prefix, "a", ams->val, sizeof(double), (size_t)len);
     dump(prefix, "R", resid_vector, sizeof(double), (size_t)N);
     dump(prefix, "x", x, sizeof(double), (size_t)N);
+    if (xdot && ptr_delta_t && ptr_theta) {
+      const double dt[2] = {*ptr_delta_t, *ptr_theta};
+      dump(prefix, "xdot", xdot, sizeof(double), (size_t)N);
+      dump(prefix, "dt", dt, sizeof(double), 2);
+    }
     fprintf(stderr, "harness: dumped N=%d msr_len=%d err=%d\n", N, len, err);
     if (getenv("GB_REF_EXIT")) exit(0);
   }

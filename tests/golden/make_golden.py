@@ -75,6 +75,33 @@ CASES = {
     "cav2d_32x32_solve": dict(mesh="quad9 32 32 1 1", phys="ns", rho=100.0,
                               visc=("newtonian", 1.0), bc="cavity2d", datum=True, mode="solve",
                               tol=1e-10, compact=True),
+    # transient: the first assembly of a time step (backward Euler, the
+    # reference's first step) at a seeded state and time derivative, and a
+    # fixed-step run from rest: three backward-Euler steps, then the deck's
+    # Crank-Nicolson (theta 0.5) with its second-order predictor
+    "cav2d_3x2_pert_transient": dict(mesh="quad9 3 2 1.5 1 0.15 7", phys="ns", rho=100.0,
+                                     visc=("newtonian", 1.0), bc="cavity2d", datum=True,
+                                     mode="assemble", seed=12,
+                                     transient=dict(dt=0.05, steps=1, theta=0.5)),
+    "box3d_2x2x2_bouss_transient": dict(mesh="hex27 2 2 2 1 1 1 0.1 5", phys="nst", rho=1.0,
+                                        visc=("newtonian", 0.71), bc="cube_heated",
+                                        datum=True, mode="assemble", seed=13, ra_pr=71000.0,
+                                        transient=dict(dt=0.01, steps=1, theta=0.5)),
+    "box3d_2x2x2_species_transient": dict(mesh="hex27 2 2 2 1 1 1 0.1 13", phys="nsty",
+                                          rho=1.0, visc=("newtonian", 0.71),
+                                          bc="cube_species", datum=True, mode="assemble",
+                                          seed=14, ra_pr=710.0, nspec=2, diff=(0.05, 0.02),
+                                          arrhenius=(3.0, 1.5), T_range=(1.0, 2.0),
+                                          transient=dict(dt=0.02, steps=1, theta=0.5)),
+    "cav2d_8x8_transient": dict(mesh="quad9 8 8 1 1", phys="ns", rho=100.0,
+                                visc=("newtonian", 1.0), bc="cavity2d", datum=True,
+                                mode="transient", tol=1e-12,
+                                transient=dict(dt=0.02, steps=6, theta=0.5)),
+    "box3d_2x2x2_bouss_transient_run": dict(mesh="hex27 2 2 2 1 1 1", phys="nst", rho=1.0,
+                                            visc=("newtonian", 0.71), bc="cube_heated",
+                                            datum=True, mode="transient", tol=1e-12,
+                                            ra_pr=7100.0,
+                                            transient=dict(dt=0.01, steps=5, theta=0.5)),
 }
 
 COMPACT_ROWS = 300  # Jacobian rows kept by a compact record
@@ -91,6 +118,23 @@ BCS = {
     "cube_species": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
     + [("T", 1, 2.0), ("T", 2, 1.0), ("Y0", 1, 1.0), ("Y1", 1, 0.0)],
 }
+
+
+def time_cards(case):
+    """Steady, or a fixed step (a negative delta_t keeps it constant,
+    src/rf_solve.c:1153-1158) with the deck's time-step parameter theta."""
+    tr = case.get("transient")
+    if not tr:
+        return ["Time integration = steady"]
+    return ["Time integration = transient",
+            "delta_t = %.17g" % (-tr["dt"]),
+            "Maximum number of time steps = %d" % tr["steps"],
+            "Maximum time = 1000.",
+            "Minimum time step = 1.e-9",
+            "Maximum time step = 10.",
+            "Time step parameter = %.17g" % tr["theta"],
+            "Time step error = 0.01 1 1 1 1 1 1 1",
+            "Printing Frequency = 1"]
 
 
 def deck_text(case):
@@ -110,7 +154,7 @@ def deck_text(case):
         "Initial Guess = zero",
         "",
         "Time Integration Specifications",
-        "Time integration = steady",
+    ] + time_cards(case) + [
         "",
         "Solver Specifications",
         "Solution Algorithm = lu",
@@ -143,12 +187,14 @@ def deck_text(case):
         "Number of bulk species = %d" % case.get("nspec", 0),
         "Number of EQ = -1",
     ]
+    # the first term multiplier is the mass (time-derivative) term's
+    mass = "1." if case.get("transient") else "0."
     for a in range(dim):
-        lines.append("EQ = momentum%d Q2 U%d Q2 0. 1. 1. 1. 1. 0." % (a + 1, a + 1))
+        lines.append("EQ = momentum%d Q2 U%d Q2 %s 1. 1. 1. 1. 0." % (a + 1, a + 1, mass))
     if case["phys"] in ("nst", "nsty"):
-        lines.append("EQ = energy Q2 T Q2 0. 1. 1. 1. 1.")
+        lines.append("EQ = energy Q2 T Q2 %s 1. 1. 1. 1." % mass)
     if case["phys"] == "nsty":
-        lines.append("EQ = species_bulk Q2 Y Q2 0. 1. 1. 1. 1.")
+        lines.append("EQ = species_bulk Q2 Y Q2 %s 1. 1. 1. 1." % mass)
     lines += ["EQ = continuity P1 P P1 1. 0.", "END OF EQ", "END OF MAT", "",
               "Post Processing Specifications", ""]
     # the BC count line must match what was written
@@ -247,10 +293,18 @@ def run_case(name, case, outdir):
                 x[temperature_unknowns(case)] = rng.uniform(lo, hi, len(temperature_unknowns(case)))
             x.astype("<f8").tofile(os.path.join(tmp, "xin.bin"))
             env2 = dict(env1, GB_REF_X_IN=os.path.join(tmp, "xin.bin"))
+            if case.get("transient"):
+                xd = rng.uniform(-1.0, 1.0, n)
+                xd.astype("<f8").tofile(os.path.join(tmp, "xdin.bin"))
+                env2["GB_REF_XDOT_IN"] = os.path.join(tmp, "xdin.bin")
             subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env2, check=True,
                            stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
             rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
             assert np.array_equal(rec["x"], x)
+            if case.get("transient"):
+                rec["xdot"] = np.fromfile(os.path.join(tmp, "d.xdot"))
+                assert np.array_equal(rec["xdot"], xd)
+                rec["delta_t_theta"] = np.fromfile(os.path.join(tmp, "d.dt"))
         else:
             if "T0" in case:
                 # initial guess: Dirichlet values, T0 at the other temperatures
@@ -267,15 +321,29 @@ def run_case(name, case, outdir):
                 rec["x0"] = x0
             p = subprocess.run([GOMA, "-i", "input"], cwd=tmp, env=env, check=True,
                                stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
-            if "converged SS!" not in p.stdout:
+            steady = case["mode"] == "solve"
+            if steady and "converged SS!" not in p.stdout:
                 raise RuntimeError("%s: reference Newton did not converge:\n%s" % (name, p.stdout[-3000:]))
-            vals = []
+            # the solution file: one block per printed step ("time = t"
+            # first in a transient run)
+            blocks, times = [[]], []
             with open(os.path.join(tmp, "soln.dat")) as f:
                 for line in f:
                     parts = line.split()
-                    if parts and parts[0][0] in "-0123456789":
-                        vals.append(float(parts[0]))
-            rec["x_converged"] = np.array(vals)
+                    if parts and parts[0] == "time":
+                        if blocks[-1]:
+                            blocks.append([])
+                        times.append(float(parts[2]))
+                    elif parts and parts[0][0] in "-0123456789":
+                        blocks[-1].append(float(parts[0]))
+            if steady:
+                rec["x_converged"] = np.array(blocks[0])
+            else:
+                rec["x_steps"] = np.array(blocks)
+                rec["times"] = np.array(times)
+                if len(blocks) != case["transient"]["steps"]:
+                    raise RuntimeError("%s: %d of %d time steps written:\n%s" % (
+                        name, len(blocks), case["transient"]["steps"], p.stdout[-3000:]))
             rec["newton_log"] = "\n".join(l for l in p.stdout.splitlines() if "]" in l[:14])
             rec["x"] = np.fromfile(os.path.join(tmp, "d.x"))
         ija = np.fromfile(os.path.join(tmp, "d.ija"), dtype="<i4")

@@ -11,16 +11,20 @@ from goma_gb300 import problem as pb
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names(mode=None, compact=False):
-    """Golden case names (of one mode); compact=True lists the compact
-    records of large cases (sampled Jacobian rows, pattern hash) instead of
-    the full ones."""
+def names(mode=None, compact=False, transient=False):
+    """Golden case names (of one mode: assemble, solve, transient);
+    compact=True lists the compact records of large cases (sampled Jacobian
+    rows, pattern hash) instead of the full ones; transient=True the
+    assemblies with time-derivative terms instead of the steady ones."""
     out = []
     for f in sorted(os.listdir(GOLDEN)):
         if f.endswith(".npz"):
             n = f[:-4]
             case = load(n)[1]
-            if (mode is None or case["mode"] == mode) and bool(case.get("compact")) == compact:
+            if mode is None and case["mode"] == "transient" and not transient:
+                continue
+            if ((mode is None or case["mode"] == mode) and bool(case.get("compact")) == compact
+                    and bool(case.get("transient")) == (transient or case["mode"] == "transient")):
                 out.append(n)
     return out
 

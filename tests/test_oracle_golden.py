@@ -61,6 +61,36 @@ def test_oracle_newton_matches_reference_at_benchmark_size(name):
     assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
 
 
+@pytest.mark.parametrize("name", gc.names("assemble", transient=True))
+def test_oracle_transient_assembly_matches_reference(name):
+    """The first assembly of a time step with a seeded state and time
+    derivative: mass terms of xdot in R, their (1 + 2 theta) / dt sensitivity
+    in J (momentum, energy, species)."""
+    g, case = gc.load(name)
+    o = oracle.Oracle(gc.problem_from_case(case))
+    assert np.array_equal(o.ija(), g["ija"])
+    dt, theta = g["delta_t_theta"]
+    R, a, st = o.matrix_fill(g["x"], xdot=g["xdot"], delta_t=dt, theta=theta)
+    assert st == 0
+    assert gc.msr_row_scaled_error(g["ija"], a, g["a"]) < TOL_RJ
+    assert np.abs(R - g["R"]).max() <= TOL_RJ * np.abs(g["R"]).max()
+
+
+@pytest.mark.parametrize("name", gc.names("transient"))
+def test_oracle_transient_run_matches_reference(name):
+    """The reference's fixed-step time loop from rest: three backward-Euler
+    steps, then Crank-Nicolson with its second-order predictor; the solution
+    after every step."""
+    g, case = gc.load(name)
+    tr = case["transient"]
+    o = oracle.Oracle(gc.problem_from_case(case))
+    xs = o.transient_run(np.zeros(o.N), tr["steps"], tr["dt"], tr["theta"], tol=case["tol"])
+    ref = g["x_steps"]
+    assert len(xs) == len(ref)
+    for k, (x, xr) in enumerate(zip(xs, ref)):
+        assert np.abs(x - xr).max() <= TOL_X * np.abs(xr).max(), k
+
+
 def test_oracle_mesh_generator_matches_package():
     from goma_gb300.problem import mesh_from_spec
     for spec in ["quad9 3 2 1.5 1 0.15 7", "hex27 2 1 3 1 0.5 1.5 0.12 9", "quad9 5 4 2 1"]:
