@@ -171,22 +171,6 @@ class Oracle:
         return out
 
 
-def predict(dt, dt_old, dt_older, theta, x_old, x_older, x_oldest, xd_old, xd_older):
-    """predict_solution (src/rf_solve.c:2767-2834): the trapezoid rule's
-    second-order extrapolation for theta = 0.5, else the first-order one;
-    xdot consistent with the predicted x."""
-    if theta == 0.5:
-        c1 = dt * (dt + dt_old) / dt_older / (dt_older + dt_old)
-        c2 = -dt * (dt + dt_old + dt_older) / (dt_old * dt_older)
-        c3 = (dt + dt_old + dt_older) * (dt + dt_old) / dt_old / (dt_older + dt_old)
-        x = c3 * x_old + c2 * x_older + c1 * x_oldest
-    else:
-        c1 = dt * (1.0 + theta * dt / dt_old)
-        c2 = theta * dt * dt / dt_old
-        x = x_old + c1 * xd_old - c2 * xd_older
-    xd = (1.0 + 2.0 * theta) / dt * (x - x_old) - 2.0 * theta * xd_old
-    return x, xd
-
     def element(self, e, x, apply_bc=True):
         x = np.ascontiguousarray(x, np.float64)
         Re = np.zeros(self.nloc)
@@ -328,3 +312,20 @@ def mesh_from_spec(spec):
         sets.append(nodes[off:off + n].copy())
         off += n
     return coords, conn, sets
+
+
+def predict(dt, dt_old, dt_older, theta, x_old, x_older, x_oldest, xd_old, xd_older):
+    """predict_solution (src/rf_solve.c:2767-2834): the trapezoid rule's
+    second-order extrapolation for theta = 0.5, else the first-order one;
+    xdot consistent with the predicted x."""
+    if theta == 0.5:
+        c1 = dt * (dt + dt_old) / dt_older / (dt_older + dt_old)
+        c2 = -dt * (dt + dt_old + dt_older) / (dt_old * dt_older)
+        c3 = (dt + dt_old + dt_older) * (dt + dt_old) / dt_old / (dt_older + dt_old)
+        x = c3 * x_old + c2 * x_older + c1 * x_oldest
+    else:
+        c1 = dt * (1.0 + theta * dt / dt_old)
+        c2 = theta * dt * dt / dt_old
+        x = x_old + c1 * xd_old - c2 * xd_older
+    xd = (1.0 + 2.0 * theta) / dt * (x - x_old) - 2.0 * theta * xd_old
+    return x, xd
