@@ -64,6 +64,17 @@ def load():
         "gb_msr_pattern_host": (ctypes.c_int, [vp, ip, llp]),
         "gb_csr_pattern": (ctypes.c_int, [vp, llp, ip]),
         "gb_csr_row": (ctypes.c_longlong, [vp, vp, ctypes.c_int, llp, ip, dp, ctypes.c_longlong]),
+        "gb_matrix_fill_full_transient": (ctypes.c_int, [vp, dp, dp, ctypes.c_double,
+                                                         ctypes.c_double, dp, dp]),
+        "gb_matrix_fill_full_transient_device": (ctypes.c_int, [vp, vp, vp, ctypes.c_double,
+                                                                ctypes.c_double, vp, vp, vp]),
+        "gb_solve_nonlinear_problem_transient": (ctypes.c_int, [vp, dp, dp, ctypes.c_double,
+                                                                ctypes.c_double,
+                                                                ctypes.POINTER(NewtonOpts), ip,
+                                                                ctypes.POINTER(NewtonStats)]),
+        "gb_solve_transient": (ctypes.c_int, [vp, dp, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_double, ctypes.POINTER(NewtonOpts), dp,
+                                              ctypes.POINTER(NewtonStats), ip]),
         "gb_first_unknown": (ctypes.c_int, [vp, ip]),
         "gb_dirichlet_init": (ctypes.c_int, [vp, dp]),
         "gb_matrix_fill_full": (ctypes.c_int, [vp, dp, dp, dp]),

@@ -52,6 +52,10 @@ struct ElemSmem {
   double U[Q2<DIM>::NN][DIM];
   double Tn[Q2<DIM>::NN];
   double Pn[Q2<DIM>::NP];
+  double Ud[Q2<DIM>::NN][DIM];  // nodal time derivatives (transient)
+  double Tdn[Q2<DIM>::NN];
+  double vd[Q2<DIM>::NQ][DIM];  // the same at the quadrature points
+  double Td[Q2<DIM>::NQ];
   int nodes[Q2<DIM>::NN];
   int e;
   double rho;  // density of this element
@@ -97,6 +101,11 @@ __global__ void __launch_bounds__(256)
     if (ENERGY) E.Tn[k] = A.x[f0 + DIM];
     if (k == C::CENT)
       for (int l = 0; l < NP; l++) E.Pn[l] = A.x[f0 + A.pofs + l];
+    if (A.xdot) {
+#pragma unroll
+      for (int j = 0; j < DIM; j++) E.Ud[k][j] = A.xdot[f0 + j];
+      E.Tdn[k] = ENERGY ? A.xdot[f0 + DIM] : 0.0;
+    }
   }
   __syncthreads();
 
@@ -107,6 +116,20 @@ __global__ void __launch_bounds__(256)
     Elem &E = S[s];
     qp_setup<DIM, ENERGY, CARREAU>(E.X, E.U, E.Tn, E.Pn, q, tab_phi, tab_dphi, A.tab_w, A.tab_pt,
                                    M, E.rho, E.qp[q]);
+    if (A.xdot) {  // v_dot and T_dot at the point (load_fv's fv_dot)
+      double vd[DIM], Td = 0.0;
+#pragma unroll
+      for (int a = 0; a < DIM; a++) vd[a] = 0.0;
+      for (int k = 0; k < NN; k++) {
+        const double ph = tab_phi[q * NN + k];
+#pragma unroll
+        for (int a = 0; a < DIM; a++) vd[a] = fma(ph, E.Ud[k][a], vd[a]);
+        if (ENERGY) Td = fma(ph, E.Tdn[k], Td);
+      }
+#pragma unroll
+      for (int a = 0; a < DIM; a++) E.vd[q][a] = vd[a];
+      E.Td[q] = Td;
+    }
   }
   __syncthreads();
 
@@ -195,7 +218,9 @@ __global__ void __launch_bounds__(256)
         dif = fma(Wi.g[p], (p == ra ? -Q.P : 0.0) + Q.mu * Q.gam[ra][p], dif);
       dif *= -dA;
       const double src = Q.f[ra] * (Wi.phi * dA);
-      Racc += adv + dif + src;
+      // mass term -rho v_dot_a phi_i dA (src/mm_fill_momentum.c:471-500)
+      const double mass = A.xdot ? -E.rho * E.vd[q][ra] * (Wi.phi * dA) : 0.0;
+      Racc += mass + adv + dif + src;
       if (JAC) {
 #pragma unroll
         for (int l = 0; l < NP; l++) JmP[l] = fma(Wi.g[ra] * Q.psi[l], dA, JmP[l]);
@@ -208,7 +233,9 @@ __global__ void __launch_bounds__(256)
         vgT = fma(Q.v[p], Q.gT[p], vgT);
         dif = fma(Wi.g[p], -M.conductivity * Q.gT[p], dif);
       }
-      Racc += vgT * (-Wi.phi * E.rho * M.heat_capacity * dA) + dif * dA;
+      // with the mass term -rho Cp T_dot phi_i dA (src/mm_fill_energy.c:315-381)
+      const double Tt = A.xdot ? vgT + E.Td[q] : vgT;
+      Racc += Tt * (-Wi.phi * E.rho * M.heat_capacity * dA) + dif * dA;
     } else if (own_c) {
       double divv = 0.0;
 #pragma unroll
@@ -223,6 +250,9 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int b = 0; b < DIM; b++) ti[b] = nmu * Wi.g[b];
     const double nkdA = -M.conductivity * dA;
+    // the mass terms' sensitivity -(1 + 2 theta) / dt rho phi_i phi_j dA
+    // (src/mm_fill_momentum.c:1586-1590), times Cp on the energy rows
+    const double nmc = -A.mass_c * E.rho;
 #pragma unroll
     for (int m = 0; m < PPT; m++) {
       const int pj = pj0 + m * (NN / PPT);
@@ -232,7 +262,7 @@ __global__ void __launch_bounds__(256)
       for (int p = 0; p < DIM; p++) dot = fma(Wi.g[p], Wj.g[p], dot);
       const double pij = Wi.phi * Wj.phi * dA;
       const double prho = -E.rho * pij;
-      const double K = fma(Wi.phi, Wj.cK, nmu * dot);
+      const double K = fma(nmc, pij, fma(Wi.phi, Wj.cK, nmu * dot));
 #pragma unroll
       for (int a = 0; a < DIM; a++)
 #pragma unroll
@@ -243,7 +273,7 @@ __global__ void __launch_bounds__(256)
           Jv[m][a][b] += val;
         }
       if (ENERGY) {
-        JTT[m] += fma(Wi.phi, Wj.cT, nkdA * dot);
+        JTT[m] += fma(nmc * M.heat_capacity, pij, fma(Wi.phi, Wj.cT, nkdA * dot));
         const double pc = -E.rho * M.heat_capacity * pij;
 #pragma unroll
         for (int b = 0; b < DIM; b++) {

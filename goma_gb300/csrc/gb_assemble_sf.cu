@@ -78,6 +78,7 @@ struct Smem {
       double A[NF][2][NN];
       double B[NF][3][NN];
       double F[NF][4][NQ]; // value, d/dxi_1..3 at the points
+      double Xd[4][NN];    // u v w T time derivatives at the nodes (transient)
     } iso;
   } X;
   double Pn[NP];
@@ -127,6 +128,11 @@ __global__ void __launch_bounds__(256, 2)
       S.X.iso.Xn[6][L] = ENERGY ? A.x[f0 + DIM] : 0.0;
       if (k == CENT)
         for (int l = 0; l < NP; l++) S.Pn[l] = A.x[f0 + A.pofs + l];
+      if (A.xdot) {
+#pragma unroll
+        for (int j = 0; j < DIM; j++) S.X.iso.Xd[j][L] = A.xdot[f0 + j];
+        S.X.iso.Xd[3][L] = ENERGY ? A.xdot[f0 + DIM] : 0.0;
+      }
     }
     __syncthreads();
     // ---- values and reference gradients at the points: three passes
@@ -211,6 +217,14 @@ __global__ void __launch_bounds__(256, 2)
         for (int l = 0; l < NP; l++) P = fma(S.Pn[l], psi[l], P);
         const double mu = M.viscosity, rho = rho_e;
         const double divv = gv[0][0] + gv[1][1] + gv[2][2];
+        // time derivatives at the point (transient; load_fv's fv_dot)
+        double vd[4] = {0.0, 0.0, 0.0, 0.0};
+        if (A.xdot)
+          for (int L = 0; L < NN; L++) {
+            const double ph = S.phi[q][L];
+#pragma unroll
+            for (int c = 0; c < 4; c++) vd[c] = fma(ph, S.X.iso.Xd[c][L], vd[c]);
+          }
 #pragma unroll
         for (int l = 0; l < NP; l++) {
           S.psidA[l][q] = psi[l] * dA;
@@ -226,14 +240,15 @@ __global__ void __launch_bounds__(256, 2)
           if (M.source_model == GB_SOURCE_BOUSSINESQ)
             f = ENERGY ? rho * M.source[a] * (-M.beta * (T - M.Tref)) : 0.0;
           const double adv = v[0] * gv[0][a] + v[1] * gv[1][a] + v[2] * gv[2][a];
-          S.cR[a][q] = dA * (f - rho * adv);
+          // with the mass term -rho v_dot_a (src/mm_fill_momentum.c:471-500)
+          S.cR[a][q] = dA * (f - rho * (adv + vd[a]));
 #pragma unroll
           for (int p = 0; p < 3; p++)
             S.tR[p][a][q] = -dA * ((p == a ? -P : 0.0) + mu * (gv[a][p] + gv[p][a]));
         }
         S.W[C_DA][q] = dA;
         S.cR[3][q] = ENERGY ? -rho * M.heat_capacity * dA *
-                                  (v[0] * gT[0] + v[1] * gT[1] + v[2] * gT[2])
+                                  (v[0] * gT[0] + v[1] * gT[1] + v[2] * gT[2] + vd[3])
                             : 0.0;
 #pragma unroll
         for (int p = 0; p < 3; p++) S.tR[p][3][q] = ENERGY ? -M.conductivity * dA * gT[p] : 0.0;
@@ -393,11 +408,15 @@ __global__ void __launch_bounds__(256, 2)
         };
         const double S1 = stage3(C_S1) + stage3(C_S1 + 1) + stage3(C_S1 + 2);
         const double trH = h(Li, Lj) + h(NN + Li, NN + Lj) + h(2 * NN + Li, 2 * NN + Lj);
-        const double D = fma(-mu, trH, S1);
         const int ni = S.nodes[ki];
         const int fi = A.fu[ni];
         const int nb = A.nbr_ptr[ni] + ns[ki * NN + kj];
-        const double mdA = ENERGY ? stage3(C_DA) : 0.0;
+        const bool tr = A.mass_c != 0.0;
+        const double mdA = (ENERGY || tr) ? stage3(C_DA) : 0.0;
+        // the mass terms' sensitivity -(1 + 2 theta) / dt rho M(dA)
+        // (src/mm_fill_momentum.c:1586-1590), times Cp on the energy row
+        const double Mt = tr ? -A.mass_c * rho_e * mdA : 0.0;
+        const double D = fma(-mu, trH, S1) + Mt;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
           const int gr = fi + a;
@@ -417,7 +436,7 @@ __global__ void __launch_bounds__(256, 2)
             double *row = A.vals + A.rowptr[gr] + A.nbr_offT[nb];
 #pragma unroll
             for (int b = 0; b < 3; b++) atomicAdd(row + b, stage3(C_TV + b));
-            atomicAdd(row + DIM, fma(Cp, S1, -kc * trH));
+            atomicAdd(row + DIM, fma(Cp, S1 + Mt, -kc * trH));
           }
         }
       }

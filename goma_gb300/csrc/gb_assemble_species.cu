@@ -1,6 +1,6 @@
 // Species rows of the element residual and analytic Jacobian (dilute
-// species, Galerkin, steady), in FP64 on sm_103a, with the coloured CSR
-// scatter.
+// species, Galerkin; steady, or with the time-derivative terms of a
+// transient step), in FP64 on sm_103a, with the coloured CSR scatter.
 //
 // Replaces, for these rows, assemble_mass_transport
 // (src/mm_fill_species.c:194) with get_continuous_species_terms (:9739),
@@ -45,6 +45,7 @@ struct QPs {
   double v[DIM];
   double gY[MS][DIM];
   double S[MS], dSdT[MS], dSdY[MS][MS];
+  double Yd[MS];  // time derivatives (transient)
 };
 
 template <int DIM>
@@ -60,6 +61,7 @@ struct Elem {
   double U[Q2<DIM>::NN][DIM];
   double Tn[Q2<DIM>::NN];
   double Yn[MS][Q2<DIM>::NN];
+  double Ydn[MS][Q2<DIM>::NN];  // nodal time derivatives (transient)
   int nodes[Q2<DIM>::NN];
   int e;
   QPs<DIM> qp[Q2<DIM>::NQ];
@@ -105,6 +107,7 @@ __global__ void __launch_bounds__(256)
     }
     E.Tn[k] = ENERGY ? A.x[f0 + DIM] : 0.0;
     for (int w = 0; w < ns; w++) E.Yn[w][k] = A.x[f0 + OY + w];
+    for (int w = 0; w < ns; w++) E.Ydn[w][k] = A.xdot ? A.xdot[f0 + OY + w] : 0.0;
   }
   __syncthreads();
 
@@ -205,6 +208,10 @@ __global__ void __launch_bounds__(256)
       }
       Q.S[w] = Sw;
       Q.dSdT[w] = dT;
+      double yd = 0.0;
+      if (A.xdot)
+        for (int k = 0; k < NN; k++) yd = fma(tab_phi[q * NN + k], E.Ydn[w][k], yd);
+      Q.Yd[w] = yd;
     }
   }
   __syncthreads();
@@ -253,7 +260,9 @@ __global__ void __launch_bounds__(256)
         vgY = fma(Q.v[p], Q.gY[w][p], vgY);
         dif = fma(Wi.g[p], nD * Q.gY[w][p], dif);
       }
-      Racc += (-vgY * Wi.phi + dif + Q.S[w] * Wi.phi) * Q.dA;
+      // with the mass term -Y_dot_w phi_i dA (coeff_rho = 1,
+      // src/mm_fill_species.c:525-551)
+      Racc += (-(vgY + Q.Yd[w]) * Wi.phi + dif + Q.S[w] * Wi.phi) * Q.dA;
     }
     const int node = nodes[i];
     const int gr = A.fu[node] + OY + w;
@@ -303,7 +312,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int p = 0; p < DIM; p++) dot = fma(Wi.g[p], Wj.g[p], dot);
         const double pij = Wi.phi * Wj.phi * dA;
-        const double diag = fma(-Wi.phi, Wj.vg, nD * dot) * dA;
+        // with the mass term's sensitivity -(1 + 2 theta) / dt phi_i phi_j dA
+        const double diag = fma(-Wi.phi, Wj.vg, nD * dot) * dA - A.mass_c * pij;
 #pragma unroll
         for (int w1 = 0; w1 < MS; w1++)
           JYY[m][w1] = fma(dSdY[w1], pij, JYY[m][w1] + (w1 == w ? diag : 0.0));

@@ -229,6 +229,8 @@ AsmArgs Context::args(const double *x, double *R, double *vals) const {
   a.status = d_status;
   a.elem_rho = d_elem_rho;
   a.pofs = L.nvn;
+  a.xdot = d_xdot;
+  a.mass_c = d_xdot ? mass_c : 0.0;
   a.mat = mat;
   return a;
 }
@@ -283,8 +285,9 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
 int Context::kernel_path(bool jacobian) const {
   if (L.dim != 3) return 1;
   const bool gemm_ok = !carreau && mat.viscosity > 0.0;
-  // per-element densities: the scalar and the sum-factorised kernels only
-  if (d_elem_rho) return gemm_ok && path != 1 ? 4 : 1;
+  // per-element densities and transient terms: the scalar and the
+  // sum-factorised kernels only
+  if (d_elem_rho || d_xdot) return gemm_ok && path != 1 ? 4 : 1;
   if (path == 0) return gemm_ok ? 4 : 1;
   if (path == 3 || path == 4) return gemm_ok ? path : 1;
   return jacobian ? path : 1;

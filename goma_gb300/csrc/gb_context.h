@@ -4,6 +4,7 @@
 
 #include <string>
 
+#include "../../include/gb_newton.h"
 #include "gb_device.h"
 #include "gb_layout.h"
 #include "gb_solve.h"
@@ -50,6 +51,10 @@ struct Context {
   double *d_x = nullptr, *d_R = nullptr, *d_vals = nullptr;
   int *d_status = nullptr;
   double *d_elem_rho = nullptr;  // per-element density (gb_set_element_density); NULL: none
+  // transient terms of later assemblies: device time derivative (N) and
+  // (1 + 2 theta) / delta_t; NULL / 0 when steady
+  const double *d_xdot = nullptr;
+  double mass_c = 0.0;
   double *d_msr = nullptr;
   std::unique_ptr<Solver> solver;
   // optional kernel timing of the element kernels (events on the launch stream)
@@ -70,6 +75,10 @@ struct Context {
   int kernel_path(bool jacobian) const;
   int to_msr_host(const double *vals, double *a_msr);
 };
+
+// Newton (gb_newton.cu); d_xdot != NULL: one transient step
+int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
+           gb_newton_stats *st, double *d_xdot, double mass_c);
 
 }  // namespace gb
 

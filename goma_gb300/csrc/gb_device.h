@@ -44,6 +44,10 @@ struct AsmArgs {
   const double *elem_rho;      // per-element density (overrides mat.density); NULL: none
   int pofs;                    // offset of the first P1 pressure at a centroid node
                                // (= nodal fields per node: dim + energy + species)
+  // transient terms: the time derivative (N; NULL: steady) and the mass
+  // coefficient (1 + 2 theta) / delta_t of its sensitivity
+  const double *xdot;
+  double mass_c;
   MaterialDev mat;
 };
 

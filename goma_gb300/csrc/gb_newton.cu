@@ -24,6 +24,18 @@ __global__ void update_kernel(int N, double damp, const double *__restrict__ dx,
     x[i] = fma(-damp, dx[i], x[i]);
 }
 
+// the transient update: x -= damp dx and xdot -= damp (1 + 2 theta) / dt dx
+// (src/mm_sol_nonlinear.c:2553-2562)
+__global__ void update_transient_kernel(int N, double damp, double mass_c,
+                                        const double *__restrict__ dx, double *__restrict__ x,
+                                        double *__restrict__ xdot) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double d = damp * dx[i];
+    x[i] -= d;
+    xdot[i] = fma(-mass_c, d, xdot[i]);
+  }
+}
+
 // inverse of csr_to_msr: MSR values -> CSR values of this layout
 __global__ void msr_to_csr_kernel(int N, const int64_t *__restrict__ rowptr,
                                   const int *__restrict__ colidx, const double *__restrict__ msr,
@@ -59,10 +71,24 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// Newton from d_x.  With d_xdot (a transient step) the assemblies carry the
+// time-derivative terms of d_xdot with sensitivity mass_c = (1 + 2 theta) /
+// delta_t, and every update moves d_xdot with d_x.
 int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
-           gb_newton_stats *st) {
+           gb_newton_stats *st, double *d_xdot, double mass_c) {
   LinearOpts lo = linear_opts(o);
   if (ensure_solver(C, lo.krylov)) return -1;
+  struct TransientScope {  // the context's transient terms for this solve only
+    Context *C;
+    TransientScope(Context *c, const double *xd, double mc) : C(c) {
+      C->d_xdot = xd;
+      C->mass_c = xd ? mc : 0.0;
+    }
+    ~TransientScope() {
+      C->d_xdot = nullptr;
+      C->mass_c = 0.0;
+    }
+  } transient_scope(C, d_xdot, mass_c);
   const double tol_min = lo.tol;
   const double eta_max = o.forcing_max > 0 ? std::max(o.forcing_max, tol_min) : 1e-2;
   double eta = eta_max, prev_norm = -1.0;
@@ -157,7 +183,11 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
       rc = -1;
       break;
     }
-    update_kernel<<<304, 256, 0, s>>>(N, o.damping > 0 ? o.damping : 1.0, d_dx, d_x);
+    if (d_xdot)
+      update_transient_kernel<<<304, 256, 0, s>>>(N, o.damping > 0 ? o.damping : 1.0, mass_c,
+                                                  d_dx, d_x, d_xdot);
+    else
+      update_kernel<<<304, 256, 0, s>>>(N, o.damping > 0 ? o.damping : 1.0, d_dx, d_x);
     cudaEventRecord(ev[5], s);
     cudaEventSynchronize(ev[5]);
     S_.factor_ms += elapsed(ev[3], ev[4]);
@@ -221,7 +251,7 @@ int gb_solve_nonlinear_problem_device(gb_ctx *ctx, double *d_x, const gb_newton_
     o = *opts;
   else
     gb_newton_opts_default(&o);
-  return gb::newton(&ctx->c, d_x, o, converged, stats);
+  return gb::newton(&ctx->c, d_x, o, converged, stats, nullptr, 0.0);
 }
 
 int gb_solve_nonlinear_problem(gb_ctx *ctx, double *x, const gb_newton_opts *opts, int *converged,

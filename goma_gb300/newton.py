@@ -121,6 +121,50 @@ class GomaNewton:
                                                _dp(a) if a is not None else None))
         return R, a
 
+    def matrix_fill_full_transient(self, x, xdot, delta_t, theta, jacobian=True):
+        """Transient matrix_fill_full (host arrays): the mass terms of xdot
+        and their (1 + 2 theta) / delta_t sensitivity.  (R, a_msr or None)."""
+        x = np.ascontiguousarray(x, np.float64)
+        xdot = np.ascontiguousarray(xdot, np.float64)
+        R = np.empty(self.N)
+        a = np.empty(self.msr_len) if jacobian else None
+        _lib.check(self._L.gb_matrix_fill_full_transient(self.h, _dp(x), _dp(xdot),
+                                                         float(delta_t), float(theta), _dp(R),
+                                                         _dp(a) if a is not None else None))
+        return R, a
+
+    def solve_transient_step(self, x, xdot, delta_t, theta, **opts):
+        """One time step's Newton solve from the predicted (x, xdot):
+        (x, xdot, converged, stats dict)."""
+        x = np.ascontiguousarray(x, np.float64).copy()
+        xdot = np.ascontiguousarray(xdot, np.float64).copy()
+        o = self.newton_opts(**opts)
+        conv = ctypes.c_int()
+        st = _lib.NewtonStats()
+        _lib.check(self._L.gb_solve_nonlinear_problem_transient(
+            self.h, _dp(x), _dp(xdot), float(delta_t), float(theta), ctypes.byref(o),
+            ctypes.byref(conv), ctypes.byref(st)))
+        return x, xdot, bool(conv.value), _stats_dict(st)
+
+    def solve_transient(self, num_steps, delta_t, theta=0.5, x0=None, **opts):
+        """The reference's fixed-step time loop (gb_solve_transient) from x0
+        (Dirichlet values applied if None): backward Euler for three steps,
+        then theta.  Returns (solutions of every step [num_steps, N], stats
+        dict with the per-step converged norms)."""
+        x = self.dirichlet_init(np.zeros(self.N)) if x0 is None else np.ascontiguousarray(
+            x0, np.float64).copy()
+        xs = np.empty((num_steps, self.N))
+        o = self.newton_opts(**opts)
+        st = _lib.NewtonStats()
+        done = ctypes.c_int()
+        _lib.check(self._L.gb_solve_transient(self.h, _dp(x), int(num_steps), float(delta_t),
+                                              float(theta), ctypes.byref(o), _dp(xs),
+                                              ctypes.byref(st), ctypes.byref(done)))
+        d = _stats_dict(st)
+        d["steps_done"] = done.value
+        d["step_residual_l2"] = [st.residual_l2[k] for k in range(min(num_steps, 64))]
+        return xs, d
+
     def matrix_fill_full_device(self, d_x, d_R, d_vals, stream=None):
         """Device pointers; enqueued on ``stream`` (default: library stream)."""
         _lib.check(self._L.gb_matrix_fill_full_device(self.h, d_x, d_R, d_vals, stream))

@@ -89,6 +89,21 @@ int gb_matrix_fill_full(gb_ctx *ctx, const double *x, double *resid_vector, doub
  * status is checked at the next gb_status() call. */
 int gb_matrix_fill_full_device(gb_ctx *ctx, const double *d_x, double *d_R, double *d_vals,
                                void *stream);
+/* Transient form of matrix_fill_full (its x, xdot, delta_t and theta
+ * arguments, src/mm_fill.c:158-176): the residual gets the mass terms of the
+ * time derivative xdot (momentum -rho v_dot phi dA, energy -rho Cp T_dot phi
+ * dA, species -Y_dot phi dA; src/mm_fill_momentum.c:471-500,
+ * src/mm_fill_energy.c:315-381, src/mm_fill_species.c:525-551) and the
+ * Jacobian their sensitivity (1 + 2 theta) / delta_t (:1586-1590).  Host
+ * arrays as gb_matrix_fill_full; delta_t > 0, 0 <= theta <= 1. */
+int gb_matrix_fill_full_transient(gb_ctx *ctx, const double *x, const double *xdot,
+                                  double delta_t, double theta, double *resid_vector,
+                                  double *a_msr);
+/* Device form (as gb_matrix_fill_full_device), d_xdot N doubles on the
+ * device. */
+int gb_matrix_fill_full_transient_device(gb_ctx *ctx, const double *d_x, const double *d_xdot,
+                                         double delta_t, double theta, double *d_R,
+                                         double *d_vals, void *stream);
 /* Synchronises the library stream and reports the determinant status of
  * all assemblies since the previous call: returns -1 (with the first bad
  * element in the message) or 0. */
@@ -245,6 +260,31 @@ void gb_newton_opts_default(gb_newton_opts *o);
  * determinant, a non-finite residual, or a CUDA error. */
 int gb_solve_nonlinear_problem(gb_ctx *ctx, double *x, const gb_newton_opts *opts,
                                int *converged, gb_newton_stats *stats);
+/* One time step of solve_nonlinear_problem (src/mm_sol_nonlinear.c:596,
+ * transient arguments delta_t, theta, xdot): Newton from the predicted x
+ * and xdot (host, N doubles each, both overwritten), every assembly with
+ * the transient terms of gb_matrix_fill_full_transient, every update
+ * x -= damping dx with xdot -= damping (1 + 2 theta) / delta_t dx
+ * (:2553-2562). */
+int gb_solve_nonlinear_problem_transient(gb_ctx *ctx, double *x, double *xdot, double delta_t,
+                                         double theta, const gb_newton_opts *opts,
+                                         int *converged, gb_newton_stats *stats);
+/* Drop-in for the transient branch of solve_problem (src/rf_solve.c:
+ * 1138-2601) with a constant time step (a negative "delta_t" card,
+ * :1153-1158): from the initial state x (host, Dirichlet values set) with
+ * zero time derivatives, num_steps steps of delta_t -- backward Euler for
+ * the first three (:1375-1386), then the time-step parameter theta (0.5:
+ * Crank-Nicolson with the second-order predictor) -- each predicted by
+ * predict_solution (:2767) and solved by Newton to opts' tolerance.  x gets
+ * the last solution; x_steps (num_steps x N doubles, may be NULL) every
+ * step's; stats (may be NULL) the sums of the Newton and Krylov counts and
+ * times, with residual_l2[k] / residual_loo_steps[k] the converged step k's
+ * L2 / L-infinity norms; *steps_done (may be NULL) the steps completed.
+ * Returns -1 when a step does not converge (no step-size reduction) or on
+ * an error. */
+int gb_solve_transient(gb_ctx *ctx, double *x, int num_steps, double delta_t, double theta,
+                       const gb_newton_opts *opts, double *x_steps, gb_newton_stats *stats,
+                       int *steps_done);
 /* Same with x in device memory (N doubles); the iterate stays there. */
 int gb_solve_nonlinear_problem_device(gb_ctx *ctx, double *d_x, const gb_newton_opts *opts,
                                       int *converged, gb_newton_stats *stats);
