@@ -723,6 +723,8 @@ def main():
                          "(default: all)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
                     help="seconds per run of the time-to-solve leg (0: no limit)")
+    ap.add_argument("--solve-krylov", type=int, default=60,
+                    help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
                     help="Krylov iteration limit of one linear solve in the time-to-solve leg")
     ap.add_argument("--solve-reuse", type=int, default=0,
@@ -908,7 +910,7 @@ def main():
                 args.solve_nel, ilu_ordering=args.solve_ilu, reference_solver=args.solve_nel <= 8,
                 modes=[m for m in args.solve_modes.split(",") if m] or None,
                 budget_s=args.solve_budget or None, factorization_reuse=args.solve_reuse,
-                max_linear_its=args.solve_max_linear)
+                max_linear_its=args.solve_max_linear, krylov=args.solve_krylov)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:
