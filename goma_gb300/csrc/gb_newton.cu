@@ -50,7 +50,7 @@ __global__ void msr_to_csr_kernel(int N, const int64_t *__restrict__ rowptr,
 
 static LinearOpts linear_opts(const gb_newton_opts &o) {
   LinearOpts l;
-  l.krylov = o.krylov_dim > 0 ? o.krylov_dim : 30;
+  l.krylov = o.krylov_dim > 0 ? (o.krylov_dim < 1023 ? o.krylov_dim : 1023) : 30;
   l.maxit = o.max_linear_its > 0 ? o.max_linear_its : 500;
   l.tol = o.linear_tol > 0 ? o.linear_tol : 1e-6;
   l.fp32_inner = o.linear_precision == GB_LINEAR_FP32_REFINED;

@@ -1345,10 +1345,12 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
       std::vector<double> hcol(j + 2, 0.0);
       double *dh1 = dh, *dh2 = dh + (m + 2), *dnrm = dh + 2 * (m + 2);
       multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
-      multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh1);
+      // one thread per coefficient (restart lengths up to 1023)
+      const int fin = ((j + 1 + 31) / 32) * 32;
+      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh1);
       gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
       multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
-      multidot_final_kernel<<<1, 64, 0, st>>>(j + 1, kRedBlocks, dpart, dh2);
+      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh2);
       gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
       norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dred);
       norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, dred, dnrm);

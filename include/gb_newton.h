@@ -210,7 +210,9 @@ typedef struct gb_newton_opts {
   int max_newton;          /* "Number of Newton Iterations" */
   double residual_tol;     /* "Normalized Residual Tolerance" (Epsilon[0]) */
   double damping;          /* "Newton correction factor" */
-  int krylov_dim;          /* "Size of Krylov subspace" (AztecOO default 30) */
+  int krylov_dim;          /* "Size of Krylov subspace" (AztecOO default 30; at most
+                              1023, and 31 for several independent problems in one
+                              context) */
   int max_linear_its;      /* "Maximum Linear Solve Iterations" */
   double linear_tol;       /* "Linear Solver Tolerance" (relative residual) */
   int linear_precision;    /* GB_LINEAR_FP64 or GB_LINEAR_FP32_REFINED */

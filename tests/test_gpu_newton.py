@@ -195,3 +195,22 @@ def test_gpu_factorization_reuse(fp32):
     _, xp, st = solve(1e4, None, 1)
     assert st["factorizations"] == 1
     assert np.abs(xp - xc).max() <= TOL_X * np.abs(xc).max()
+
+
+def test_gpu_long_gmres_restart_matches_short_one():
+    """A restart length beyond 63 (its Gram-Schmidt coefficients need more
+    than two warps in the final reduction) solves the same Newton system to
+    the same solution as GMRES(30)."""
+    prob = pb.boussinesq_cube_3d(4, 1e4, 0.71)
+    o = oracle.Oracle(prob)
+    x = o.dirichlet_init(np.random.default_rng(3).uniform(-0.5, 0.5, o.N))
+    R, a, _ = o.matrix_fill(x)
+    a_s, R_s, _ = o.row_sum_scale(a, R)
+    gn = GomaNewton(prob)
+    dx30, its30, rr30 = gn.linear_solve(a_s, R_s, linear_tol=1e-11, max_linear_its=4000,
+                                        krylov_dim=30)
+    dx150, its150, rr150 = gn.linear_solve(a_s, R_s, linear_tol=1e-11, max_linear_its=4000,
+                                           krylov_dim=150)
+    assert rr30 <= 1e-11 and rr150 <= 1e-11
+    assert its150 <= its30
+    assert np.abs(dx150 - dx30).max() <= 1e-8 * np.abs(dx30).max()
