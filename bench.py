@@ -204,7 +204,7 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
     torch.cuda.synchronize()
     del warm, xw, tw
     sols = {}
-    modes = list(modes) if modes else ["plain_fp64", "learned_fp64", "learned_fp32"] + (
+    modes = list(modes) if modes else ["plain_fp64", "secant_fp32", "learned_fp32"] + (
         ["plain_fp64_reference_solver"] if reference_solver else [])
     for mode in modes:
         prob = pb.boussinesq_cube_3d(nel, ra0, PR)
@@ -720,7 +720,7 @@ def main():
                     help="comma-separated runs of the time-to-solve leg: plain_fp64, "
                          "learned_fp64, learned_fp32, secant_fp32, secant_fp64, "
                          "plain_fp64_reference_solver "
-                         "(default: all)")
+                         "(default: plain_fp64, secant_fp32, learned_fp32)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
                     help="seconds per run of the time-to-solve leg (0: no limit)")
     ap.add_argument("--solve-krylov", type=int, default=60,
