@@ -31,6 +31,27 @@ import math
 import numpy as np
 
 
+# array helpers: the driver runs on numpy arrays (host problems) or torch
+# tensors (GomaArcProblemDevice, vectors resident on the GPU)
+def _dot(a, b):
+    return float((a * b).sum())
+
+
+def _norm(a):
+    return math.sqrt(_dot(a, a))
+
+
+def _finite(a):
+    if isinstance(a, np.ndarray):
+        return bool(np.all(np.isfinite(a)))
+    import torch
+    return bool(torch.isfinite(a).all())
+
+
+def _copy(a):
+    return a.copy() if isinstance(a, np.ndarray) else a.clone()
+
+
 def msr_row_scale(ija, a):
     """Row scales of an MSR matrix as the reference's row_sum_scale_MSR
     (src/sl_matrix_util.c:506): sign(a_ii) * sum_j |a_ij| (1 for an
@@ -83,6 +104,62 @@ class GomaArcProblem:
         return self.gn.dirichlet_init(x)
 
 
+class GomaArcProblemDevice:
+    """linearize() with every vector on the GPU (torch float64 tensors):
+    assembly through gb_matrix_fill_full_device into the context's CSR
+    values, row-sum scaling on the device (gb_row_sum_scale_device), and
+    ILU(0)-GMRES through gb_linear_solve_device, factorising once per
+    linearisation and reusing the factors for its further right-hand sides.
+    Only scalars (norms, dot products) come back to the host."""
+
+    def __init__(self, gn, set_param, **linear_opts):
+        import torch
+        self.gn = gn
+        self.set_param = set_param
+        self.opts = dict(linear_tol=1e-10, max_linear_its=4000, krylov_dim=60)
+        self.opts.update(linear_opts)
+        self.torch = torch
+        dev = torch.device("cuda")
+        self.R = torch.empty(gn.N, dtype=torch.float64, device=dev)
+        self.scale = torch.empty(gn.N, dtype=torch.float64, device=dev)
+
+    def _sync(self):
+        self.gn.status()   # the library stream: its assembly / scaling are done
+
+    def residual(self, x, lam):
+        self.set_param(self.gn, lam)
+        self.torch.cuda.current_stream().synchronize()
+        self.gn.matrix_fill_full_device(x.data_ptr(), self.R.data_ptr(), None)
+        self._sync()
+        return self.R.clone()
+
+    def linearize(self, x, lam):
+        torch = self.torch
+        self.set_param(self.gn, lam)
+        torch.cuda.current_stream().synchronize()
+        gn = self.gn
+        gn.matrix_fill_full_device(x.data_ptr(), self.R.data_ptr(), gn.d_vals)
+        gn.scale_device(gn.d_vals, self.R.data_ptr(), self.scale.data_ptr())
+        self._sync()
+        R = self.R.clone()
+        scale = self.scale.clone()
+        first = [True]
+
+        def solve(rhs):
+            rhs = rhs.contiguous()
+            dx = torch.empty_like(rhs)
+            torch.cuda.current_stream().synchronize()
+            gn.linear_solve_device(gn.d_vals, rhs.data_ptr(), dx.data_ptr(),
+                                   factorization_reuse=0 if first[0] else 2, **self.opts)
+            first[0] = False
+            return dx
+
+        return R, solve, scale
+
+    def dirichlet_init(self, x):
+        return self.gn.dirichlet_init(x)
+
+
 def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta=1.0,
                            tol=1e-10, max_corrector=12, ds_min=None, ds_max=None,
                            dlam_rel=1e-6, direction=1.0):
@@ -95,9 +172,9 @@ def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta
     the list of solutions."""
     ds_min = ds_min if ds_min is not None else ds / 64.0
     ds_max = ds_max if ds_max is not None else ds * 8.0
-    x = np.asarray(x0, np.float64).copy()
+    x = _copy(x0) if not isinstance(x0, np.ndarray) else np.asarray(x0, np.float64).copy()
     lam = float(lam0)
-    n = x.size
+    n = x.numel() if hasattr(x, "numel") else x.size
     w = theta / n
 
     def dR_dlam(xc, lc, scale):
@@ -107,10 +184,10 @@ def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta
     def tangent(xc, lc, prev):
         _, solve, scale = problem.linearize(xc, lc)
         b = solve(-dR_dlam(xc, lc, scale))
-        norm = math.sqrt(w * float(b @ b) + 1.0)
+        norm = math.sqrt(w * _dot(b, b) + 1.0)
         t = (b / norm, 1.0 / norm)
         if prev is not None:
-            if w * float(t[0] @ prev[0]) + t[1] * prev[1] < 0.0:
+            if w * _dot(t[0], prev[0]) + t[1] * prev[1] < 0.0:
                 t = (-t[0], -t[1])
         elif direction < 0:
             t = (-t[0], -t[1])
@@ -119,7 +196,7 @@ def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta
     t = tangent(x, lam, None)
     records = [{"lam": lam, "ds": 0.0, "corrector_its": 0, "residual": None,
                 "lamdot": t[1]}]
-    sols = [x.copy()]
+    sols = [_copy(x)]
     step = 0
     while step < nsteps:
         xp = x + ds * t[0]
@@ -129,17 +206,17 @@ def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta
         rn = np.inf
         for it in range(1, max_corrector + 1):
             R, solve, scale = problem.linearize(xc, lc)
-            rn = float(np.linalg.norm(R))
-            Nc = w * float(t[0] @ (xc - x)) + t[1] * (lc - lam) - ds
+            rn = _norm(R)
+            Nc = w * _dot(t[0], xc - x) + t[1] * (lc - lam) - ds
             if rn < tol and abs(Nc) < tol * max(1.0, abs(ds)):
                 ok = True
                 break
             a = solve(-R)
             b = solve(-dR_dlam(xc, lc, scale))
-            dl = -(Nc + w * float(t[0] @ a)) / (t[1] + w * float(t[0] @ b))
+            dl = -(Nc + w * _dot(t[0], a)) / (t[1] + w * _dot(t[0], b))
             xc = xc + a + dl * b
             lc = lc + dl
-            if not np.all(np.isfinite(xc)):
+            if not _finite(xc):
                 break
         if not ok:
             ds *= 0.5
@@ -150,7 +227,7 @@ def arclength_continuation(problem, x0, lam0, ds, nsteps, lam_bounds=None, theta
         t = tangent(x, lam, t)
         records.append({"lam": lam, "ds": ds, "corrector_its": it, "residual": rn,
                         "lamdot": t[1]})
-        sols.append(x.copy())
+        sols.append(_copy(x))
         step += 1
         if it <= 3:
             ds = min(ds * 1.5, ds_max)

@@ -234,8 +234,9 @@ __global__ void __launch_bounds__(256)
         dif = fma(Wi.g[p], -M.conductivity * Q.gT[p], dif);
       }
       // with the mass term -rho Cp T_dot phi_i dA (src/mm_fill_energy.c:315-381)
+      // and the heat source phi_i h dA (:374-378)
       const double Tt = A.xdot ? vgT + E.Td[q] : vgT;
-      Racc += Tt * (-Wi.phi * E.rho * M.heat_capacity * dA) + dif * dA;
+      Racc += Tt * (-Wi.phi * E.rho * M.heat_capacity * dA) + dif * dA + Q.hs * (Wi.phi * dA);
     } else if (own_c) {
       double divv = 0.0;
 #pragma unroll
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(256)
           Jv[m][a][b] += val;
         }
       if (ENERGY) {
-        JTT[m] += fma(nmc * M.heat_capacity, pij, fma(Wi.phi, Wj.cT, nkdA * dot));
+        JTT[m] += fma(nmc * M.heat_capacity + Q.dhs, pij, fma(Wi.phi, Wj.cT, nkdA * dot));
         const double pc = -E.rho * M.heat_capacity * pij;
 #pragma unroll
         for (int b = 0; b < DIM; b++) {

@@ -152,6 +152,13 @@ int Context::set_material(const gb_material &m) {
     mat.ssm[w] = model;
     for (int k = 0; k < 4; k++) mat.ssp[w][k] = on ? m.species_source[w][k] : 0.0;
   }
+  if (m.heat_source_model != GB_HEAT_SOURCE_NONE &&
+      m.heat_source_model != GB_HEAT_SOURCE_CONSTANT &&
+      m.heat_source_model != GB_HEAT_SOURCE_EXPONENTIAL)
+    return fail("unsupported heat source model");
+  mat.hsm = L.energy ? m.heat_source_model : GB_HEAT_SOURCE_NONE;
+  mat.hs[0] = m.heat_source[0];
+  mat.hs[1] = m.heat_source[1];
   carreau = m.viscosity_model == GB_VISC_CARREAU;
   desc.mat = m;
   return 0;
@@ -284,6 +291,8 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
 
 int Context::kernel_path(bool jacobian) const {
   if (L.dim != 3) return 1;
+  // a heat source: the scalar kernel
+  if (mat.hsm != GB_HEAT_SOURCE_NONE) return 1;
   const bool gemm_ok = !carreau && mat.viscosity > 0.0;
   // per-element densities and transient terms: the scalar and the
   // sum-factorised kernels only

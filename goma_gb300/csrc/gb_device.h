@@ -20,6 +20,10 @@ struct MaterialDev {
   double diff[GB_MAX_SPECIES];
   int ssm[GB_MAX_SPECIES];
   double ssp[GB_MAX_SPECIES][4];
+  // energy heat source (GB_HEAT_SOURCE_*): CONSTANT hs[0], EXPONENTIAL
+  // hs[0] exp(hs[1] T)
+  int hsm;
+  double hs[2];
 };
 
 // Everything the assembly kernel reads or writes.  Device pointers.

@@ -33,6 +33,7 @@ struct QP {
   double f[DIM];
   double dfT[DIM];
   double psi[DIM + 1];
+  double hs, dhs;  // heat source and its T sensitivity
   int bad;
 };
 
@@ -176,6 +177,19 @@ __device__ __forceinline__ void qp_setup(const double (*X)[DIM], const double (*
       Q.f[a] = f;
       Q.dfT[a] = dfT;
     }
+    // heat source (heat_source, src/mm_fill_energy.c:1724; the exponential
+    // one is a USER model, src/user_mp.c:472)
+    double hs = 0.0, dhs = 0.0;
+    if (ENERGY) {
+      if (M.hsm == GB_HEAT_SOURCE_CONSTANT) {
+        hs = M.hs[0];
+      } else if (M.hsm == GB_HEAT_SOURCE_EXPONENTIAL) {
+        hs = M.hs[0] * exp(M.hs[1] * T);
+        dhs = M.hs[1] * hs;
+      }
+    }
+    Q.hs = hs;
+    Q.dhs = dhs;
     Q.T = T;
     Q.P = P;
     Q.mu = mu;

@@ -291,7 +291,13 @@ int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rh
   Context &c = ctx->c;
   const gb::LinearOpts lo = gb::linear_opts(o);
   if (gb::ensure_solver(&c, lo.krylov)) return -1;
-  if (c.solver->factor(d_vals, lo.fp32_inner, c.stream)) return -1;
+  // GB_FACTOR_REUSE keeps the last factors when there are any (a second
+  // solve with the same matrix, or a lagged preconditioner)
+  const bool reuse = o.factorization_reuse == GB_FACTOR_REUSE &&
+                     c.solver->has_factors(lo.fp32_inner);
+  if (reuse ? c.solver->refresh(d_vals, lo.fp32_inner, c.stream)
+            : c.solver->factor(d_vals, lo.fp32_inner, c.stream))
+    return -1;
   gb::LinearStats ls;
   if (gb::linear_solve(&c, d_rhs, d_dx, lo, &ls, c.stream)) return -1;
   cudaError_t e = cudaStreamSynchronize(c.stream);

@@ -17,6 +17,7 @@ VISC_NEWTONIAN, VISC_CARREAU = 0, 1
 SOURCE_CONSTANT, SOURCE_BOUSSINESQ = 0, 1
 MAX_SPECIES = 4
 SPECIES_SOURCE_NONE, SPECIES_SOURCE_CONSTANT, SPECIES_SOURCE_ARRHENIUS = 0, 1, 2
+HEAT_SOURCE_NONE, HEAT_SOURCE_CONSTANT, HEAT_SOURCE_EXPONENTIAL = 0, 1, 2
 
 
 def VAR_Y(w):
@@ -156,6 +157,10 @@ class Material:
     # S_w = nu k0 exp(-E/T) Y_s
     diffusivity: Tuple[float, ...] = ()
     species_source: Tuple[Tuple[int, Tuple[float, ...]], ...] = ()
+    # energy equation heat source: HEAT_SOURCE_CONSTANT h = c0, or
+    # HEAT_SOURCE_EXPONENTIAL h = c0 exp(c1 T) (Frank-Kamenetskii / Bratu)
+    heat_source_model: int = HEAT_SOURCE_NONE
+    heat_source: Tuple[float, float] = (0.0, 0.0)
 
 
 @dataclass
@@ -185,7 +190,8 @@ class CMaterial(ctypes.Structure):
                 ("reference_temperature", ctypes.c_double),
                 ("diffusivity", ctypes.c_double * MAX_SPECIES),
                 ("species_source_model", ctypes.c_int * MAX_SPECIES),
-                ("species_source", (ctypes.c_double * 4) * MAX_SPECIES)]
+                ("species_source", (ctypes.c_double * 4) * MAX_SPECIES),
+                ("heat_source_model", ctypes.c_int), ("heat_source", ctypes.c_double * 2)]
 
 
 class CProblemDesc(ctypes.Structure):
@@ -212,6 +218,8 @@ def c_material(mt: Material):
         cm.species_source_model[w] = model
         for k, v in enumerate(params):
             cm.species_source[w][k] = v
+    cm.heat_source_model = mt.heat_source_model
+    cm.heat_source[0], cm.heat_source[1] = mt.heat_source
     return cm
 
 
@@ -295,6 +303,20 @@ def reacting_channel_3d(nx, ny, nz, lx=2.0, ly=2.0, lz=1.0, seed=0, re=100.0, di
                    species_source=((SPECIES_SOURCE_ARRHENIUS, (k0, activation, -1.0, 0.0)),
                                    (SPECIES_SOURCE_ARRHENIUS, (k0, activation, 1.0, 0.0))))
     return Problem(mesh, mat, True, list(REACTING3D_BCS), (-1, 0.0), 2)
+
+
+def bratu_square_2d(n, lam=1.0, mesh=None):
+    """Frank-Kamenetskii / Bratu problem on the unit square, n x n QUAD9: the
+    energy equation with the heat source lam exp(T), unit conductivity, T =
+    0 on the whole boundary; the fluid is at rest (no-slip walls all round,
+    no body force, pressure datum on element 0), so the flow rows have the
+    zero solution.  Its solution branch has a fold at lam ~ 6.808."""
+    mesh = mesh or box_mesh(2, n, n)
+    mat = Material(density=1.0, viscosity=1.0, heat_capacity=1.0, conductivity=1.0,
+                   heat_source_model=HEAT_SOURCE_EXPONENTIAL, heat_source=(lam, 1.0))
+    bcs = list(CAVITY2D_BCS[:6]) + [(VAR_U1, 3, 0.0), (VAR_U2, 3, 0.0)]
+    bcs += [(VAR_T, s, 0.0) for s in (1, 2, 3, 4)]
+    return Problem(mesh, mat, True, bcs, (0, 0.0))
 
 
 def carreau_step_2d(nx, ny, re, lx=3.0, ly=1.0, mesh=None, mu0=1.0, mu_inf=0.01, lam=1.0,

@@ -298,7 +298,9 @@ int gb_row_sum_scale_device(gb_ctx *ctx, double *d_vals, double *d_R, double *d_
 
 /* The Krylov solve of one Newton step (the Linear_Solver switch,
  * src/mm_sol_nonlinear.c:1624): factor ILU(0) of the scaled matrix
- * d_vals (device CSR values) and solve A dx = rhs by GMRES.  Device arrays. */
+ * d_vals (device CSR values) and solve A dx = rhs by GMRES.  Device arrays.
+ * With opts->factorization_reuse = GB_FACTOR_REUSE the last factors are kept
+ * when there are any (a second right-hand side with the same matrix). */
 int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rhs, double *d_dx,
                            const gb_newton_opts *opts, int *iterations, double *relres);
 /* Host form taking the reference's MSR values (gb_msr_length() doubles,

@@ -14,6 +14,8 @@
  *   - material: density, Newtonian or Carreau-Yasuda viscosity
  *     (src/mm_viscosity.c:981), heat capacity, Fourier conductivity,
  *     CONSTANT or BOUSSINESQ momentum source (src/mm_std_models.c:125);
+ *   - heat source of the energy equation: CONSTANT, or c0 exp(c1 T) as a
+ *     USER model (usr_heat_source, src/user_mp.c:472);
  *   - species sources: CONSTANT, or the Arrhenius rate of a USER model
  *     (usr_species_source, src/user_mp.c:598, called from
  *     src/mm_fill_species.c:10146):  S_w = nu k0 exp(-E/T) Y_s;
@@ -51,6 +53,15 @@ extern "C" {
 #define GB_SOURCE_CONSTANT 0
 #define GB_SOURCE_BOUSSINESQ 1
 
+/* "Heat Source" of the energy equation (heat_source, src/mm_fill_energy.c:
+ * 1724): none, CONSTANT h = c0, or the USER model (usr_heat_source,
+ * src/user_mp.c:472) h = c0 exp(c1 T), the Frank-Kamenetskii / Bratu
+ * source; R_T[i] += phi_i h dA, J_TT += phi_i dh/dT phi_j dA
+ * (src/mm_fill_energy.c:374-381, :477-481). */
+#define GB_HEAT_SOURCE_NONE 0
+#define GB_HEAT_SOURCE_CONSTANT 1
+#define GB_HEAT_SOURCE_EXPONENTIAL 2
+
 typedef struct gb_material {
   double density;          /* "Density = CONSTANT" */
   int viscosity_model;     /* GB_VISC_* ("Liquid Constitutive Equation") */
@@ -72,6 +83,8 @@ typedef struct gb_material {
   /* CONSTANT: [0] = S.  ARRHENIUS: k0, E, nu, s with S_w = nu k0 exp(-E/T) Y_s
    * (needs the energy equation, T > 0). */
   double species_source[GB_MAX_SPECIES][4];
+  int heat_source_model;   /* GB_HEAT_SOURCE_* ("Heat Source") */
+  double heat_source[2];   /* c0, c1 */
 } gb_material;
 
 typedef struct gb_problem_desc {

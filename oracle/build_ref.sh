@@ -43,9 +43,11 @@ gcc $SHIMC -c "$SHIM/tpl_stubs.c" -o "$OUT/tpl_stubs.o"
 gcc $SHIMC -c "$HERE/mesh_gen.c" -o "$OUT/mesh_gen.o"
 gcc $CFLAGS -c "$SHIM/harness.c" -o "$OUT/harness.o"
 gcc $CFLAGS -c "$SHIM/user_species.c" -o "$OUT/user_species.o"
+gcc $CFLAGS -c "$SHIM/user_heat.c" -o "$OUT/user_heat.o"
 gcc $SHIMC -c "$SHIM/ref_main.c" -o "$OUT/ref_main.o"
 OBJS=$(ls "$OUT"/obj/*.o | grep -v '/main\.o$')
 gcc -o "$OUT/goma_ref" "$OUT/ref_main.o" $OBJS "$OUT"/exo_mem.o "$OUT"/mpi_serial.o \
   "$OUT"/band_lu.o "$OUT"/tpl_stubs.o "$OUT"/mesh_gen.o "$OUT"/harness.o "$OUT"/user_species.o \
-  -Wl,--wrap=matrix_fill_full -Wl,--wrap=numerical_jacobian -Wl,--wrap=usr_species_source -lm
+  "$OUT"/user_heat.o -Wl,--wrap=matrix_fill_full -Wl,--wrap=numerical_jacobian \
+  -Wl,--wrap=usr_species_source -Wl,--wrap=usr_heat_source -lm
 echo "build_ref: built $OUT/goma_ref"

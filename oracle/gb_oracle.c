@@ -496,6 +496,15 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
       for (int a = 0; a < dim; a++) f[a] = m->momentum_source[a];
     }
     const double rho = m->density, rcp = m->density * m->heat_capacity, kc = m->conductivity;
+    /* heat source (heat_source, src/mm_fill_energy.c:1724): CONSTANT, or the
+     * USER model c0 exp(c1 T) (usr_heat_source, src/user_mp.c:472) */
+    double hsrc = 0.0, dhsrc = 0.0;
+    if (m->heat_source_model == GB_HEAT_SOURCE_CONSTANT) {
+      hsrc = m->heat_source[0];
+    } else if (m->heat_source_model == GB_HEAT_SOURCE_EXPONENTIAL) {
+      hsrc = m->heat_source[0] * exp(m->heat_source[1] * T);
+      dhsrc = m->heat_source[1] * hsrc;
+    }
 
     /* momentum */
     for (int a = 0; a < dim; a++) {
@@ -554,8 +563,10 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
         double dif = 0.0;
         for (int pp = 0; pp < dim; pp++) dif += gphi[i][pp] * (-kc * gT[pp]);
         dif *= dA;
-        /* mass term -rho Cp T_dot phi_i dA (src/mm_fill_energy.c:315-381) */
-        Re[ri] += adv + dif - rcp * Td * phi[i] * dA;
+        /* mass term -rho Cp T_dot phi_i dA (src/mm_fill_energy.c:315-381),
+         * heat source phi_i h dA (:374-378) */
+        Re[ri] += adv + dif - rcp * Td * phi[i] * dA + hsrc * phi[i] * dA;
+        for (int j = 0; j < nn; j++) JE(ri, oT + j) += dhsrc * phi[i] * phi[j] * dA;
         if (mc != 0.0)
           for (int j = 0; j < nn; j++) JE(ri, oT + j) += -mc * rcp * phi[i] * phi[j] * dA;
         for (int j = 0; j < nn; j++) {

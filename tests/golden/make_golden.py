@@ -104,6 +104,18 @@ CASES = {
                                             transient=dict(dt=0.01, steps=5, theta=0.5)),
 }
 
+# the Frank-Kamenetskii / Bratu problem: energy with the heat source
+# c0 exp(c1 T) (a USER model, oracle/ref_shim/user_heat.c), T = 0 all round,
+# the fluid at rest
+CASES.update({
+    "bratu2d_4x4_pert": dict(mesh="quad9 4 4 1 1 0.12 3", phys="nst", rho=1.0,
+                             visc=("newtonian", 1.0), bc="bratu2d", datum=True,
+                             mode="assemble", seed=15, ra_pr=0.0, heat=(5.0, 1.0)),
+    "bratu2d_8x8_solve": dict(mesh="quad9 8 8 1 1", phys="nst", rho=1.0,
+                              visc=("newtonian", 1.0), bc="bratu2d", datum=True, mode="solve",
+                              tol=1e-12, ra_pr=0.0, heat=(5.0, 1.0)),
+})
+
 COMPACT_ROWS = 300  # Jacobian rows kept by a compact record
 
 # Dirichlet sets: (variable, node set id, value), applied in this order
@@ -114,6 +126,8 @@ BCS = {
               ("V", 5, 0.0), ("U", 6, 1.0), ("V", 6, 0.0)],
     "cube_heated": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
     + [("T", 1, 1.0), ("T", 2, 0.0)],
+    "bratu2d": [(c, s, 0.0) for s in (1, 2, 4, 3) for c in ("U", "V")]
+    + [("T", s, 0.0) for s in (1, 2, 3, 4)],
     # heated box with two species fed at x = 0: T in [1, 2] keeps exp(-E/T) finite
     "cube_species": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
     + [("T", 1, 2.0), ("T", 2, 1.0), ("Y0", 1, 1.0), ("Y1", 1, 0.0)],
@@ -231,8 +245,14 @@ def mat_text(case):
         "Permeability = CONSTANT 0.", "",
         ] + species_props(case) + [
         "---Source Terms", src, "Solid Body Source = CONSTANT 0. 0. 0.",
-        "Mass Source = CONSTANT 0.", "Heat Source = CONSTANT 0."] + species_sources(case) + [
+        "Mass Source = CONSTANT 0.", heat_source(case)] + species_sources(case) + [
         "Current Source = CONSTANT 0.", ""])
+
+
+def heat_source(case):
+    if "heat" in case:
+        return "Heat Source = USER %.17g %.17g" % tuple(case["heat"])
+    return "Heat Source = CONSTANT 0."
 
 
 def species_props(case):

@@ -77,8 +77,12 @@ def problem_from_case(case):
         mat.diffusivity = tuple(case["diff"])
         mat.species_source = tuple((pb.SPECIES_SOURCE_ARRHENIUS, (k0, E, -1.0 if w == 0 else 1.0, 0))
                                    for w in range(ns))
+    if "heat" in case:
+        mat.heat_source_model = pb.HEAT_SOURCE_EXPONENTIAL
+        mat.heat_source = tuple(case["heat"])
     bcs = {"cavity2d": pb.CAVITY2D_BCS, "bfs2d": pb.BFS2D_BCS,
-           "cube_heated": pb.HEATED3D_BCS, "cube_species": pb.SPECIES3D_BCS}[case["bc"]]
+           "cube_heated": pb.HEATED3D_BCS, "cube_species": pb.SPECIES3D_BCS,
+           "bratu2d": pb.bratu_square_2d(1).bcs}[case["bc"]]
     return pb.Problem(mesh, mat, energy, list(bcs), (0, 0.0) if case["datum"] else (-1, 0.0),
                       num_species=ns)
 
