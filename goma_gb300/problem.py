@@ -18,6 +18,7 @@ SOURCE_CONSTANT, SOURCE_BOUSSINESQ = 0, 1
 MAX_SPECIES = 4
 SPECIES_SOURCE_NONE, SPECIES_SOURCE_CONSTANT, SPECIES_SOURCE_ARRHENIUS = 0, 1, 2
 HEAT_SOURCE_NONE, HEAT_SOURCE_CONSTANT, HEAT_SOURCE_EXPONENTIAL = 0, 1, 2
+IBC_QSIDE, IBC_QCONV, IBC_FLOW_PRESSURE = 1, 2, 3
 
 
 def VAR_Y(w):
@@ -60,6 +61,8 @@ class Mesh:
     conn: np.ndarray        # (num_elems, 9|27) int32
     node_sets: List[np.ndarray]  # node set id k+1 -> ascending node ids
     shape: Tuple[int, ...] = ()
+    # side set id k+1 -> (elements, Exodus side numbers), both int32
+    side_sets: List[Tuple[np.ndarray, np.ndarray]] = field(default_factory=list)
 
     @property
     def num_nodes(self):
@@ -117,7 +120,18 @@ def box_mesh(dim, nx, ny, nz=1, lx=1.0, ly=1.0, lz=1.0, amp=0.0, seed=0):
         sets = [i == 0, i == NX - 1, j == 0, j == NY - 1, k == 0, k == NZ - 1]
     node_sets = [np.nonzero(s)[0].astype(np.int32) for s in sets]
     shape = (nx, ny) if dim == 2 else (nx, ny, nz)
-    return Mesh(dim, coords, np.ascontiguousarray(conn, dtype=np.int32), node_sets, shape)
+    # side sets on the same boundaries as node sets 1..4 (2-D) / 1..6 (3-D),
+    # Exodus side numbers: QUAD9 1 t=-1, 2 s=+1, 3 t=+1, 4 s=-1; HEX27 the
+    # same and 5 u=-1, 6 u=+1
+    eid = np.arange(nx * ny * (nz if dim == 3 else 1), dtype=np.int32)
+    if dim == 2:
+        sel = [(ey == 0, 1), (ex == nx - 1, 2), (ey == ny - 1, 3), (ex == 0, 4)]
+    else:
+        sel = [(ex == 0, 4), (ex == nx - 1, 2), (ey == 0, 1), (ey == ny - 1, 3), (ez == 0, 5),
+               (ez == nz - 1, 6)]
+    side_sets = [(eid[m], np.full(int(m.sum()), sd, np.int32)) for m, sd in sel]
+    return Mesh(dim, coords, np.ascontiguousarray(conn, dtype=np.int32), node_sets, shape,
+                side_sets)
 
 
 def mesh_from_spec(spec):
@@ -172,6 +186,9 @@ class Problem:
     bcs: List[Tuple[int, int, float]] = field(default_factory=list)
     pressure_datum: Tuple[int, float] = (-1, 0.0)
     num_species: int = 0
+    # integrated boundary conditions: (IBC_* type, side set id (1-based),
+    # value 0, value 1)
+    ibcs: List[Tuple[int, int, float, float]] = field(default_factory=list)
 
     @property
     def dim(self):
@@ -204,7 +221,12 @@ class CProblemDesc(ctypes.Structure):
                 ("bc_ptr", ctypes.POINTER(ctypes.c_int)),
                 ("bc_nodes", ctypes.POINTER(ctypes.c_int)),
                 ("pressure_datum_elem", ctypes.c_int),
-                ("pressure_datum_value", ctypes.c_double)]
+                ("pressure_datum_value", ctypes.c_double),
+                ("num_ibc", ctypes.c_int), ("ibc_type", ctypes.POINTER(ctypes.c_int)),
+                ("ibc_value", ctypes.POINTER(ctypes.c_double)),
+                ("ibc_ptr", ctypes.POINTER(ctypes.c_int)),
+                ("ibc_elem", ctypes.POINTER(ctypes.c_int)),
+                ("ibc_side", ctypes.POINTER(ctypes.c_int))]
 
 
 def c_material(mt: Material):
@@ -240,13 +262,25 @@ def make_desc(prob: Problem):
         bc_val = np.zeros(1, np.float64)
     cm = c_material(prob.material)
     P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    ib_type = np.array([b[0] for b in prob.ibcs] or [0], dtype=np.int32)
+    ib_val = np.array([v for b in prob.ibcs for v in (b[2], b[3])] or [0.0], dtype=np.float64)
+    ib_sets = [m.side_sets[b[1] - 1] for b in prob.ibcs]
+    ib_ptr = np.zeros(len(ib_sets) + 1, dtype=np.int32)
+    ib_ptr[1:] = np.cumsum([len(e) for e, _ in ib_sets]) if ib_sets else []
+    ib_elem = (np.concatenate([e for e, _ in ib_sets]).astype(np.int32) if ib_sets
+               else np.zeros(1, np.int32))
+    ib_side = (np.concatenate([sd for _, sd in ib_sets]).astype(np.int32) if ib_sets
+               else np.zeros(1, np.int32))
     d = CProblemDesc(m.dim, m.num_nodes, m.num_elems, P(coords, ctypes.c_double),
                      P(conn, ctypes.c_int), 1 if prob.energy else 0, int(prob.num_species),
                      cm, len(prob.bcs),
                      P(bc_var, ctypes.c_int), P(bc_val, ctypes.c_double), P(bc_ptr, ctypes.c_int),
                      P(bc_nodes, ctypes.c_int), int(prob.pressure_datum[0]),
-                     float(prob.pressure_datum[1]))
-    return d, (coords, conn, bc_var, bc_val, bc_ptr, bc_nodes)
+                     float(prob.pressure_datum[1]), len(prob.ibcs), P(ib_type, ctypes.c_int),
+                     P(ib_val, ctypes.c_double), P(ib_ptr, ctypes.c_int),
+                     P(ib_elem, ctypes.c_int), P(ib_side, ctypes.c_int))
+    return d, (coords, conn, bc_var, bc_val, bc_ptr, bc_nodes, ib_type, ib_val, ib_ptr, ib_elem,
+               ib_side)
 
 
 # ------------------------------------------------------------ standard cases

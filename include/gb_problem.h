@@ -62,6 +62,21 @@ extern "C" {
 #define GB_HEAT_SOURCE_CONSTANT 1
 #define GB_HEAT_SOURCE_EXPONENTIAL 2
 
+/* Integrated (weak) boundary conditions on element sides, as
+ * apply_integrated_bc adds them (src/mm_fill.c:2976, src/bc_integ.c):
+ * R[row of node i] += sum_q w_q phi_i(q) sdet(q) func(q) over the side's
+ * Gauss points (3 on a QUAD9 edge, 3 x 3 on a HEX27 face,
+ * src/el_elm_info.c:1987), rows with a Dirichlet card left to that card:
+ *   QSIDE          energy, func = q (value[0])                 (:1518)
+ *   QCONV          energy, func = h (T_inf - T), dfunc/dT_j = -h phi_j
+ *                  (h = value[0], T_inf = value[1]; qrad_surf without
+ *                  radiation, src/mm_ns_bc.c:15145)
+ *   FLOW_PRESSURE  momentum a, func = -P n_a (P = value[0]; flow_n_dot_T_hydro,
+ *                  src/mm_ns_bc.c:6057), n the outward unit normal */
+#define GB_IBC_QSIDE 1
+#define GB_IBC_QCONV 2
+#define GB_IBC_FLOW_PRESSURE 3
+
 typedef struct gb_material {
   double density;          /* "Density = CONSTANT" */
   int viscosity_model;     /* GB_VISC_* ("Liquid Constitutive Equation") */
@@ -111,6 +126,17 @@ typedef struct gb_problem_desc {
    * pinned to pressure_datum_value; -1 for none. */
   int pressure_datum_elem;
   double pressure_datum_value;
+  /* Integrated boundary conditions (GB_IBC_*): card c of type ibc_type[c]
+   * with values ibc_value[2c], ibc_value[2c+1] on the sides ibc_ptr[c] ..
+   * ibc_ptr[c+1]-1; side k is element ibc_elem[k] (0-based), Exodus side
+   * ibc_side[k]: 1..4 on a QUAD9 (t = -1, s = +1, t = +1, s = -1), 1..6 on a
+   * HEX27 (t = -1, s = +1, t = +1, s = -1, u = -1, u = +1).  num_ibc 0: none. */
+  int num_ibc;
+  const int *ibc_type;
+  const double *ibc_value;
+  const int *ibc_ptr;
+  const int *ibc_elem;
+  const int *ibc_side;
 } gb_problem_desc;
 
 #ifdef __cplusplus

@@ -31,6 +31,11 @@ struct orc_problem {
    * coefficient (1 + 2 theta) / delta_t of its sensitivity */
   const double *xdot;
   double mass_c;
+  /* integrated boundary conditions (owned copies) and, per element, its
+   * (card, side) pairs: eibc_ptr[e] .. eibc_ptr[e+1]-1 */
+  int *ibc_type, *ibc_ptr, *ibc_elem, *ibc_side;
+  double *ibc_value;
+  int *eibc_ptr, *eibc_card, *eibc_side;
 };
 
 /* ---------------------------------------------------------------- basis */
@@ -239,6 +244,43 @@ orc_problem *orc_create(const gb_problem_desc *desc) {
     }
   }
 
+  /* integrated boundary conditions: owned copies, then per element */
+  {
+    const int nc = desc->num_ibc > 0 ? desc->num_ibc : 0;
+    const int ns = nc ? desc->ibc_ptr[nc] : 0;
+    p->ibc_type = (int *)malloc(sizeof(int) * (size_t)(nc + 1));
+    p->ibc_value = (double *)malloc(sizeof(double) * (size_t)(2 * nc + 1));
+    p->ibc_ptr = (int *)calloc((size_t)nc + 1, sizeof(int));
+    p->ibc_elem = (int *)malloc(sizeof(int) * (size_t)(ns + 1));
+    p->ibc_side = (int *)malloc(sizeof(int) * (size_t)(ns + 1));
+    if (nc) {
+      memcpy(p->ibc_type, desc->ibc_type, sizeof(int) * (size_t)nc);
+      memcpy(p->ibc_value, desc->ibc_value, sizeof(double) * (size_t)(2 * nc));
+      memcpy(p->ibc_ptr, desc->ibc_ptr, sizeof(int) * (size_t)(nc + 1));
+      memcpy(p->ibc_elem, desc->ibc_elem, sizeof(int) * (size_t)ns);
+      memcpy(p->ibc_side, desc->ibc_side, sizeof(int) * (size_t)ns);
+    }
+    p->d.num_ibc = nc;
+    p->d.ibc_type = p->ibc_type;
+    p->d.ibc_value = p->ibc_value;
+    p->d.ibc_ptr = p->ibc_ptr;
+    p->d.ibc_elem = p->ibc_elem;
+    p->d.ibc_side = p->ibc_side;
+    p->eibc_ptr = (int *)calloc((size_t)ne + 1, sizeof(int));
+    p->eibc_card = (int *)malloc(sizeof(int) * (size_t)(ns + 1));
+    p->eibc_side = (int *)malloc(sizeof(int) * (size_t)(ns + 1));
+    for (int k = 0; k < ns; k++) p->eibc_ptr[p->ibc_elem[k] + 1]++;
+    for (int e2 = 0; e2 < ne; e2++) p->eibc_ptr[e2 + 1] += p->eibc_ptr[e2];
+    int *cnt = (int *)calloc((size_t)ne + 1, sizeof(int));
+    for (int c = 0; c < nc; c++)
+      for (int k = p->ibc_ptr[c]; k < p->ibc_ptr[c + 1]; k++) {
+        const int el = p->ibc_elem[k], slot = p->eibc_ptr[el] + cnt[el]++;
+        p->eibc_card[slot] = c;
+        p->eibc_side[slot] = p->ibc_side[k];
+      }
+    free(cnt);
+  }
+
   /* Dirichlet cards in order: a later card overwrites (src/mm_bc.c:132) */
   p->dbc = (int *)malloc(sizeof(int) * (size_t)p->N);
   p->dbc_val = (double *)calloc((size_t)p->N, sizeof(double));
@@ -291,6 +333,14 @@ void orc_destroy(orc_problem *p) {
   free(p->ija);
   free(p->dbc);
   free(p->dbc_val);
+  free(p->ibc_type);
+  free(p->ibc_value);
+  free(p->ibc_ptr);
+  free(p->ibc_elem);
+  free(p->ibc_side);
+  free(p->eibc_ptr);
+  free(p->eibc_card);
+  free(p->eibc_side);
   free(p);
 }
 
@@ -347,6 +397,82 @@ void orc_element_dofs(const orc_problem *p, int e, int *g) {
  * then the hard-set Dirichlet rows of put_dirichlet_in_matrix
  * (src/bc_dirich.c:44): row zeroed, diagonal DIRICHLET_PENALTY = 1,
  * residual 0. */
+/* The integrated boundary conditions of one element side (apply_integrated_bc,
+ * src/bc_integ.c): Gauss points on the side (find_surf_st,
+ * src/el_elm_info.c:1987), sdet and the outward normal from the side's
+ * tangents, R_i += w phi_i sdet func, J_ij += w phi_i sdet dfunc/dx_j. */
+static void side_terms(const orc_problem *p, int card, int side, const double (*X)[3],
+                       const double *Tn, double *Re, double *Je) {
+  const int dim = p->d.dim, nn = p->nn, nloc = p->nloc, oT = dim * nn;
+  /* side -> fixed reference coordinate and its value */
+  static const int fix2[4][2] = {{1, -1}, {0, 1}, {1, 1}, {0, -1}};
+  static const int fix3[6][2] = {{1, -1}, {0, 1}, {1, 1}, {0, -1}, {2, -1}, {2, 1}};
+  const int fi = dim == 2 ? fix2[side - 1][0] : fix3[side - 1][0];
+  const double fv = dim == 2 ? fix2[side - 1][1] : fix3[side - 1][1];
+  int fr[2], nf = 0;
+  for (int r = 0; r < dim; r++)
+    if (r != fi) fr[nf++] = r;
+  const double g[3] = {GQ_PT, 0.0, -GQ_PT}, gw[3] = {GQ_W0, GQ_W1, GQ_W0};
+  const int type = p->ibc_type[card];
+  const double v0 = p->ibc_value[2 * card], v1 = p->ibc_value[2 * card + 1];
+  const int nq = dim == 2 ? 3 : 9;
+  /* element centre (for the outward orientation) */
+  double xc[3] = {0, 0, 0};
+  {
+    double xi0[3] = {0, 0, 0}, phc[27], dphc[27][3];
+    q2_basis(dim, xi0, phc, dphc);
+    for (int k = 0; k < nn; k++)
+      for (int j = 0; j < dim; j++) xc[j] += phc[k] * X[k][j];
+  }
+  for (int iq = 0; iq < nq; iq++) {
+    double xi[3] = {0, 0, 0}, w;
+    xi[fi] = fv;
+    xi[fr[0]] = g[iq % 3];
+    w = gw[iq % 3];
+    if (dim == 3) {
+      xi[fr[1]] = g[iq / 3];
+      w *= gw[iq / 3];
+    }
+    double phi[27], dphi[27][3];
+    q2_basis(dim, xi, phi, dphi);
+    double t[2][3] = {{0, 0, 0}, {0, 0, 0}}, xq[3] = {0, 0, 0}, T = 0.0;
+    for (int k = 0; k < nn; k++) {
+      for (int j = 0; j < dim; j++) {
+        xq[j] += phi[k] * X[k][j];
+        for (int m = 0; m < nf; m++) t[m][j] += dphi[k][fr[m]] * X[k][j];
+      }
+      T += phi[k] * Tn[k];
+    }
+    double n[3] = {0, 0, 0}, sdet;
+    if (dim == 2) {
+      sdet = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
+      n[0] = t[0][1] / sdet;
+      n[1] = -t[0][0] / sdet;
+    } else {
+      double c[3] = {t[0][1] * t[1][2] - t[0][2] * t[1][1], t[0][2] * t[1][0] - t[0][0] * t[1][2],
+                     t[0][0] * t[1][1] - t[0][1] * t[1][0]};
+      sdet = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+      for (int j = 0; j < 3; j++) n[j] = c[j] / sdet;
+    }
+    double o = 0.0;
+    for (int j = 0; j < dim; j++) o += n[j] * (xq[j] - xc[j]);
+    if (o < 0.0)
+      for (int j = 0; j < dim; j++) n[j] = -n[j];
+    const double ws = w * sdet;
+    for (int i = 0; i < nn; i++) {
+      const double wi = ws * phi[i];
+      if (type == GB_IBC_QSIDE) {
+        Re[oT + i] += wi * v0;
+      } else if (type == GB_IBC_QCONV) {
+        Re[oT + i] += wi * v0 * (v1 - T);
+        for (int j = 0; j < nn; j++) Je[(size_t)(oT + i) * nloc + oT + j] += wi * (-v0 * phi[j]);
+      } else if (type == GB_IBC_FLOW_PRESSURE) {
+        for (int a = 0; a < dim; a++) Re[a * nn + i] += wi * (-v0 * n[a]);
+      }
+    }
+  }
+}
+
 int orc_element(const orc_problem *p, int e, const double *x, double *Re, double *Je,
                 int apply_bc) {
   const int nn = p->nn, dim = p->d.dim, nloc = p->nloc, nq = dim == 2 ? 9 : 27;
@@ -630,6 +756,9 @@ int orc_element(const orc_problem *p, int e, const double *x, double *Re, double
       }
     }
   }
+  /* integrated boundary conditions of this element's sides */
+  for (int k = p->eibc_ptr[e]; k < p->eibc_ptr[e + 1]; k++)
+    side_terms(p, p->eibc_card[k], p->eibc_side[k], (const double (*)[3])X, Tn, Re, Je);
   if (apply_bc) {
     for (int r = 0; r < nloc; r++) {
       if (p->dbc[g[r]] == -1) continue;
