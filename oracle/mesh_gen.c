@@ -148,7 +148,70 @@ int gb_mesh_build_perturbed(gb_mesh *m, int dim, int nx, int ny, int nz, double 
     }
   }
   free(tmp);
+  /* side sets */
+  {
+    const int ne = m->num_elems;
+    int *te = (int *)malloc((size_t)ne * sizeof(int));
+    if (!te) return -1;
+    /* (selector, side): 2-D y=0, x=Lx, y=Ly, x=0; 3-D x=0, x=Lx, y=0, y=Ly, z=0, z=Lz */
+    static const int side2[4] = {1, 2, 3, 4};
+    static const int side3[6] = {4, 2, 1, 3, 5, 6};
+    m->num_ssets = dim == 2 ? 4 : 6;
+    for (int s = 0; s < m->num_ssets; s++) {
+      int n = 0;
+      for (int e = 0; e < ne; e++) {
+        const int ex = e % nx, ey = (e / nx) % ny, ez = e / (nx * ny);
+        int on = 0;
+        if (dim == 2) {
+          switch (s) {
+          case 0: on = ey == 0; break;
+          case 1: on = ex == nx - 1; break;
+          case 2: on = ey == ny - 1; break;
+          case 3: on = ex == 0; break;
+          }
+        } else {
+          switch (s) {
+          case 0: on = ex == 0; break;
+          case 1: on = ex == nx - 1; break;
+          case 2: on = ey == 0; break;
+          case 3: on = ey == ny - 1; break;
+          case 4: on = ez == 0; break;
+          case 5: on = ez == nz - 1; break;
+          }
+        }
+        if (on) te[n++] = e;
+      }
+      m->sset_len[s] = n;
+      m->sset_elem[s] = (int *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+      m->sset_side[s] = (int *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int));
+      if (!m->sset_elem[s] || !m->sset_side[s]) return -1;
+      for (int k = 0; k < n; k++) {
+        m->sset_elem[s][k] = te[k];
+        m->sset_side[s][k] = dim == 2 ? side2[s] : side3[s];
+      }
+    }
+    free(te);
+  }
   return 0;
+}
+
+int gb_mesh_side_nodes(int dim, int side, int *local) {
+  /* Exodus side node orders, 1-based element node numbers */
+  static const int q9[4][3] = {{1, 2, 5}, {2, 3, 6}, {3, 4, 7}, {4, 1, 8}};
+  static const int h27[6][9] = {{1, 2, 6, 5, 9, 14, 17, 13, 26},
+                                {2, 3, 7, 6, 10, 15, 18, 14, 25},
+                                {3, 4, 8, 7, 11, 16, 19, 15, 27},
+                                {1, 5, 8, 4, 13, 20, 16, 12, 24},
+                                {1, 4, 3, 2, 12, 11, 10, 9, 22},
+                                {5, 6, 7, 8, 17, 18, 19, 20, 23}};
+  if (dim == 2) {
+    if (side < 1 || side > 4) return 0;
+    for (int k = 0; k < 3; k++) local[k] = q9[side - 1][k] - 1;
+    return 3;
+  }
+  if (side < 1 || side > 6) return 0;
+  for (int k = 0; k < 9; k++) local[k] = h27[side - 1][k] - 1;
+  return 9;
 }
 
 int gb_mesh_build_from_spec(gb_mesh *m, const char *spec) {
@@ -178,5 +241,9 @@ void gb_mesh_free(gb_mesh *m) {
   free(m->z);
   free(m->conn);
   for (int s = 0; s < m->num_sets; s++) free(m->set_nodes[s]);
+  for (int s = 0; s < m->num_ssets; s++) {
+    free(m->sset_elem[s]);
+    free(m->sset_side[s]);
+  }
   memset(m, 0, sizeof(*m));
 }

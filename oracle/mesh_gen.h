@@ -39,7 +39,19 @@ typedef struct gb_mesh {
   int num_sets;
   int set_len[GB_MESH_MAX_SETS];
   int *set_nodes[GB_MESH_MAX_SETS]; /* ascending 0-based node ids */
+  /* side sets on the boundaries of node sets 1..4 (2-D) / 1..6 (3-D):
+   * 0-based elements and Exodus side numbers (QUAD9 1 t=-1, 2 s=+1,
+   * 3 t=+1, 4 s=-1; HEX27 the same and 5 u=-1, 6 u=+1) */
+  int num_ssets;
+  int sset_len[GB_MESH_MAX_SETS];
+  int *sset_elem[GB_MESH_MAX_SETS];
+  int *sset_side[GB_MESH_MAX_SETS];
 } gb_mesh;
+
+/* Local nodes (0-based, Goma order) of Exodus side `side` (1-based) of a
+ * QUAD9 (3 nodes: corners then mid-edge) or HEX27 (9: corners, mid-edges,
+ * face centre); returns the count. */
+int gb_mesh_side_nodes(int dim, int side, int *local);
 
 /* Reference-coordinate offsets (-1,0,1 mapped to grid steps 0,1,2) of each
  * local node. */

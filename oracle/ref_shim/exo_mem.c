@@ -69,7 +69,7 @@ int ex_get_init(int id, char *title, int *num_dim, int *num_nodes, int *num_elem
   *num_elem = g_mesh.num_elems;
   *num_blk = 1;
   *num_ns = g_mesh.num_sets;
-  *num_ss = 0;
+  *num_ss = g_mesh.num_ssets;
   return 0;
 }
 
@@ -87,8 +87,19 @@ int ex_inquire(int id, int req, int *ri, float *rf, char *rc) {
   case 10: /* NS_NODE_LEN */
     for (int s = 0; s < g_mesh.num_sets; s++) v += g_mesh.set_len[s];
     break;
+  case 11: /* SIDE_SETS */
+    v = g_mesh.num_ssets;
+    break;
+  case 12: /* SS_NODE_LEN */
+    for (int s = 0; s < g_mesh.num_ssets; s++)
+      v += g_mesh.sset_len[s] * (g_mesh.dim == 2 ? 3 : 9);
+    break;
+  case 13: /* SS_ELEM_LEN */
+    for (int s = 0; s < g_mesh.num_ssets; s++) v += g_mesh.sset_len[s];
+    break;
   case 17: /* EB_PROP */
   case 18: /* NS_PROP */
+  case 19: /* SS_PROP */
     v = 1;
     break;
   default:
@@ -136,6 +147,8 @@ int ex_get_ids(int id, int type, int *ids) {
     ids[0] = 1;
   } else if (type == EXM_NODE_SET) {
     for (int s = 0; s < g_mesh.num_sets; s++) ids[s] = s + 1;
+  } else if (type == EXM_SIDE_SET) {
+    for (int s = 0; s < g_mesh.num_ssets; s++) ids[s] = s + 1;
   }
   return 0;
 }
@@ -178,6 +191,22 @@ typedef struct {
 
 int ex_get_concat_sets(int id, int type, exm_set_specs *sp) {
   (void)id;
+  if (type == EXM_SIDE_SET) {
+    int off = 0;
+    for (int s = 0; s < g_mesh.num_ssets; s++) {
+      sp->sets_ids[s] = s + 1;
+      sp->num_entries_per_set[s] = g_mesh.sset_len[s];
+      sp->num_dist_per_set[s] = 0;
+      sp->sets_entry_index[s] = off;
+      sp->sets_dist_index[s] = 0;
+      for (int i = 0; i < g_mesh.sset_len[s]; i++) {
+        sp->sets_entry_list[off + i] = g_mesh.sset_elem[s][i] + 1;
+        if (sp->sets_extra_list) sp->sets_extra_list[off + i] = g_mesh.sset_side[s][i];
+      }
+      off += g_mesh.sset_len[s];
+    }
+    return 0;
+  }
   if (type != EXM_NODE_SET) return 0;
   int off = 0;
   for (int s = 0; s < g_mesh.num_sets; s++) {
@@ -193,15 +222,24 @@ int ex_get_concat_sets(int id, int type, exm_set_specs *sp) {
 }
 int ex_get_side_set_node_list_len(int id, int64_t ss, int *len) {
   (void)id;
-  (void)ss;
-  *len = 0;
+  const int s = (int)ss - 1;
+  *len = (s >= 0 && s < g_mesh.num_ssets) ? g_mesh.sset_len[s] * (g_mesh.dim == 2 ? 3 : 9) : 0;
   return 0;
 }
+/* per side its node count and the nodes (1-based), Exodus side order */
 int ex_get_side_set_node_list(int id, int64_t ss, int *cnt, int *list) {
   (void)id;
-  (void)ss;
-  (void)cnt;
-  (void)list;
+  const int s = (int)ss - 1;
+  if (s < 0 || s >= g_mesh.num_ssets) return 0;
+  int off = 0, loc[9];
+  for (int i = 0; i < g_mesh.sset_len[s]; i++) {
+    const int e = g_mesh.sset_elem[s][i];
+    const int n = gb_mesh_side_nodes(g_mesh.dim, g_mesh.sset_side[s][i], loc);
+    cnt[i] = n;
+    for (int k = 0; k < n; k++)
+      list[off + k] = g_mesh.conn[(size_t)e * g_mesh.nodes_per_elem + loc[k]] + 1;
+    off += n;
+  }
   return 0;
 }
 int ex_get_prop_names(int id, int type, char **names) {
@@ -217,6 +255,8 @@ int ex_get_prop_array(int id, int type, const char *name, int *vals) {
     vals[0] = 1;
   } else if (type == EXM_NODE_SET) {
     for (int s = 0; s < g_mesh.num_sets; s++) vals[s] = s + 1;
+  } else if (type == EXM_SIDE_SET) {
+    for (int s = 0; s < g_mesh.num_ssets; s++) vals[s] = s + 1;
   }
   return 0;
 }

@@ -104,6 +104,27 @@ CASES = {
                                             transient=dict(dt=0.01, steps=5, theta=0.5)),
 }
 
+# integrated (weak) boundary conditions on side sets: a heat flux (QSIDE), a
+# convective heat transfer (QCONV, h and T_inf) and an outflow pressure
+# (FLOW_PRESSURE)
+CASES.update({
+    "channel2d_4x3_ibc": dict(mesh="quad9 4 3 2 1 0.12 17", phys="nst", rho=10.0,
+                              visc=("newtonian", 1.0), bc="channel2d_t", datum=False,
+                              mode="assemble", seed=16, ra_pr=0.0,
+                              ibc=[("FLOW_PRESSURE", 2, (0.5,)), ("QCONV", 1, (2.0, 0.25)),
+                                   ("QSIDE", 3, (0.7,))]),
+    "box3d_2x2x2_ibc": dict(mesh="hex27 2 2 2 1 1 1 0.1 19", phys="nst", rho=1.0,
+                            visc=("newtonian", 0.71), bc="box_open_top", datum=False,
+                            mode="assemble", seed=17, ra_pr=710.0,
+                            ibc=[("QCONV", 2, (2.0, 0.25)), ("QSIDE", 5, (0.7,)),
+                                 ("FLOW_PRESSURE", 6, (0.3,))]),
+    "channel2d_6x3_ibc_solve": dict(mesh="quad9 6 3 2 1", phys="nst", rho=10.0,
+                                    visc=("newtonian", 1.0), bc="channel2d_t", datum=False,
+                                    mode="solve", tol=1e-12, ra_pr=0.0,
+                                    ibc=[("FLOW_PRESSURE", 2, (0.5,)),
+                                         ("QCONV", 1, (2.0, 0.25)), ("QSIDE", 3, (0.7,))]),
+})
+
 # the Frank-Kamenetskii / Bratu problem: energy with the heat source
 # c0 exp(c1 T) (a USER model, oracle/ref_shim/user_heat.c), T = 0 all round,
 # the fluid at rest
@@ -126,6 +147,13 @@ BCS = {
               ("V", 5, 0.0), ("U", 6, 1.0), ("V", 6, 0.0)],
     "cube_heated": [(c, s, 0.0) for s in (1, 2, 3, 4, 5, 6) for c in ("U", "V", "W")]
     + [("T", 1, 1.0), ("T", 2, 0.0)],
+    # channel: walls y = 0 and y = Ly, plug inflow u = 1 with T = 1 at x = 0,
+    # the outflow x = Lx left to an integrated condition
+    "channel2d_t": [("U", 1, 0.0), ("V", 1, 0.0), ("U", 3, 0.0), ("V", 3, 0.0),
+                    ("U", 4, 1.0), ("V", 4, 0.0), ("T", 4, 1.0)],
+    # box: no-slip on the x and y faces, T = 1 at x = 0, the top z = Lz open
+    "box_open_top": [(c, s, 0.0) for s in (1, 2, 3, 4, 5) for c in ("U", "V", "W")]
+    + [("T", 1, 1.0)],
     "bratu2d": [(c, s, 0.0) for s in (1, 2, 4, 3) for c in ("U", "V")]
     + [("T", s, 0.0) for s in (1, 2, 3, 4)],
     # heated box with two species fed at x = 0: T in [1, 2] keeps exp(-E/T) finite
@@ -187,6 +215,8 @@ def deck_text(case):
             lines.append("BC = Y NS %d %d %.17g" % (ns, int(var[1:]), val))
         else:
             lines.append("BC = %s NS %d %.17g" % (var, ns, val))
+    for name, ss, vals in case.get("ibc", []):   # integrated conditions on side sets
+        lines.append("BC = %s SS %d %s" % (name, ss, " ".join("%.17g" % v for v in vals)))
     lines.append("END OF BC")
     if case["datum"]:
         lines += ["", "PRESSURE DATUM = 0 0."]
@@ -213,6 +243,7 @@ def deck_text(case):
               "Post Processing Specifications", ""]
     # the BC count line must match what was written
     nbc = sum(1 for v, _, _ in BCS[case["bc"]] if not (dim == 2 and v == "W"))
+    nbc += len(case.get("ibc", []))
     lines[lines.index("Number of BC = %d" % len(BCS[case["bc"]]))] = "Number of BC = %d" % nbc
     return "\n".join(lines)
 

@@ -80,11 +80,19 @@ def problem_from_case(case):
     if "heat" in case:
         mat.heat_source_model = pb.HEAT_SOURCE_EXPONENTIAL
         mat.heat_source = tuple(case["heat"])
+    U1, U2, U3, T = pb.VAR_U1, pb.VAR_U2, pb.VAR_U3, pb.VAR_T
     bcs = {"cavity2d": pb.CAVITY2D_BCS, "bfs2d": pb.BFS2D_BCS,
            "cube_heated": pb.HEATED3D_BCS, "cube_species": pb.SPECIES3D_BCS,
-           "bratu2d": pb.bratu_square_2d(1).bcs}[case["bc"]]
+           "bratu2d": pb.bratu_square_2d(1).bcs,
+           "channel2d_t": [(U1, 1, 0.0), (U2, 1, 0.0), (U1, 3, 0.0), (U2, 3, 0.0),
+                           (U1, 4, 1.0), (U2, 4, 0.0), (T, 4, 1.0)],
+           "box_open_top": [(c, s, 0.0) for s in (1, 2, 3, 4, 5) for c in (U1, U2, U3)]
+           + [(T, 1, 1.0)]}[case["bc"]]
+    kinds = {"QSIDE": pb.IBC_QSIDE, "QCONV": pb.IBC_QCONV, "FLOW_PRESSURE": pb.IBC_FLOW_PRESSURE}
+    ibcs = [(kinds[name], ss, float(vals[0]), float(vals[1]) if len(vals) > 1 else 0.0)
+            for name, ss, vals in case.get("ibc", [])]
     return pb.Problem(mesh, mat, energy, list(bcs), (0, 0.0) if case["datum"] else (-1, 0.0),
-                      num_species=ns)
+                      num_species=ns, ibcs=ibcs)
 
 
 def msr_row_scaled_error(ija, a, ref):
