@@ -108,7 +108,7 @@ Context::~Context() {
   void *ptrs[] = {d_coords, d_conn,   d_fu,     d_dbc,     d_dbc_val, d_rowptr, d_colidx,
                   d_nbr_ptr, d_nbr_off, d_nbr_offT, d_nbr_node, d_nslot, d_tab_phi, d_tab_dphi, d_tab_w,
                   d_tab_pt, d_tab_iso, d_color_elems, d_x, d_R, d_vals, d_status, d_msr,
-                  d_elem_rho};
+                  d_elem_rho, d_side_elem, d_side_side, d_side_type, d_side_val};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (d_sf) cudaFree(d_sf);
@@ -200,6 +200,34 @@ int Context::init(const gb_problem_desc *d) {
     build_sf_tables(tphi.data(), tdphi.data(), kLoc27, ell, dell, sft[0]);
     if (upload(&d_sf, sft, "tab")) return -1;
   }
+  // integrated boundary conditions: the cards expanded to their sides
+  if (d->num_ibc > 0) {
+    std::vector<int> se, ss, st;
+    std::vector<double> sv;
+    const int maxside = L.dim == 2 ? 4 : 6;
+    for (int c = 0; c < d->num_ibc; c++) {
+      const int ty = d->ibc_type[c];
+      if (ty != GB_IBC_QSIDE && ty != GB_IBC_QCONV && ty != GB_IBC_FLOW_PRESSURE)
+        return fail("unsupported integrated boundary condition");
+      if (ty != GB_IBC_FLOW_PRESSURE && !L.energy)
+        return fail("a QSIDE or QCONV condition needs the energy equation");
+      for (int k = d->ibc_ptr[c]; k < d->ibc_ptr[c + 1]; k++) {
+        if (d->ibc_elem[k] < 0 || d->ibc_elem[k] >= L.num_elems || d->ibc_side[k] < 1 ||
+            d->ibc_side[k] > maxside)
+          return fail("integrated boundary condition side out of range");
+        se.push_back(d->ibc_elem[k]);
+        ss.push_back(d->ibc_side[k]);
+        st.push_back(ty);
+        sv.push_back(d->ibc_value[2 * c]);
+        sv.push_back(d->ibc_value[2 * c + 1]);
+      }
+    }
+    num_sides = (int)se.size();
+    if (num_sides > 0 &&
+        (upload(&d_side_elem, se, "sides") || upload(&d_side_side, ss, "sides") ||
+         upload(&d_side_type, st, "sides") || upload(&d_side_val, sv, "sides")))
+      return -1;
+  }
   if ((e = cudaMalloc(&d_x, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "x");
   if ((e = cudaMalloc(&d_R, sizeof(double) * L.N)) != cudaSuccess) return cuda_fail(e, "R");
   if ((e = cudaMalloc(&d_vals, sizeof(double) * L.nnz)) != cudaSuccess)
@@ -277,6 +305,11 @@ int Context::assemble(const double *x, double *R, double *vals, cudaStream_t st)
                                   d_color_elems + L.color_ptr[c], n, st);
       if (e != cudaSuccess) return cuda_fail(e, "species assembly launch");
     }
+  }
+  if (num_sides > 0) {
+    SideArgs sa{num_sides, d_side_elem, d_side_side, d_side_type, d_side_val};
+    e = launch_assemble_sides(a, sa, L.dim, L.energy != 0, st);
+    if (e != cudaSuccess) return cuda_fail(e, "boundary condition launch");
   }
   if (timing) {
     cudaEventRecord(ev_k1, st);

@@ -56,6 +56,10 @@ struct Context {
   const double *d_xdot = nullptr;
   double mass_c = 0.0;
   double *d_msr = nullptr;
+  // integrated boundary conditions, one entry per side
+  int num_sides = 0;
+  int *d_side_elem = nullptr, *d_side_side = nullptr, *d_side_type = nullptr;
+  double *d_side_val = nullptr;
   std::unique_ptr<Solver> solver;
   // optional kernel timing of the element kernels (events on the launch stream)
   bool timing = false;

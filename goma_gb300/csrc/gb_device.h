@@ -55,8 +55,22 @@ struct AsmArgs {
   MaterialDev mat;
 };
 
+// Integrated boundary conditions, one entry per element side (the cards of
+// gb_problem_desc expanded): element, Exodus side number, GB_IBC_* type and
+// the card's two values.  Device pointers.
+struct SideArgs {
+  int num_sides;
+  const int *elem;
+  const int *side;
+  const int *type;
+  const double *val;  // 2 per side
+};
+
 cudaError_t launch_assemble(const AsmArgs &a, int dim, bool energy, bool carreau, bool jac,
                             const int *elems, int nelem, cudaStream_t st);
+// the side terms (gb_assemble_bc.cu); launched after the element kernels
+cudaError_t launch_assemble_sides(const AsmArgs &a, const SideArgs &s, int dim, bool energy,
+                                  cudaStream_t st);
 size_t assemble_smem_bytes(int dim, bool energy, bool carreau);
 // species rows (gb_assemble_species.cu); launched after the flow kernel of
 // the same colour

@@ -49,7 +49,8 @@ def test_analytic_jacobian_matches_finite_differences(prob_fn):
 
 @pytest.mark.parametrize("name", ["cav2d_2x2", "cav2d_3x2_pert", "bfs2d_4x2_carreau",
                                   "box3d_2x2x2_bouss", "box3d_2x1x3_carreau_t",
-                                  "box3d_2x2x2_species"])
+                                  "box3d_2x2x2_species", "bratu2d_4x4_pert",
+                                  "channel2d_4x3_ibc", "box3d_2x2x2_ibc"])
 def test_gpu_jacobian_passes_the_reference_checker_like_the_reference(name):
     """The reference's own Jacobian checker (numerical_jacobian with
     Debug = -2, src/mm_numjac.c:716, restated in tests/numjac_check.py) on

@@ -35,7 +35,8 @@ def _layout(o, prob):
     return nj.Layout(prob, o.first_unknown(prob.mesh.num_nodes))
 
 
-@pytest.mark.parametrize("name", ["cav2d_2x2", "cav2d_3x2_pert", "bfs2d_4x2_carreau"])
+@pytest.mark.parametrize("name", ["cav2d_2x2", "cav2d_3x2_pert", "bfs2d_4x2_carreau",
+                                  "bratu2d_4x4_pert", "channel2d_4x3_ibc"])
 def test_checker_on_oracle_flags_what_the_reference_flagged(name):
     with open(REF) as f:
         ref = json.load(f)[name]
