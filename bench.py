@@ -333,6 +333,57 @@ def reacting_channel_assembly(nx, ny, nz, steps=3, warmup=2):
     return out
 
 
+def reacting_channel_solve(nx=64, ny=64, nz=32, tol=1e-8, max_newton=15, max_linear_its=2000,
+                           krylov=60):
+    """The reacting channel (HEX27 Q2/P1 Navier-Stokes + energy + 2 Arrhenius
+    species, 7.0 M unknowns at 64 x 64 x 32) solved by Newton from the inflow
+    state (u = 1, T = 1.5, Y_0 = 1, Y_1 = 0 inside, the Dirichlet values on
+    the boundary) to the scaled residual `tol`, with FP32-inner ILU(0)-GMRES
+    inside FP64 refinement and Eisenstat-Walker forcing: time, Newton and
+    Krylov counts and the per-phase split.  The reference's 32-bit MSR cannot
+    hold this problem."""
+    import time as _time
+
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    t0 = _time.perf_counter()
+    prob = pb.reacting_channel_3d(nx, ny, nz, seed=0)
+    gn = GomaNewton(prob)
+    gn.set_ilu_ordering(0)
+    setup_s = _time.perf_counter() - t0
+    fu = np.empty(prob.mesh.num_nodes + 1, np.int32)
+    from goma_gb300 import _lib
+    _lib.check(gn._L.gb_first_unknown(gn.h, fu.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    x = np.zeros(gn.N)
+    x[fu[:-1] + 0] = 1.0          # u
+    x[fu[:-1] + 3] = 1.5          # T
+    x[fu[:-1] + 4] = 1.0          # Y_0
+    x = gn.dirichlet_init(x)
+    torch.cuda.synchronize()
+    t1 = _time.perf_counter()
+    x, conv, st = gn.solve_nonlinear_problem(
+        x, residual_tol=tol, linear_tol=1e-8, max_newton=max_newton,
+        max_linear_its=max_linear_its, krylov_dim=krylov, fp32_inner=True, inner_tol=1e-3,
+        forcing=1, forcing_max=1e-2)
+    torch.cuda.synchronize()
+    dt = _time.perf_counter() - t1
+    out = {"workload": "reacting channel %dx%dx%d HEX27 Q2/P1 NS + energy + 2 Arrhenius species, "
+                       "Newton from the inflow state to scaled |R| < %g, FP32-inner "
+                       "ILU(0)-GMRES(%d), forcing rule" % (nx, ny, nz, tol, krylov),
+           "unknowns": gn.N, "csr_nnz": gn.nnz, "converged": conv, "seconds": dt,
+           "layout_and_upload_s": setup_s, "newton_its": st["newton_its"],
+           "linear_its": st["linear_its"], "residual_l2": st["residual_l2"],
+           "newton_seconds": {k.replace("_ms", ""): st[k] * 1e-3
+                              for k in ("assemble_ms", "scale_ms", "factor_ms", "solve_ms",
+                                        "total_ms")}}
+    print("reacting_solve:", {k: out[k] for k in ("converged", "seconds", "newton_its",
+                                                  "linear_its")}, file=sys.stderr, flush=True)
+    gn.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def batch_sweep_assembly(num=512, seed=0, steps=3, warmup=2):
     """Assembly throughput of the 512-problem sweep held as one union: one
     launch per colour over every problem's elements, per-element Reynolds
@@ -936,6 +987,8 @@ def main():
                 extra[w] = factorization_reuse_solves(16)
             elif w == "cpu_solve":
                 extra[w] = cpu_time_to_solve(8)
+            elif w == "reacting_solve":
+                extra[w] = reacting_channel_solve()
             elif w.startswith("krylov"):
                 extra[w] = krylov_kernels(int(w[len("krylov"):] or 16))
         line["workloads"] = extra
