@@ -63,6 +63,8 @@ def load():
         "gb_msr_pattern": (ctypes.c_int, [vp, ip]),
         "gb_msr_pattern_host": (ctypes.c_int, [vp, ip, llp]),
         "gb_csr_pattern": (ctypes.c_int, [vp, llp, ip]),
+        "gb_sweep_order_host": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_ushort),
+                                               ip, ip]),
         "gb_csr_row": (ctypes.c_longlong, [vp, vp, ctypes.c_int, llp, ip, dp, ctypes.c_longlong]),
         "gb_matrix_fill_full_transient": (ctypes.c_int, [vp, dp, dp, ctypes.c_double,
                                                          ctypes.c_double, dp, dp]),

@@ -435,6 +435,29 @@ int gb_ilu_permutation_host(const gb_problem_desc *desc, int *perm, int *num_col
   return 0;
 }
 
+int gb_sweep_order_host(const gb_problem_desc *desc, int ordering, unsigned short *rel,
+                        int *lev, int *levu) {
+  if (!desc || !rel) return fail("NULL argument");
+  gb::Layout L, Lp;
+  if (gb::build_layout(desc, L, gb::g_err) != 0) return -1;
+  const gb::Layout *LP = &L;
+  if (ordering == GB_ILU_MULTICOLOUR) {
+    std::vector<int> pm, um;
+    std::vector<int64_t> vm;
+    gb::multicolour_order(L, pm);
+    gb::permute_layout(L, pm, Lp, um, vm);
+    LP = &Lp;
+  }
+  gb::IluSchedule S;
+  gb::build_ilu_schedule(*LP, S);
+  std::vector<uint16_t> r;
+  if (gb::build_sweep_order(*LP, S.lev, S.levu, r)) return fail("a matrix row is too long");
+  memcpy(rel, r.data(), sizeof(uint16_t) * r.size());
+  if (lev) memcpy(lev, S.lev.data(), sizeof(int) * S.lev.size());
+  if (levu) memcpy(levu, S.levu.data(), sizeof(int) * S.levu.size());
+  return 0;
+}
+
 int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx) {
   if (!ctx || !rowptr || !colidx) return fail("NULL argument");
   const gb::Layout &L = ctx->c.L;

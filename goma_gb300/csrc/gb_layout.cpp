@@ -378,3 +378,63 @@ void permute_layout(const Layout &L, const std::vector<int> &perm, Layout &Lp,
 }
 
 }  // namespace gb
+
+namespace gb {
+
+int build_sweep_order(const Layout &L, const std::vector<int> &lev, const std::vector<int> &levu,
+                      std::vector<uint16_t> &rel) {
+  rel.assign((size_t)L.nnz, 0);
+  const int Tr = L.energy ? L.dim : -1;
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : bad)
+  for (int n = 0; n < L.num_nodes; n++) {
+    const int b = L.nbr_ptr[n], e = L.nbr_ptr[n + 1];
+    // neighbour slots below and above n, by level then node number
+    std::vector<int> lo, up;
+    for (int s = b; s < e; s++) {
+      const int m = L.nbr_node[s];
+      if (m < n) lo.push_back(s);
+      if (m > n) up.push_back(s);
+    }
+    std::stable_sort(lo.begin(), lo.end(), [&](int a, int c) {
+      return lev[L.nbr_node[a]] < lev[L.nbr_node[c]];
+    });
+    std::stable_sort(up.begin(), up.end(), [&](int a, int c) {
+      return levu[L.nbr_node[a]] < levu[L.nbr_node[c]];
+    });
+    const int f0 = L.fu[n], nr = L.fu[n + 1] - f0;
+    for (int r = 0; r < nr; r++) {
+      const int64_t i = f0 + r;
+      const bool rowT = r == Tr;
+      auto off = [&](int s) { return rowT ? L.nbr_offT[s] : L.nbr_off[s]; };
+      auto len = [&](int s) {
+        const int q = L.nbr_node[s];
+        return rowT ? L.nvn : L.fu[q + 1] - L.fu[q];
+      };
+      // lower segment starts at the row start; upper at the first column
+      // after the own node's block
+      int self = b;
+      while (L.nbr_node[self] != n) self++;
+      const int64_t lo0 = L.rowptr[i];
+      const int64_t up0 = L.rowptr[i] + off(self) + len(self);
+      int64_t k = 0;
+      for (int s : lo)
+        for (int t = 0; t < len(s); t++) {
+          const int64_t v = off(s) + t;
+          if (v > 65535) bad = 1;
+          rel[(size_t)(lo0 + k++)] = (uint16_t)v;
+        }
+      k = 0;
+      const int64_t base = off(self) + len(self);
+      for (int s : up)
+        for (int t = 0; t < len(s); t++) {
+          const int64_t v = off(s) + t - base;
+          if (v > 65535) bad = 1;
+          rel[(size_t)(up0 + k++)] = (uint16_t)v;
+        }
+    }
+  }
+  return bad ? -1 : 0;
+}
+
+}  // namespace gb

@@ -46,6 +46,16 @@ void permute_layout(const Layout &L, const std::vector<int> &perm, Layout &Lp,
 // so that every pressure pivot comes after all velocities of its element.
 // Returns perm (old node -> new node) and the number of colours.
 int multicolour_order(const Layout &L, std::vector<int> &perm);
+// Order in which a sync-free triangular sweep adds each row's off-node
+// entries: the lower neighbours of node n (m < n) by ascending dependency
+// level lev[m], the upper ones by ascending levu[m] (ties by node number),
+// so the values a row needs first are the ones published longest ago.
+// rel[p], for CSR position p of a row's off-node lower segment [rowptr[i],
+// diag(i) - r) or upper segment [diag(i) + 1 + na, rowptr[i+1]), is the
+// position within the same segment of the entry to take p-th.  Returns -1
+// when a segment is longer than 65,535 entries.
+int build_sweep_order(const Layout &L, const std::vector<int> &lev, const std::vector<int> &levu,
+                      std::vector<uint16_t> &rel);
 // MSR pattern of the reference (diagonal first, off-diagonals ascending).
 void layout_msr_pattern(const Layout &L, int *ija);
 int64_t layout_msr_length(const Layout &L);

@@ -547,6 +547,7 @@ struct TrsvArgs {
   const int64_t *rowptr;
   const int *colidx;
   const int64_t *diag;
+  const uint16_t *rel; // entry p of an off-node segment is taken from segment start + rel[p]
   int num_nodes;
   int Tr;              // local index of the energy row, -1 without energy
   int nvn;             // nodal fields per node
@@ -670,8 +671,9 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
 #pragma unroll
       for (int k = 0; k < kPrefetch; k++) {
         const int64_t p = pr0 + lane + 32 * k;
-        pv[k] = p < pr1 ? (A)lu[p] : (A)0;
-        pc[k] = p < pr1 ? g.colidx[p] : -1;
+        const int64_t q = p < pr1 ? pr0 + g.rel[p] : 0;  // level-sorted entry order
+        pv[k] = p < pr1 ? (A)lu[q] : (A)0;
+        pc[k] = p < pr1 ? g.colidx[q] : -1;
       }
       if (LOWER ? lane < r : lane < na) ov = (A)lu[LOWER ? di - r + lane : di + 1 + lane];
       if (!LOWER && lane == 0) dv = (A)lu[di];
@@ -686,8 +688,13 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
     bool gave_up = false;
     for (int r = warp; r < nr; r += NW) {
       A s0 = 0;
-      int64_t p, p1;
-      if (r == warp) {  // the prefetched row: poll its values, then add in order
+      int64_t p, p1, sb;  // sb: start of the row's off-node segment
+      if (r == warp) {
+        // the prefetched row: load all its values at once, then add them in
+        // the fixed (level-sorted, oldest first) order, each as soon as it
+        // and every earlier one are published -- the values published long
+        // ago are added while the newest ones are still awaited, and every
+        // wait re-polls all the values still pending
         A zv[kPrefetch];
         unsigned pending = 0;
 #pragma unroll
@@ -699,45 +706,51 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
           }
         }
         long long polls = 0;
-        while (pending) {
-          if (++polls > g.spin_limit || ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
-            gave_up = true;
-            break;
-          }
-          __nanosleep(32);
 #pragma unroll
-          for (int k = 0; k < kPrefetch; k++) {
-            if (pending & (1u << k)) {
-              const T v = ld_relaxed(x + pc[k]);
-              if (!unpublished(v)) {
-                zv[k] = (A)v;
-                pending &= ~(1u << k);
+        for (int k = 0; k < kPrefetch; k++) {
+          while (!gave_up && (pending & (1u << k))) {
+            if (++polls > g.spin_limit ||
+                ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
+              gave_up = true;
+              break;
+            }
+            __nanosleep(32);
+#pragma unroll
+            for (int j = 0; j < kPrefetch; j++) {
+              if (j >= k && (pending & (1u << j))) {
+                const T v = ld_relaxed(x + pc[j]);
+                if (!unpublished(v)) {
+                  zv[j] = (A)v;
+                  pending &= ~(1u << j);
+                }
               }
             }
           }
-        }
-#pragma unroll
-        for (int k = 0; k < kPrefetch; k++)
           if (pc[k] >= 0) s0 = fmx(pv[k], zv[k], s0);
+        }
         p = pr0 + lane + 32 * kPrefetch;
         p1 = pr1;
+        sb = pr0;
       } else {
         const int i = f0 + r;
         const int64_t di = g.diag[i];
         const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
         if (LOWER) {
-          p = g.rowptr[i] + lane;
+          sb = g.rowptr[i];
           p1 = di - r;
           if (lane < r) own[r][lane] = (A)lu[di - r + lane];
         } else {
-          p = di + 1 + na + lane;
+          sb = di + 1 + na;
           p1 = g.rowptr[i + 1];
           if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
           if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
         }
+        p = sb + lane;
       }
-      for (; p < p1; p += 32) s0 = fmx((A)lu[p], (A)poll_value(x + g.colidx[p], gave_up, g.error, g.spin_limit),
-                                       s0);
+      for (; p < p1; p += 32) {
+        const int64_t q = sb + g.rel[p];
+        s0 = fmx((A)lu[q], (A)poll_value(x + g.colidx[q], gave_up, g.error, g.spin_limit), s0);
+      }
       const A sum = wsum(s0);
       if (lane == 0) part[r] = sum;
     }
@@ -815,6 +828,7 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.rowptr = S->P.rowptr;
   g.colidx = S->P.colidx;
   g.diag = S->P.diag;
+  g.rel = S->d_sweep_rel;
   g.num_nodes = S->C->L.num_nodes;
   g.Tr = S->C->L.energy ? S->C->L.dim : -1;
   g.nvn = S->C->L.nvn;
@@ -847,6 +861,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
     std::vector<int> fill(maxl + 1, 0);
     for (int n = 0; n < nn; n++) S.lo_nodes[S.lo_ptr[lev[n]] + fill[lev[n]]++] = n;
   }
+  S.lev = lev;
   std::vector<int> levu(nn, 0);
   int maxu = 0;
   for (int n = nn - 1; n >= 0; n--) {
@@ -866,6 +881,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
     std::vector<int> fill(maxu + 1, 0);
     for (int n = 0; n < nn; n++) S.up_nodes[S.up_ptr[levu[n]] + fill[levu[n]]++] = n;
   }
+  S.levu = levu;
 }
 
 // ------------------------------------------------------------ Solver
@@ -960,6 +976,14 @@ int Solver::init(Context *c, int krylov) {
   up_ptr = S.up_ptr;
   num_levels = (int)lo_ptr.size() - 1;
   lo_nodes_host = S.lo_nodes;
+  {
+    std::vector<uint16_t> rel;
+    if (build_sweep_order(*LP, S.lev, S.levu, rel)) return fail("a matrix row is too long for the sweeps");
+    GB_CU(cudaMalloc(&d_sweep_rel, sizeof(uint16_t) * rel.size()), "sweep order");
+    owned.push_back(d_sweep_rel);
+    GB_CU(cudaMemcpy(d_sweep_rel, rel.data(), sizeof(uint16_t) * rel.size(),
+                     cudaMemcpyHostToDevice), "sweep order");
+  }
   GB_CU(cudaMalloc(&d_lo_nodes, sizeof(int) * S.lo_nodes.size()), "sched");
   GB_CU(cudaMemcpy(d_lo_nodes, S.lo_nodes.data(), sizeof(int) * S.lo_nodes.size(),
                    cudaMemcpyHostToDevice), "sched");

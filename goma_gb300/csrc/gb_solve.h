@@ -18,6 +18,7 @@ struct Context;
 struct IluSchedule {
   std::vector<int> lo_nodes, lo_ptr;  // forward (L) levels
   std::vector<int> up_nodes, up_ptr;  // backward (U) levels
+  std::vector<int> lev, levu;         // every node's forward / backward level
 };
 void build_ilu_schedule(const Layout &L, IluSchedule &S);
 
@@ -68,6 +69,7 @@ struct Solver {
   int *d_lo_nodes = nullptr, *d_up_nodes = nullptr;
   std::vector<int> lo_ptr, up_ptr;
   std::vector<int> lo_nodes_host;  // the lower sweep's order (host copy)
+  uint16_t *d_sweep_rel = nullptr; // level-sorted entry order of the sweeps (build_sweep_order)
   int *d_lo_nodes_rev = nullptr;   // it reversed, for the injected sweep fault
   const double *d_A = nullptr;  // scaled FP64 matrix the factors were built from
   double pivot_tau = 1e-4;      // ILU(0) pivot floor on the row-scaled matrix

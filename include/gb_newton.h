@@ -57,6 +57,16 @@ int gb_msr_pattern_host(const gb_problem_desc *desc, int *ija, long long *msr_le
  * (nnz).  Any output may be NULL. */
 int gb_ilu_permutation_host(const gb_problem_desc *desc, int *perm, int *num_colours, int *umap,
                             long long *rowptr, int *colidx, long long *vmap);
+/* Host only: the order in which the sync-free ILU(0) sweeps add each row's
+ * off-node entries (oldest dependency level first) for the given node
+ * ordering (GB_ILU_*), in the CSR layout of that ordering (the permuted one
+ * of gb_ilu_permutation_host for GB_ILU_MULTICOLOUR): entry p of a row's
+ * off-node lower or upper segment is read from the segment's start +
+ * rel[p] (nnz values); lev / levu (num_nodes, may be NULL) get every
+ * node's forward / backward dependency level.  For inspecting the sweeps;
+ * no counterpart in the reference. */
+int gb_sweep_order_host(const gb_problem_desc *desc, int ordering, unsigned short *rel,
+                        int *lev, int *levu);
 /* CSR pattern used on the device: rowptr (N+1, int64), colidx (nnz). */
 int gb_csr_pattern(const gb_ctx *ctx, long long *rowptr, int *colidx);
 /* One row of the CSR matrix: its 64-bit start offset in the CSR arrays, its

@@ -94,3 +94,58 @@ def _old_node_of_unknowns(N, prob):
     counts = np.array([nvn + (dim + 1 if n in cent else 0) for n in range(nn)])
     assert counts.sum() == N
     return np.repeat(np.arange(nn), counts)
+
+
+@pytest.mark.parametrize("ordering", [0, 1], ids=["natural", "multicolour"])
+@pytest.mark.parametrize("prob_fn", [
+    lambda: pb.lid_cavity_2d(4),
+    lambda: pb.boussinesq_cube_3d(3),
+    lambda: pb.reacting_channel_3d(2, 2, 1),
+], ids=["cavity2d", "bouss3d", "reacting3d"])
+def test_sweep_order_is_a_level_sorted_permutation_of_each_segment(prob_fn, ordering):
+    """The order in which the sync-free sweeps read a row's off-node entries
+    (checked here on the host before any sweep uses it): within every
+    row's lower segment [row start, own block) and upper segment (after the
+    own block, row end) it is a permutation of the segment's positions, it
+    stays inside the segment, and it takes the neighbour nodes by ascending
+    dependency level (forward levels for the lower, backward for the
+    upper segment)."""
+    prob = prob_fn()
+    L = _lib.load()
+    desc, keep = pb.make_desc(prob)
+    ija = msr_pattern_host(prob)
+    N = int(ija[0]) - 1
+    nnz = len(ija) - 1
+    nn = prob.mesh.num_nodes
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))  # noqa: E731
+    rel = np.empty(nnz, np.uint16)
+    lev = np.empty(nn, np.int32)
+    levu = np.empty(nn, np.int32)
+    _lib.check(L.gb_sweep_order_host(ctypes.byref(desc), ordering, P(rel, ctypes.c_ushort),
+                                     P(lev, ctypes.c_int), P(levu, ctypes.c_int)))
+    if ordering == 0:
+        rp, ci = _csr_from_msr(ija, N)
+        node = _old_node_of_unknowns(N, prob)
+    else:
+        perm = np.empty(nn, np.int32)
+        umap = np.empty(N, np.int32)
+        rp = np.empty(N + 1, np.int64)
+        ci32 = np.empty(nnz, np.int32)
+        _lib.check(L.gb_ilu_permutation_host(ctypes.byref(desc), P(perm, ctypes.c_int), None,
+                                             P(umap, ctypes.c_int), P(rp, ctypes.c_longlong),
+                                             P(ci32, ctypes.c_int), None))
+        ci = ci32.astype(np.int64)
+        node = perm[_old_node_of_unknowns(N, prob)[umap]]
+    del keep
+    for i in range(N):
+        n = node[i]
+        cols = ci[rp[i]:rp[i + 1]]
+        own = np.flatnonzero(node[cols] == n)
+        lo0, lo1 = rp[i], rp[i] + own[0]
+        up0, up1 = rp[i] + own[-1] + 1, rp[i + 1]
+        for s0, s1, lv, below in ((lo0, lo1, lev, True), (up0, up1, levu, False)):
+            r = rel[s0:s1].astype(np.int64)
+            assert np.array_equal(np.sort(r), np.arange(s1 - s0)), i
+            nodes = node[ci[s0 + r]]
+            assert np.all(nodes < n) if below else np.all(nodes > n)
+            assert np.all(np.diff(lv[nodes]) >= 0), i
