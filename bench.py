@@ -151,7 +151,7 @@ def cpu_baseline(nel=NEL, threads=None, steps=1):
     return out
 
 
-def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=60,
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=150,
                   forcing=1, reference_solver=True, modes=None, budget_s=None,
                   factorization_reuse=0, max_linear_its=4000):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
@@ -334,7 +334,7 @@ def reacting_channel_assembly(nx, ny, nz, steps=3, warmup=2):
 
 
 def reacting_channel_solve(nx=64, ny=64, nz=32, tol=1e-8, max_newton=15, max_linear_its=2000,
-                           krylov=60):
+                           krylov=150):
     """The reacting channel (HEX27 Q2/P1 Navier-Stokes + energy + 2 Arrhenius
     species, 7.0 M unknowns at 64 x 64 x 32) solved by Newton from the inflow
     state (u = 1, T = 1.5, Y_0 = 1, Y_1 = 0 inside, the Dirichlet values on
@@ -673,7 +673,7 @@ def krylov_kernels(nel, iters=30, ra=1e4):
 
 
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
-                     predictors=("zeroth", "secant", "learned")):
+                     predictors=("zeroth", "secant", "learned"), krylov=150):
     """The learned-predictor configuration: backward-facing step, nx x ny
     QUAD9 Q2/P1, Carreau-Yasuda fluid (mu0 = 1, mu_inf = 0.01, lambda = 1,
     a = 2, n = 0.5), Re re0 -> re1 in nsteps uniform continuation steps, the
@@ -692,7 +692,7 @@ def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150
     for pred in predictors:
         gn = GomaNewton(pb.carreau_step_2d(nx, ny, re0))
         opts = dict(residual_tol=1e-10, linear_tol=1e-8, max_newton=25, max_linear_its=3000,
-                    forcing=1, forcing_max=1e-2)
+                    krylov_dim=krylov, forcing=1, forcing_max=1e-2)
         t0 = _time.perf_counter()
         recs, _ = continuation(gn, re0, re1, nsteps, predictor=pred, newton_opts=opts,
                                learned_opts=dict(steps=300, batch=4096, lr=2e-3),
@@ -774,7 +774,10 @@ def main():
                          "(default: plain_fp64, secant_fp32, learned_fp32)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
                     help="seconds per run of the time-to-solve leg (0: no limit)")
-    ap.add_argument("--solve-krylov", type=int, default=60,
+    ap.add_argument("--bfs-budget", type=float, default=150.0,
+                    help="seconds per predictor of the bfs workload (the 200-step sweep stops "
+                         "there)")
+    ap.add_argument("--solve-krylov", type=int, default=150,
                     help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
                     help="Krylov iteration limit of one linear solve in the time-to-solve leg")
@@ -980,7 +983,7 @@ def main():
                                              max_ratio=1.6, budget_s=900.0, check=1,
                                              max_linear_its=2500)
             elif w == "bfs":
-                extra[w] = bfs_continuation()
+                extra[w] = bfs_continuation(budget_s=args.bfs_budget)
             elif w == "ilu_orders":
                 extra[w] = ilu_orders()
             elif w == "reuse":
