@@ -268,14 +268,16 @@ __global__ void spmv_kernel(int N, const int64_t *__restrict__ rowptr,
                             const T *__restrict__ x, T *__restrict__ y) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) / LPR;
   const int l = threadIdx.x % LPR;
-  if (g >= N) return;
-  const int64_t r0 = rowptr[g], r1 = rowptr[g + 1];
+  const bool live = g < N;  // the whole warp takes part in the shuffles
   using A = acc_t<T>;
   A s = 0;
-  for (int64_t k = r0 + l; k < r1; k += LPR) s = fmx((A)vals[k], (A)__ldg(x + colidx[k]), s);
+  if (live) {
+    const int64_t r0 = rowptr[g], r1 = rowptr[g + 1];
+    for (int64_t k = r0 + l; k < r1; k += LPR) s = fmx((A)vals[k], (A)__ldg(x + colidx[k]), s);
+  }
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
-  if (l == 0) y[g] = (T)s;
+  if (live && l == 0) y[g] = (T)s;
 }
 
 // ------------------------------------------------------------ ILU(0)
@@ -1078,6 +1080,10 @@ static int lanes_per_row(const Layout &L) {
 
 template <class T>
 static cudaError_t spmv(const Context *C, int lpr, const T *vals, const T *x, T *y, cudaStream_t st) {
+  // FP64: 8 lanes a row.  On GB300 the FP64 product is bound by the FP64
+  // pipe as much as by HBM (ncu: pipe 89 % busy at 32 lanes a row, half of it
+  // the shuffle-reduction adds); 8 lanes cut those adds to a sixth.
+  if (sizeof(T) == 8) lpr = 8;
   const int N = C->L.N, threads = 256;
   const int blocks = (int)(((int64_t)N * lpr + threads - 1) / threads);
   switch (lpr) {
