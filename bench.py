@@ -922,9 +922,17 @@ def main():
     bytes_asm = 8 * nnz + 8 * N + 8 * N + 4 * elems * 27 + 8 * 3 * nodes
     bytes_launch = bytes_asm / gn.num_colors
     hbm_gbs = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+    # DRAM traffic of one launch: the 16^3 capture of the same kernel (ncu,
+    # one 512-element launch: dram__bytes_read 71.0 MB + write 13.3 MB,
+    # profiles/assemble_sf_kernel_hex27_boussinesq.md) scaled by the elements
+    # of this launch; the traffic is the matrix update per element, so it
+    # grows in proportion
+    traffic = (71.0e6 + 13.3e6) / 512 * elems_per_launch if args.path in (0, 4) else None
     roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": fp64_peak,
                 "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one 512-element "
+                                  "launch at 16^3 (ncu), scaled to this launch's elements",
                 "kernel": "%s, one colour, %d elements" % (kernel_name, elems_per_launch),
                 "launch_ms": per_launch_ms,
                 "flop_per_element": flop_el,
