@@ -318,35 +318,80 @@ struct IluArgs {
   const int *fu;
   const int64_t *rowptr;
   const int *nbr_ptr, *nbr_node, *nbr_off, *nbr_offT;
+  const int *nbr_self;  // every node's own position in its neighbour list
   int dim, nvn, energy;
   int maxnb, lmax, maxnr;
   double tau;
   int *nfix;
 };
 
+// Shared memory of one ilu0_block_kernel CTA (element type of size tsize).
+static size_t ilu_smem_bytes(size_t tsize, int maxnb, int maxnr, int lmax) {
+  return sizeof(int64_t) * (size_t)maxnb * maxnr +                          // srow
+         tsize * ((size_t)maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs + kMaxNodeDofs) +
+         sizeof(int) * (11 * (size_t)maxnb + 4);
+}
+
+// ILU(0) of one node's block row (one CTA per node, the nodes of one
+// dependency level per launch).  The block row of node n -- its rows over
+// the columns of all its neighbours -- lives in shared memory.  For every
+// lower neighbour m, in increasing order:
+//   step 1  L_nm = A_nm U_mm^-1   (U_mm: m's diagonal block, already final)
+//   step 2  A_nq -= L_nm U_mq     for every neighbour q > m of m that is
+//                                 also a neighbour of n
+// then the diagonal block is factorised in place and the row written back.
+// Everything that depends only on the node graph and on finished nodes is
+// loaded up front for all m at once (their neighbour-list bounds, own
+// positions and row starts); per m one round of loads brings m's neighbour
+// list (with each neighbour's slot in n's list, found in shared memory) and
+// U_mm, and a second one the U_mq entries.  Step 2 runs over the compacted
+// list of shared neighbours, one thread per (neighbour, column), each thread
+// loading its U column once and updating all rows of n.  Step 1 multiplies
+// by reciprocal pivots computed once per m.
 template <class T>
 __global__ void __launch_bounds__(256)
     ilu0_block_kernel(const int *__restrict__ nodes, IluArgs g, const double *__restrict__ A,
                       T *__restrict__ lu) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  int64_t *srow = reinterpret_cast<int64_t *>(sm_raw);          // [16] row starts of node m
-  T *blk = reinterpret_cast<T *>(srow + kMaxNodeDofs);           // [maxnr][lmax]
+  int64_t *srow = reinterpret_cast<int64_t *>(sm_raw);          // [maxnb][maxnr] row starts of m
+  T *blk = reinterpret_cast<T *>(srow + (size_t)g.maxnb * g.maxnr);  // [maxnr][lmax]
   T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [16][16] L_nm
   T *umm = lnm + kMaxNodeDofs * kMaxNodeDofs;                    // [16][16] U_mm
-  int *snb = reinterpret_cast<int *>(umm + kMaxNodeDofs * kMaxNodeDofs);  // [maxnb]
-  int *soff = snb + g.maxnb;
-  int *sndof = soff + g.maxnb;
-  int *tmap = sndof + g.maxnb;                                   // [maxnb]
+  T *rdm = umm + kMaxNodeDofs * kMaxNodeDofs;                    // [16] 1 / U_mm diagonal
+  int *snb = reinterpret_cast<int *>(rdm + kMaxNodeDofs);        // [maxnb] neighbours of n
+  int *soff = snb + g.maxnb;                                     // their column offsets
+  int *sndof = soff + g.maxnb;                                   // their unknown counts
+  int *smb = sndof + g.maxnb;        // lower neighbour m: start of its neighbour list
+  int *smnb = smb + g.maxnb;         // its length
+  int *smoff = smnb + g.maxnb;       // m's own block in m's rows (offset, energy-row offset)
+  int *smoffT = smoff + g.maxnb;
+  int *tslot = smoffT + g.maxnb;     // per neighbour t of m: slot in n's list, or -1
+  int *toff = tslot + g.maxnb;       //   its column offsets in m's rows
+  int *toffT = toff + g.maxnb;
+  int *plist = toffT + g.maxnb;      // compacted t with tslot[t] >= 0
+  int *s_np = plist + g.maxnb;
   const int n = nodes[blockIdx.x];
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
   const int base = g.nbr_ptr[n], nb = g.nbr_ptr[n + 1] - base;
   const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
   const int Tr = g.energy ? g.dim : -1;  // local index of the energy row
+  const int self = g.nbr_self[n];
   for (int s2 = tid; s2 < nb; s2 += nt) {
     const int q = g.nbr_node[base + s2];
     snb[s2] = q;
     soff[s2] = g.nbr_off[base + s2];
-    sndof[s2] = g.fu[q + 1] - g.fu[q];
+    const int fq = g.fu[q];
+    sndof[s2] = g.fu[q + 1] - fq;
+    if (s2 < self) {
+      const int mb = g.nbr_ptr[q];
+      const int ms = g.nbr_self[q];
+      smb[s2] = mb;
+      smnb[s2] = g.nbr_ptr[q + 1] - mb;
+      smoff[s2] = g.nbr_off[mb + ms];
+      smoffT[s2] = g.nbr_offT[mb + ms];
+      for (int dk = 0; dk < g.fu[q + 1] - fq; dk++)
+        srow[(size_t)s2 * g.maxnr + dk] = g.rowptr[fq + dk];
+    }
   }
   __syncthreads();
   const int L = soff[nb - 1] + sndof[nb - 1];
@@ -366,20 +411,14 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
-  int self = 0;
-  {
-    int lo = 0, hi = nb - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (snb[mid] < n) lo = mid + 1; else hi = mid;
-    }
-    self = lo;
-  }
   __syncthreads();
   for (int sm = 0; sm < self; sm++) {
-    const int m = snb[sm], mb = g.nbr_ptr[m], mnb = g.nbr_ptr[m + 1] - mb;
-    const int fm = g.fu[m], nm = sndof[sm], cm = soff[sm];
-    // neighbours q > m of m that are also neighbours of n
+    const int m = snb[sm], mb = smb[sm], mnb = smnb[sm];
+    const int nm = sndof[sm], cm = soff[sm];
+    const int64_t *mrow = srow + (size_t)sm * g.maxnr;
+    // round A: m's neighbours q > m that are also neighbours of n (slot in
+    // n's list by binary search in shared memory), their column offsets,
+    // and U_mm
     for (int t = tid; t < mnb; t += nt) {
       const int q = g.nbr_node[mb + t];
       int slot = -1;
@@ -391,27 +430,33 @@ __global__ void __launch_bounds__(256)
         }
         if (snb[lo] == q) slot = lo;
       }
-      tmap[t] = slot;
-    }
-    // self slot of m in its own list (for U_mm)
-    int mself = 0;
-    {
-      int lo = 0, hi = mnb - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (g.nbr_node[mb + mid] < m) lo = mid + 1; else hi = mid;
+      tslot[t] = slot;
+      if (slot >= 0) {
+        toff[t] = g.nbr_off[mb + t];
+        toffT[t] = g.nbr_offT[mb + t];
       }
-      mself = lo;
     }
-    // U_mm and node m's row starts into shared memory (one round of loads)
-    if (tid < nm) srow[tid] = g.rowptr[fm + tid];
     for (int w = tid; w < nm * nm; w += nt) {
       const int dk = w / nm, d2 = w - dk * nm;
       const bool rowkT = dk == Tr;
       T u = (T)0;
       if (d2 >= dk && !(rowkT && d2 >= g.nvn))
-        u = lu[g.rowptr[fm + dk] + (rowkT ? g.nbr_offT[mb + mself] : g.nbr_off[mb + mself]) + d2];
+        u = lu[mrow[dk] + (rowkT ? smoffT[sm] : smoff[sm]) + d2];
       umm[dk * kMaxNodeDofs + d2] = u;
+    }
+    __syncthreads();
+    if (tid < nm) rdm[tid] = (T)1 / umm[tid * kMaxNodeDofs + tid];
+    if (tid < 32) {
+      // compact the shared neighbours (ascending t)
+      int cnt = 0;
+      for (int t0 = 0; t0 < mnb; t0 += 32) {
+        const int t = t0 + lane;
+        const bool hit = t < mnb && tslot[t] >= 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (hit) plist[cnt + __popc(bal & ((1u << lane) - 1u))] = t;
+        cnt += __popc(bal);
+      }
+      if (lane == 0) *s_np = cnt;
     }
     __syncthreads();
     // step 1: L_nm = A_nm U_mm^-1, one thread per row, from shared memory
@@ -423,7 +468,7 @@ __global__ void __launch_bounds__(256)
           lnm[r * kMaxNodeDofs + dk] = (T)0;
           continue;
         }
-        const T l = br[dk] / umm[dk * kMaxNodeDofs + dk];
+        const T l = br[dk] * rdm[dk];
         br[dk] = l;
         lnm[r * kMaxNodeDofs + dk] = l;
         for (int d2 = dk + 1; d2 < nm; d2++) {
@@ -433,24 +478,32 @@ __global__ void __launch_bounds__(256)
       }
     }
     __syncthreads();
-    // step 2: A_nq -= L_nm U_mq for every shared neighbour q > m, all
-    // (q, row, column) targets at once: f = (t, r, d), d fastest so that a
-    // warp reads consecutive entries of U_mq
-    const int per_t = nr * kMaxNodeDofs;
-    for (int f = tid; f < mnb * per_t; f += nt) {
-      const int t = f / per_t, rem = f - t * per_t;
-      const int r = rem / kMaxNodeDofs, d = rem - r * kMaxNodeDofs;
-      const int slot = tmap[t];
-      if (slot < 0 || d >= sndof[slot]) continue;
-      if (r == Tr && d >= g.nvn) continue;
-      const int off = g.nbr_off[mb + t], offT = g.nbr_offT[mb + t];
-      T acc = (T)0;
-      for (int dk = 0; dk < nm; dk++) {
-        const bool rowkT = dk == Tr;
-        if (rowkT && d >= g.nvn) continue;
-        acc += lnm[r * kMaxNodeDofs + dk] * (T)lu[srow[dk] + (rowkT ? offT : off) + d];
+    // step 2: A_nq -= L_nm U_mq, one thread per (shared neighbour, column d)
+    // loading the column of U_mq once and updating every row of n
+    const int np = *s_np;
+    for (int f = tid; f < np * g.maxnr; f += nt) {
+      const int k = f / g.maxnr, d = f - k * g.maxnr;
+      const int t = plist[k], slot = tslot[t];
+      if (d >= sndof[slot]) continue;
+      const int off = toff[t], offT = toffT[t];
+      T u[kMaxNodeDofs];
+#pragma unroll
+      for (int dk = 0; dk < kMaxNodeDofs; dk++) {
+        u[dk] = (T)0;
+        if (dk < nm && !(dk == Tr && d >= g.nvn)) u[dk] = lu[mrow[dk] + (dk == Tr ? offT : off) + d];
       }
-      blk[(size_t)r * g.lmax + soff[slot] + d] -= acc;
+      T *col = blk + soff[slot] + d;
+      for (int r = 0; r < nr; r++) {
+        if (r == Tr && d >= g.nvn) continue;
+        T acc = (T)0;
+#pragma unroll
+        for (int dk = 0; dk < kMaxNodeDofs; dk++) {
+          if (dk >= nm) break;
+          if (dk == Tr && d >= g.nvn) continue;
+          acc += lnm[r * kMaxNodeDofs + dk] * u[dk];
+        }
+        col[(size_t)r * g.lmax] -= acc;
+      }
     }
     __syncthreads();
   }
@@ -519,16 +572,17 @@ __global__ void __launch_bounds__(256)
 // values its rows reference, so it polls those values themselves until none
 // is the sentinel -- no per-node flag, no fence: each value is published by
 // one single-copy-atomic store.  The node is solved in two stages:
-//   A  all warps: for every row of the node, the dot product with the
-//      solution values of OTHER nodes (the long part of the row, rows spread
-//      over the warps; each lane keeps its polled values in registers and
-//      adds them in a fixed order, so the result does not depend on arrival
-//      order);
-//   B  warp 0, lane r for row r: the small in-node triangular solve, one
-//      shuffle per column, from the diagonal block held in shared memory.
-// A warp loads its first row's factor values, column indices, in-node
-// entries and the node's right-hand side before it polls, so only the
-// gather of the solution values stays on the critical path.  A node depends
+//   A  all warps: for every row of the node, the right-hand side less the
+//      dot product with the solution values of OTHER nodes (the long part of
+//      the row, rows spread over the warps; each lane keeps its polled values
+//      in registers and adds them in a fixed order, so the result does not
+//      depend on arrival order);
+//   B  warp 0, lane r for row r: row r of the node's precomputed diagonal-
+//      block inverse (block_inverse_kernel, in shared memory) times those
+//      values -- independent products, no chain of substitution steps.
+// A warp loads its first row's factor values and column indices, and the
+// CTA the block inverse, before it polls, so only the gather of the
+// solution values stays on the critical path.  A node depends
 // only on nodes of lower levels, which hold earlier tickets, and every CTA of
 // the grid is resident, so a value a CTA waits for is always owed by a CTA
 // that is running or done.  Every wait is bounded: past spin_limit polls the
@@ -554,6 +608,7 @@ struct TrsvArgs {
   const int *colidx;
   const int64_t *diag;
   const uint16_t *rel; // entry p of an off-node segment is taken from segment start + rel[p]
+  const int64_t *inv_ptr;  // node n's diagonal-block inverses start at inv_ptr[n] (L's, then U's)
   int num_nodes;
   int Tr;              // local index of the energy row, -1 without energy
   int nvn;             // nodal fields per node
@@ -618,38 +673,73 @@ __device__ __forceinline__ T poll_value(const T *p, bool &gave_up, const int *er
   return v;
 }
 
-// Stage B, shared by both sweeps: lane r of the calling warp solves row r of
-// the node's diagonal block.  L: unit lower triangle, own[r][c] = L(r, c)
-// for c < r.  U: own[r][j] = U(r, r+1+j) for j < na(r), rdg[r] = 1 / U(r, r).
-// v holds rhs - (off-node part) on entry; returns the solution of row r.
+// Dense inverses of every node's diagonal blocks of the factors: of the
+// unit lower block of L and of the upper block of U (nr x nr each, stored
+// column by column, entry (r, c) at c * nr + r; L's first).  With them a
+// sweep finishes a node with one small matrix-vector product,
+// x_n = D^-1 (b_n - off-node part), whose products are independent, in place
+// of a substitution whose steps each wait for the previous one.  Block
+// layout: a node's unknowns are contiguous and every row of the node holds
+// every own-node column except the energy row, which lacks the pressure
+// columns (they come last); row r's own-node columns start r entries before
+// its diagonal.  One warp per node, lane j computes column j of both
+// inverses by substitution.
+template <class T>
+__global__ void block_inverse_kernel(TrsvArgs g, const T *__restrict__ lu, T *__restrict__ inv) {
+  using A = acc_t<T>;
+  const int wpb = blockDim.x >> 5, j = threadIdx.x & 31;
+  for (int n = blockIdx.x * wpb + (threadIdx.x >> 5); n < g.num_nodes; n += gridDim.x * wpb) {
+    const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+    T *Li = inv + g.inv_ptr[n], *Ui = Li + nr * nr;
+    if (j >= nr) continue;
+    A x[kMaxNodeDofs];
+    // column j of L^-1: x_i = [i == j] - sum_{j <= c < i} L(i, c) x_c
+    for (int i = 0; i < nr; i++) {
+      A v = i == j ? (A)1 : (A)0;
+      if (i > j) {
+        const int64_t rb = g.diag[f0 + i] - i;  // row i's own-node columns start here
+        for (int c = j; c < i; c++) v -= (A)lu[rb + c] * x[c];
+      }
+      x[i] = v;
+      Li[(size_t)j * nr + i] = (T)v;
+    }
+    // column j of U^-1: x_i = ([i == j] - sum_{i < c <= j} U(i, c) x_c) / U(i, i)
+    for (int i = nr - 1; i >= 0; i--) {
+      A v = (A)0;
+      if (i <= j) {
+        const int64_t di = g.diag[f0 + i];
+        const int cend = i == g.Tr ? min(j, g.nvn - 1) : j;  // energy row: no pressure columns
+        v = i == j ? (A)1 : (A)0;
+        for (int c = i + 1; c <= cend; c++) v -= (A)lu[di + (c - i)] * x[c];
+        v = v / (A)lu[di];
+      }
+      x[i] = v;
+      Ui[(size_t)j * nr + i] = (T)v;
+    }
+  }
+}
+
+// Stage B, shared by the sweeps: lane r of the calling warp returns row r of
+// D^-1 bv, D^-1 the node's block inverse (entry (r, c) at inv_s[c * 16 + r],
+// lower triangular for L, upper for U), bv the rows' right-hand sides less
+// their off-node parts; the products are added in column order.
 template <class A, bool LOWER>
-__device__ __forceinline__ A node_block_solve(A v, int lane, int nr, int Tr, int nvn,
-                                              const A (*own)[kMaxNodeDofs], const A *rdg) {
-  if (LOWER) {
-    for (int c = 0; c < nr - 1; c++) {
-      const A zc = __shfl_sync(0xffffffffu, v, c);
-      if (lane > c && lane < nr) v = fmx(-own[lane][c], zc, v);
-    }
-  } else {
-    const int na = (lane == Tr ? nvn : nr) - 1 - lane;
-    for (int c = nr - 1; c >= 0; c--) {
-      if (lane == c) v *= rdg[c];
-      const A zc = __shfl_sync(0xffffffffu, v, c);
-      const int j = c - lane - 1;
-      if (j >= 0 && j < na) v = fmx(-own[lane][j], zc, v);
-    }
+__device__ __forceinline__ A node_block_apply(int lane, int nr, const A *inv_s, const A *bv) {
+  A v = (A)0;
+  if (lane < nr) {
+    for (int c = 0; c < nr; c++)
+      if (LOWER ? c <= lane : c >= lane) v = fmx(inv_s[c * kMaxNodeDofs + lane], bv[c], v);
   }
   return v;
 }
 
 template <class T, bool LOWER>
 __global__ void __launch_bounds__(kTrsvThreads, 3)
-    trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu, const T *__restrict__ b, T *x) {
+    trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu, const T *__restrict__ binv,
+                          const T *__restrict__ b, T *x) {
   using A = acc_t<T>;
-  __shared__ A part[kMaxNodeDofs];               // off-node sums per row
-  __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];  // own-node entries of the sweep's factor
-  __shared__ A rdg[kMaxNodeDofs];                // reciprocal U diagonal
-  __shared__ A rhs[kMaxNodeDofs];                // the node's right-hand side
+  __shared__ A bv[kMaxNodeDofs];                      // per row: rhs less the off-node part
+  __shared__ A inv_s[kMaxNodeDofs * kMaxNodeDofs];    // the node's block inverse, by column
   __shared__ int s_node;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
@@ -666,8 +756,6 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
     A pv[kPrefetch];
     int pc[kPrefetch];
     int64_t pr0 = 0, pr1 = 0;
-    A rv = 0, ov = 0, dv = 1;
-    if (tid < nr) rv = (A)__ldcg(b + f0 + tid);
     if (warp < nr) {
       const int r = warp, i = f0 + r;
       const int64_t di = g.diag[i];
@@ -681,18 +769,18 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
         pv[k] = p < pr1 ? (A)lu[q] : (A)0;
         pc[k] = p < pr1 ? g.colidx[q] : -1;
       }
-      if (LOWER ? lane < r : lane < na) ov = (A)lu[LOWER ? di - r + lane : di + 1 + lane];
-      if (!LOWER && lane == 0) dv = (A)lu[di];
     }
-    if (tid < nr) rhs[tid] = rv;
-    if (warp < nr) {
-      const int r = warp;
-      if (LOWER ? lane < r : lane < (r == g.Tr ? g.nvn : nr) - 1 - r) own[r][lane] = ov;
-      if (!LOWER && lane == 0) rdg[r] = (A)1 / dv;
+    {
+      const T *bi = binv + g.inv_ptr[n] + (LOWER ? 0 : nr * nr);
+      for (int w = tid; w < nr * nr; w += kTrsvThreads) {
+        const int c = w / nr;
+        inv_s[c * kMaxNodeDofs + (w - c * nr)] = (A)bi[w];
+      }
     }
     // stage A
     bool gave_up = false;
     for (int r = warp; r < nr; r += NW) {
+      const A rhs_r = (A)__ldcg(b + f0 + r);
       A s0 = 0;
       int64_t p, p1, sb;  // sb: start of the row's off-node segment
       if (r == warp) {
@@ -741,16 +829,8 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
         const int i = f0 + r;
         const int64_t di = g.diag[i];
         const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
-        if (LOWER) {
-          sb = g.rowptr[i];
-          p1 = di - r;
-          if (lane < r) own[r][lane] = (A)lu[di - r + lane];
-        } else {
-          sb = di + 1 + na;
-          p1 = g.rowptr[i + 1];
-          if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
-          if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
-        }
+        sb = LOWER ? g.rowptr[i] : di + 1 + na;
+        p1 = LOWER ? di - r : g.rowptr[i + 1];
         p = sb + lane;
       }
       for (; p < p1; p += 32) {
@@ -758,13 +838,12 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
         s0 = fmx((A)lu[q], (A)poll_value(x + g.colidx[q], gave_up, g.error, g.spin_limit), s0);
       }
       const A sum = wsum(s0);
-      if (lane == 0) part[r] = sum;
+      if (lane == 0) bv[r] = rhs_r - sum;
     }
     if (__syncthreads_or(gave_up) && tid == 0) atomicExch(g.error, 1);
     // stage B
     if (warp == 0) {
-      A v = lane < nr ? rhs[lane] - part[lane] : (A)0;
-      v = node_block_solve<A, LOWER>(v, lane, nr, g.Tr, g.nvn, own, rdg);
+      const A v = node_block_apply<A, LOWER>(lane, nr, inv_s, bv);
       if (lane < nr) st_relaxed(x + f0 + lane, (T)v);
     }
     __syncthreads();
@@ -780,33 +859,30 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
 template <class T, bool LOWER>
 __global__ void __launch_bounds__(kTrsvThreads)
     trsv_level_cta_kernel(const int *__restrict__ nodes, TrsvArgs g, const T *__restrict__ lu,
-                          T *__restrict__ z) {
+                          const T *__restrict__ binv, T *__restrict__ z) {
   using A = acc_t<T>;
-  __shared__ A part[kMaxNodeDofs];
-  __shared__ A own[kMaxNodeDofs][kMaxNodeDofs];
-  __shared__ A rdg[kMaxNodeDofs];
-  __shared__ A rhs[kMaxNodeDofs];
+  __shared__ A bv[kMaxNodeDofs];
+  __shared__ A inv_s[kMaxNodeDofs * kMaxNodeDofs];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
   const int n = nodes[blockIdx.x];
   const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
-  // the node's own right-hand side, all rows at once (only this CTA writes it)
-  if (tid < nr) rhs[tid] = (A)z[f0 + tid];
+  {
+    const T *bi = binv + g.inv_ptr[n] + (LOWER ? 0 : nr * nr);
+    for (int w = tid; w < nr * nr; w += kTrsvThreads) {
+      const int c = w / nr;
+      inv_s[c * kMaxNodeDofs + (w - c * nr)] = (A)bi[w];
+    }
+  }
+  // rows over the warps; a node's own right-hand side is read before any
+  // of its values is written (only this CTA writes them, after the barrier)
   for (int r = warp; r < nr; r += NW) {
     const int i = f0 + r;
     const int64_t di = g.diag[i];
     const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
-    int64_t p0, p1;
-    if (LOWER) {
-      p0 = g.rowptr[i];
-      p1 = di - r;
-      if (lane < r) own[r][lane] = (A)lu[di - r + lane];
-    } else {
-      p0 = di + 1 + na;
-      p1 = g.rowptr[i + 1];
-      if (lane < na) own[r][lane] = (A)lu[di + 1 + lane];
-      if (lane == 0) rdg[r] = (A)1 / (A)lu[di];
-    }
+    const int64_t p0 = LOWER ? g.rowptr[i] : di + 1 + na;
+    const int64_t p1 = LOWER ? di - r : g.rowptr[i + 1];
+    const A rhs_r = (A)z[i];
     A s0 = 0, s1 = 0;
     int64_t p = p0 + lane;
     for (; p + 32 < p1; p += 64) {
@@ -815,12 +891,11 @@ __global__ void __launch_bounds__(kTrsvThreads)
     }
     if (p < p1) s0 = fmx((A)lu[p], (A)z[g.colidx[p]], s0);
     const A sum = wsum(s0 + s1);
-    if (lane == 0) part[r] = sum;
+    if (lane == 0) bv[r] = rhs_r - sum;
   }
   __syncthreads();
   if (warp == 0) {
-    A v = lane < nr ? rhs[lane] - part[lane] : (A)0;
-    v = node_block_solve<A, LOWER>(v, lane, nr, g.Tr, g.nvn, own, rdg);
+    const A v = node_block_apply<A, LOWER>(lane, nr, inv_s, bv);
     if (lane < nr) z[f0 + lane] = (T)v;
   }
 }
@@ -835,6 +910,7 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.colidx = S->P.colidx;
   g.diag = S->P.diag;
   g.rel = S->d_sweep_rel;
+  g.inv_ptr = S->d_inv_ptr;
   g.num_nodes = S->C->L.num_nodes;
   g.Tr = S->C->L.energy ? S->C->L.dim : -1;
   g.nvn = S->C->L.nvn;
@@ -895,7 +971,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
 Solver::~Solver() {
   if (prec64) cudaGraphExecDestroy(prec64);
   if (prec32) cudaGraphExecDestroy(prec32);
-  void *p[] = {d_lu, d_lu32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
+  void *p[] = {d_lu, d_lu32, d_binv, d_binv32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
                d_sweep_y, d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
@@ -976,6 +1052,31 @@ int Solver::init(Context *c, int krylov) {
     P.nbr_off = c->d_nbr_off;
     P.nbr_offT = c->d_nbr_offT;
   }
+  {
+    std::vector<int> self(LP->num_nodes);
+    for (int n = 0; n < LP->num_nodes; n++) {
+      auto b = LP->nbr_node.begin() + LP->nbr_ptr[n], e = LP->nbr_node.begin() + LP->nbr_ptr[n + 1];
+      self[n] = (int)(std::lower_bound(b, e, n) - b);
+    }
+    int *d = nullptr;
+    GB_CU(cudaMalloc(&d, sizeof(int) * self.size()), "neighbour self positions");
+    owned.push_back(d);
+    GB_CU(cudaMemcpy(d, self.data(), sizeof(int) * self.size(), cudaMemcpyHostToDevice),
+          "neighbour self positions");
+    P.nbr_self = d;
+    // offsets of every node's diagonal-block inverses (L's and U's, nr^2 each)
+    std::vector<int64_t> ip(LP->num_nodes + 1, 0);
+    for (int n = 0; n < LP->num_nodes; n++) {
+      const int64_t nr = LP->fu[n + 1] - LP->fu[n];
+      ip[n + 1] = ip[n] + 2 * nr * nr;
+    }
+    inv_len = ip.back();
+    GB_CU(cudaMalloc(&d_inv_ptr, sizeof(int64_t) * ip.size()), "block inverse offsets");
+    owned.push_back(d_inv_ptr);
+    GB_CU(cudaMemcpy(d_inv_ptr, ip.data(), sizeof(int64_t) * ip.size(), cudaMemcpyHostToDevice),
+          "block inverse offsets");
+    GB_CU(cudaMalloc(&d_binv, sizeof(double) * inv_len), "block inverses");
+  }
   IluSchedule S;
   build_ilu_schedule(*LP, S);
   lo_ptr = S.lo_ptr;
@@ -1007,9 +1108,8 @@ int Solver::init(Context *c, int krylov) {
     lmax = std::max(lmax, LP->nbr_off[LP->nbr_ptr[n + 1] - 1] + LP->fu[q + 1] - LP->fu[q]);
   }
   {
-    const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
-    const size_t sm64 = sizeof(double) * ((size_t)(L.nvn + L.npres) * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
-    const size_t sm32 = sizeof(float) * ((size_t)(L.nvn + L.npres) * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
+    const size_t sm64 = ilu_smem_bytes(sizeof(double), maxnb, L.nvn + L.npres, lmax);
+    const size_t sm32 = ilu_smem_bytes(sizeof(float), maxnb, L.nvn + L.npres, lmax);
     if (sm64 > 200 * 1024) return fail("ILU(0) block row does not fit in shared memory");
     GB_CU(cudaFuncSetAttribute(ilu0_block_kernel<double>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64), "smem");
@@ -1095,7 +1195,8 @@ static cudaError_t spmv(const Context *C, int lpr, const T *vals, const T *x, T 
 }
 
 template <class T>
-static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, cudaGraphExec_t *out) {
+static cudaError_t capture_prec(Solver *S, const T *lu, const T *binv, T *z, cudaStream_t st,
+                                cudaGraphExec_t *out) {
   cudaGraph_t g;
   const TrsvArgs a = trsv_args(S);
   cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -1103,12 +1204,12 @@ static cudaError_t capture_prec(Solver *S, const T *lu, T *z, cudaStream_t st, c
   for (size_t l = 0; l + 1 < S->lo_ptr.size(); l++) {
     const int cnt = S->lo_ptr[l + 1] - S->lo_ptr[l];
     trsv_level_cta_kernel<T, true><<<cnt, kTrsvThreads, 0, st>>>(S->d_lo_nodes + S->lo_ptr[l], a,
-                                                                 lu, z);
+                                                                 lu, binv, z);
   }
   for (size_t l = 0; l + 1 < S->up_ptr.size(); l++) {
     const int cnt = S->up_ptr[l + 1] - S->up_ptr[l];
     trsv_level_cta_kernel<T, false><<<cnt, kTrsvThreads, 0, st>>>(S->d_up_nodes + S->up_ptr[l],
-                                                                  a, lu, z);
+                                                                  a, lu, binv, z);
   }
   e = cudaStreamEndCapture(st, &g);
   if (e != cudaSuccess) return e;
@@ -1129,6 +1230,7 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   g.nbr_node = P.nbr_node;
   g.nbr_off = P.nbr_off;
   g.nbr_offT = P.nbr_offT;
+  g.nbr_self = P.nbr_self;
   g.dim = L.dim;
   g.nvn = L.nvn;
   g.energy = L.energy;
@@ -1148,7 +1250,6 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
       owned.push_back(d_tp32);
     }
   }
-  const size_t ints = sizeof(int) * 4 * (size_t)maxnb;
   const double *Af = vals;  // the matrix the factors are built from
   if (ordering == 1) {
     gather_kernel<double><<<1216, 256, 0, st>>>(nnz, d_vmap, vals, d_Ap);
@@ -1158,24 +1259,35 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   for (size_t l = 0; l + 1 < lo_ptr.size(); l++) {
     const int cnt = lo_ptr[l + 1] - lo_ptr[l];
     if (fp32) {
-      const size_t sm = sizeof(float) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
+      const size_t sm = ilu_smem_bytes(sizeof(float), maxnb, g.maxnr, lmax);
       ilu0_block_kernel<float><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, Af, d_lu32);
     } else {
-      const size_t sm = sizeof(double) * ((size_t)g.maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs) + ints + sizeof(int64_t) * kMaxNodeDofs;
+      const size_t sm = ilu_smem_bytes(sizeof(double), maxnb, g.maxnr, lmax);
       ilu0_block_kernel<double><<<cnt, 256, sm, st>>>(d_lo_nodes + lo_ptr[l], g, Af, d_lu);
     }
   }
   GB_CU(cudaGetLastError(), "ILU(0) factorisation");
+  {
+    const TrsvArgs a = trsv_args(this);
+    if (fp32) {
+      if (!d_binv32) GB_CU(cudaMalloc(&d_binv32, sizeof(float) * inv_len), "block inverses");
+      block_inverse_kernel<float><<<(C->L.num_nodes + 7) / 8, 256, 0, st>>>(a, d_lu32, d_binv32);
+    } else {
+      block_inverse_kernel<double><<<(C->L.num_nodes + 7) / 8, 256, 0, st>>>(a, d_lu, d_binv);
+    }
+    GB_CU(cudaGetLastError(), "block inverses");
+  }
   if (fp32) {
     to_f32_kernel<<<1216, 256, 0, st>>>(nnz, vals, d_a32);
     GB_CU(cudaGetLastError(), "FP32 matrix copy");
     if (!prec32 && use_level_graph())
-      GB_CU(capture_prec<float>(this, d_lu32, ordering ? d_tp32 : d_t32, st, &prec32),
+      GB_CU(capture_prec<float>(this, d_lu32, d_binv32, ordering ? d_tp32 : d_t32, st, &prec32),
             "ILU32 graph");
     have_lu32 = true;
   } else {
     if (!prec64 && use_level_graph())
-      GB_CU(capture_prec<double>(this, d_lu, ordering ? d_tp : d_t, st, &prec64), "ILU graph");
+      GB_CU(capture_prec<double>(this, d_lu, d_binv, ordering ? d_tp : d_t, st, &prec64),
+            "ILU graph");
     have_lu64 = true;
   }
   return 0;
@@ -1207,7 +1319,7 @@ int Solver::copy_factors(double *host, bool fp32, cudaStream_t st) {
 }
 
 template <class T>
-static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
+static int sync_free_apply(Solver *S, const T *lu, const T *binv, T *z, cudaStream_t st) {
   if (!S->d_flags) {
     GB_CU(cudaMalloc(&S->d_flags, 16 * sizeof(unsigned)), "trsv tickets");
     GB_CU(cudaMemsetAsync(S->d_flags, 0, 16 * sizeof(unsigned), st), "trsv tickets");
@@ -1250,10 +1362,10 @@ static int sync_free_apply(Solver *S, const T *lu, T *z, cudaStream_t st) {
   // L: z -> y, then U: y -> z; each output starts all unpublished
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y, g.tickets + 0);
   g.order = lo_order;
-  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lu, z, y);
+  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lu, binv, z, y);
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z, g.tickets + 1);
   g.order = S->d_up_nodes;
-  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lu, y, z);
+  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lu, binv, y, z);
   GB_CU(cudaGetLastError(), "trsv");
   return 0;
 }
@@ -1274,15 +1386,15 @@ int Solver::check_trsv_error() {
 }
 
 template <class T>
-static int apply_prec(Solver *S, const T *lu, T *t, T *tp, cudaGraphExec_t graph,
-                      cudaStream_t st) {
+static int apply_prec(Solver *S, const T *lu, const T *binv, T *t, T *tp,
+                      cudaGraphExec_t graph, cudaStream_t st) {
   T *z = t;
   if (S->ordering == 1) {  // t -> P t, solve, P^T
     gather_kernel<T><<<304, 256, 0, st>>>(S->N, S->d_umap, t, tp);
     z = tp;
   }
   if (!S->use_level_graph()) {
-    if (sync_free_apply<T>(S, lu, z, st)) return -1;
+    if (sync_free_apply<T>(S, lu, binv, z, st)) return -1;
   } else {
     GB_CU(cudaGraphLaunch(graph, st), "ILU apply");
   }
@@ -1292,10 +1404,10 @@ static int apply_prec(Solver *S, const T *lu, T *t, T *tp, cudaGraphExec_t graph
 }
 
 int Solver::apply_prec64(cudaStream_t st) {
-  return apply_prec<double>(this, d_lu, d_t, d_tp, prec64, st);
+  return apply_prec<double>(this, d_lu, d_binv, d_t, d_tp, prec64, st);
 }
 int Solver::apply_prec32(cudaStream_t st) {
-  return apply_prec<float>(this, d_lu32, d_t32, d_tp32, prec32, st);
+  return apply_prec<float>(this, d_lu32, d_binv32, d_t32, d_tp32, prec32, st);
 }
 
 // ------------------------------------------------------------ helpers

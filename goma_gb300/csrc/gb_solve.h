@@ -31,6 +31,7 @@ struct PrecLayout {
   const int *colidx = nullptr;
   const int64_t *diag = nullptr;
   const int *nbr_ptr = nullptr, *nbr_node = nullptr, *nbr_off = nullptr, *nbr_offT = nullptr;
+  const int *nbr_self = nullptr;  // each node's position in its own neighbour list
 };
 
 struct Solver {
@@ -64,6 +65,12 @@ struct Solver {
   double *d_lu = nullptr;
   float *d_lu32 = nullptr;
   float *d_a32 = nullptr;       // FP32 copy of the scaled matrix
+  // dense inverses of every node's diagonal blocks of the factors (L's then
+  // U's, nr^2 values each, from d_inv_ptr[node]): FP64 and FP32
+  double *d_binv = nullptr;
+  float *d_binv32 = nullptr;
+  int64_t *d_inv_ptr = nullptr;
+  int64_t inv_len = 0;
   int64_t *d_diag = nullptr;    // position of the diagonal in every row
   int *d_fu = nullptr;          // first unknown per node (shared with C)
   int *d_lo_nodes = nullptr, *d_up_nodes = nullptr;
