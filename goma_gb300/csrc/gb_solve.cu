@@ -562,9 +562,16 @@ __global__ void __launch_bounds__(256)
 }
 
 // Sync-free triangular solves: one launch per sweep, one CTA per node at a
-// time.  CTAs take nodes from an atomic ticket in the order of their
+// time.  The nodes are numbered ("tickets") in the order of their
 // dependency levels (the level schedule of the sweep: all of level 0, then
-// level 1, ...; independent problems in one matrix interleave).  A sweep
+// level 1, ...; independent problems in one matrix interleave), and CTA b of
+// a G-CTA grid takes tickets b, b + G, b + 2G, ... in turn -- no atomic, and
+// a CTA reads its next node's ticket entry while it works on the current
+// one.  Per ticket a table holds the node's first unknown, unknown count and
+// block-inverse offset; per row one holds its off-node segment; the factor
+// values and column indices of the segments are stored in the sweep's own
+// (level-sorted) order, so a CTA reaches its rows' data in two dependent
+// loads.  A sweep
 // reads its right-hand side from one vector and writes its solution into
 // another that was filled beforehand with an "unpublished" sentinel (a
 // signalling NaN: arithmetic never produces one, so every computed value,
@@ -583,9 +590,10 @@ __global__ void __launch_bounds__(256)
 // A warp loads its first row's factor values and column indices, and the
 // CTA the block inverse, before it polls, so only the gather of the
 // solution values stays on the critical path.  A node depends
-// only on nodes of lower levels, which hold earlier tickets, and every CTA of
-// the grid is resident, so a value a CTA waits for is always owed by a CTA
-// that is running or done.  Every wait is bounded: past spin_limit polls the
+// only on nodes of lower levels, which hold earlier tickets; every CTA of the
+// grid is resident and takes its tickets in increasing order, so the lowest
+// unfinished ticket always has all its dependencies published and is held
+// by a CTA that is working on it: the sweep makes progress.  Every wait is bounded: past spin_limit polls the
 // CTA records an error, computes and publishes anyway (so no other CTA can
 // wait forever), every later wait of the sweep stops within 1024 polls, and
 // the host reports the failure after the sweep.  A legitimate wait lasts
@@ -602,7 +610,13 @@ static constexpr int kPrefetch = 10;  // row entries per lane loaded before the 
 static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
-  const int *order;    // nodes in the order the sweep hands them out (by level)
+  // the sync-free sweep's own tables, set per sweep: per ticket the node's
+  // (unknown count << 32 | first unknown) and the offset of its block
+  // inverse; per unknown the row's off-node segment [begin, end); the
+  // segments' column indices in sweep (level-sorted) order
+  const longlong2 *tick;
+  const longlong2 *seg;
+  const int *cols;
   const int *fu;
   const int64_t *rowptr;
   const int *colidx;
@@ -612,7 +626,6 @@ struct TrsvArgs {
   int num_nodes;
   int Tr;              // local index of the energy row, -1 without energy
   int nvn;             // nodal fields per node
-  unsigned *tickets;   // [0] L sweep, [1] U sweep (reset before each sweep)
   int *error;          // set when a wait gave up
   long long spin_limit;  // polls before a wait gives up
 };
@@ -647,10 +660,9 @@ __device__ __forceinline__ void st_relaxed(float *p, float v) {
   asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
 }
 
-// fill a sweep's output with the sentinel and reset its ticket counter
+// fill a sweep's output with the sentinel
 template <class T>
-__global__ void trsv_prepare_kernel(int64_t n, T *x, unsigned *ticket) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *ticket = 0u;
+__global__ void trsv_prepare_kernel(int64_t n, T *x) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     set_unpublished(x + i);
@@ -667,7 +679,6 @@ __device__ __forceinline__ T poll_value(const T *p, bool &gave_up, const int *er
       gave_up = true;
       return (T)0;
     }
-    __nanosleep(32);
     v = ld_relaxed(p);
   }
   return v;
@@ -733,62 +744,73 @@ __device__ __forceinline__ A node_block_apply(int lane, int nr, const A *inv_s, 
   return v;
 }
 
+// Copies every row's off-node segments of src into dst in the sweeps'
+// level-sorted order (entry p of a segment from segment start + rel[p]), so
+// the sync-free sweeps read factor values and column indices contiguously,
+// without the extra indirection.  One warp per row.
+template <class E>
+__global__ void sweep_gather_kernel(int N, const longlong2 *__restrict__ segL,
+                                    const longlong2 *__restrict__ segU,
+                                    const uint16_t *__restrict__ rel, const E *__restrict__ src,
+                                    E *__restrict__ dst) {
+  const int wpb = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * wpb + (threadIdx.x >> 5); i < N; i += gridDim.x * wpb) {
+    for (int h = 0; h < 2; h++) {
+      const longlong2 sg = h ? segU[i] : segL[i];
+      for (int64_t p = sg.x + lane; p < sg.y; p += 32) dst[p] = src[sg.x + rel[p]];
+    }
+  }
+}
+
 template <class T, bool LOWER>
-__global__ void __launch_bounds__(kTrsvThreads, 3)
-    trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lu, const T *__restrict__ binv,
+__global__ void __launch_bounds__(kTrsvThreads, 4)
+    trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lus, const T *__restrict__ binv,
                           const T *__restrict__ b, T *x) {
   using A = acc_t<T>;
   __shared__ A bv[kMaxNodeDofs];                      // per row: rhs less the off-node part
   __shared__ A inv_s[kMaxNodeDofs * kMaxNodeDofs];    // the node's block inverse, by column
-  __shared__ int s_node;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kTrsvThreads / 32;
-  while (true) {
-    if (tid == 0) {
-      const unsigned t = atomicAdd(g.tickets + (LOWER ? 0 : 1), 1u);
-      s_node = t < (unsigned)g.num_nodes ? g.order[t] : -1;
-    }
-    __syncthreads();
-    const int n = s_node;
-    if (n < 0) return;
-    const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
+  const unsigned nt = (unsigned)g.num_nodes, stride = gridDim.x;
+  unsigned t = blockIdx.x;
+  longlong2 tk = t < nt ? g.tick[t] : make_longlong2(0, 0);
+  for (; t < nt; t += stride) {
+    const int f0 = (int)(tk.x & 0xffffffffll), nr = (int)(tk.x >> 32);
+    const int64_t inv_off = tk.y;
     // before polling: everything that does not depend on the sweep
     A pv[kPrefetch];
     int pc[kPrefetch];
     int64_t pr0 = 0, pr1 = 0;
     if (warp < nr) {
-      const int r = warp, i = f0 + r;
-      const int64_t di = g.diag[i];
-      const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;
-      pr0 = LOWER ? g.rowptr[i] : di + 1 + na;
-      pr1 = LOWER ? di - r : g.rowptr[i + 1];
+      const longlong2 sg = g.seg[f0 + warp];
+      pr0 = sg.x;
+      pr1 = sg.y;
 #pragma unroll
       for (int k = 0; k < kPrefetch; k++) {
         const int64_t p = pr0 + lane + 32 * k;
-        const int64_t q = p < pr1 ? pr0 + g.rel[p] : 0;  // level-sorted entry order
-        pv[k] = p < pr1 ? (A)lu[q] : (A)0;
-        pc[k] = p < pr1 ? g.colidx[q] : -1;
+        pv[k] = p < pr1 ? (A)lus[p] : (A)0;
+        pc[k] = p < pr1 ? g.cols[p] : -1;
       }
     }
-    {
-      const T *bi = binv + g.inv_ptr[n] + (LOWER ? 0 : nr * nr);
-      for (int w = tid; w < nr * nr; w += kTrsvThreads) {
-        const int c = w / nr;
-        inv_s[c * kMaxNodeDofs + (w - c * nr)] = (A)bi[w];
-      }
+    for (int w = tid; w < nr * nr; w += kTrsvThreads) {
+      const int c = w / nr;
+      inv_s[c * kMaxNodeDofs + (w - c * nr)] = (A)binv[inv_off + w];
     }
+    // this CTA's next node (static round-robin tickets)
+    if (t + stride < nt) tk = g.tick[t + stride];
     // stage A
     bool gave_up = false;
     for (int r = warp; r < nr; r += NW) {
       const A rhs_r = (A)__ldcg(b + f0 + r);
       A s0 = 0;
-      int64_t p, p1, sb;  // sb: start of the row's off-node segment
+      int64_t p, p1;
       if (r == warp) {
         // the prefetched row: load all its values at once, then add them in
         // the fixed (level-sorted, oldest first) order, each as soon as it
         // and every earlier one are published -- the values published long
-        // ago are added while the newest ones are still awaited, and every
-        // wait re-polls all the values still pending
+        // ago are added while the newest ones are still awaited; a wait
+        // re-polls only the value it waits for, so waiting warps issue few
+        // instructions
         A zv[kPrefetch];
         unsigned pending = 0;
 #pragma unroll
@@ -808,35 +830,23 @@ __global__ void __launch_bounds__(kTrsvThreads, 3)
               gave_up = true;
               break;
             }
-            __nanosleep(32);
-#pragma unroll
-            for (int j = 0; j < kPrefetch; j++) {
-              if (j >= k && (pending & (1u << j))) {
-                const T v = ld_relaxed(x + pc[j]);
-                if (!unpublished(v)) {
-                  zv[j] = (A)v;
-                  pending &= ~(1u << j);
-                }
-              }
+            const T v = ld_relaxed(x + pc[k]);
+            if (!unpublished(v)) {
+              zv[k] = (A)v;
+              pending &= ~(1u << k);
             }
           }
           if (pc[k] >= 0) s0 = fmx(pv[k], zv[k], s0);
         }
         p = pr0 + lane + 32 * kPrefetch;
         p1 = pr1;
-        sb = pr0;
       } else {
-        const int i = f0 + r;
-        const int64_t di = g.diag[i];
-        const int na = (r == g.Tr ? g.nvn : nr) - 1 - r;  // own columns above the diagonal
-        sb = LOWER ? g.rowptr[i] : di + 1 + na;
-        p1 = LOWER ? di - r : g.rowptr[i + 1];
-        p = sb + lane;
+        const longlong2 sg = g.seg[f0 + r];
+        p = sg.x + lane;
+        p1 = sg.y;
       }
-      for (; p < p1; p += 32) {
-        const int64_t q = sb + g.rel[p];
-        s0 = fmx((A)lu[q], (A)poll_value(x + g.colidx[q], gave_up, g.error, g.spin_limit), s0);
-      }
+      for (; p < p1; p += 32)
+        s0 = fmx((A)lus[p], (A)poll_value(x + g.cols[p], gave_up, g.error, g.spin_limit), s0);
       const A sum = wsum(s0);
       if (lane == 0) bv[r] = rhs_r - sum;
     }
@@ -900,11 +910,13 @@ __global__ void __launch_bounds__(kTrsvThreads)
   }
 }
 
-// the sweeps' view of the preconditioner layout (tickets and the order are
-// set by the sync-free sweep)
+// the sweeps' view of the preconditioner layout (the sync-free sweep sets
+// its tickets, segments and columns)
 static TrsvArgs trsv_args(const Solver *S) {
   TrsvArgs g;
-  g.order = nullptr;
+  g.tick = nullptr;
+  g.seg = nullptr;
+  g.cols = nullptr;
   g.fu = S->P.fu;
   g.rowptr = S->P.rowptr;
   g.colidx = S->P.colidx;
@@ -914,7 +926,6 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.num_nodes = S->C->L.num_nodes;
   g.Tr = S->C->L.energy ? S->C->L.dim : -1;
   g.nvn = S->C->L.nvn;
-  g.tickets = nullptr;
   g.error = nullptr;
   g.spin_limit = S->C->sweep_spin_limit > 0 ? S->C->sweep_spin_limit : kSpinLimit;
   return g;
@@ -971,7 +982,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
 Solver::~Solver() {
   if (prec64) cudaGraphExecDestroy(prec64);
   if (prec32) cudaGraphExecDestroy(prec32);
-  void *p[] = {d_lu, d_lu32, d_binv, d_binv32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
+  void *p[] = {d_lu, d_lu32, d_lus, d_lus32, d_binv, d_binv32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
                d_sweep_y, d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
@@ -1052,6 +1063,7 @@ int Solver::init(Context *c, int krylov) {
     P.nbr_off = c->d_nbr_off;
     P.nbr_offT = c->d_nbr_offT;
   }
+  std::vector<int64_t> ip(LP->num_nodes + 1, 0);  // block-inverse offsets
   {
     std::vector<int> self(LP->num_nodes);
     for (int n = 0; n < LP->num_nodes; n++) {
@@ -1065,7 +1077,6 @@ int Solver::init(Context *c, int krylov) {
           "neighbour self positions");
     P.nbr_self = d;
     // offsets of every node's diagonal-block inverses (L's and U's, nr^2 each)
-    std::vector<int64_t> ip(LP->num_nodes + 1, 0);
     for (int n = 0; n < LP->num_nodes; n++) {
       const int64_t nr = LP->fu[n + 1] - LP->fu[n];
       ip[n + 1] = ip[n] + 2 * nr * nr;
@@ -1082,7 +1093,6 @@ int Solver::init(Context *c, int krylov) {
   lo_ptr = S.lo_ptr;
   up_ptr = S.up_ptr;
   num_levels = (int)lo_ptr.size() - 1;
-  lo_nodes_host = S.lo_nodes;
   {
     std::vector<uint16_t> rel;
     if (build_sweep_order(*LP, S.lev, S.levu, rel)) return fail("a matrix row is too long for the sweeps");
@@ -1090,6 +1100,54 @@ int Solver::init(Context *c, int krylov) {
     owned.push_back(d_sweep_rel);
     GB_CU(cudaMemcpy(d_sweep_rel, rel.data(), sizeof(uint16_t) * rel.size(),
                      cudaMemcpyHostToDevice), "sweep order");
+  }
+  {
+    // the sync-free sweeps' tables: every row's off-node segments, the
+    // tickets of both sweeps, and the column indices in sweep order
+    const int Tr = L.energy ? L.dim : -1;
+    std::vector<longlong2> sl(N), su(N);
+    for (int n = 0; n < LP->num_nodes; n++) {
+      const int f0 = LP->fu[n], nr = LP->fu[n + 1] - f0;
+      for (int r = 0; r < nr; r++) {
+        const int i = f0 + r;
+        auto b = LP->colidx.begin() + LP->rowptr[i], e = LP->colidx.begin() + LP->rowptr[i + 1];
+        const int64_t di = (int64_t)(std::lower_bound(b, e, i) - LP->colidx.begin());
+        const int na = (r == Tr ? L.nvn : nr) - 1 - r;
+        sl[i] = make_longlong2(LP->rowptr[i], di - r);
+        su[i] = make_longlong2(di + 1 + na, LP->rowptr[i + 1]);
+      }
+    }
+    auto ticks = [&](const std::vector<int> &order, bool upper) {
+      std::vector<longlong2> tk(order.size());
+      for (size_t t = 0; t < order.size(); t++) {
+        const int n = order[t], f0 = LP->fu[n];
+        const long long nr = LP->fu[n + 1] - f0;
+        tk[t] = make_longlong2((nr << 32) | (long long)f0, ip[n] + (upper ? nr * nr : 0));
+      }
+      return tk;
+    };
+    auto upv = [&](const auto &vec, auto **dst, const char *what) -> int {
+      GB_CU(cudaMalloc((void **)dst, sizeof(vec[0]) * vec.size()), what);
+      owned.push_back(*dst);
+      GB_CU(cudaMemcpy(*dst, vec.data(), sizeof(vec[0]) * vec.size(), cudaMemcpyHostToDevice),
+            what);
+      return 0;
+    };
+    if (upv(sl, &d_segL, "sweep segments") || upv(su, &d_segU, "sweep segments") ||
+        upv(ticks(S.lo_nodes, false), &d_tick_lo, "sweep tickets") ||
+        upv(ticks(S.up_nodes, true), &d_tick_up, "sweep tickets"))
+      return -1;
+    {
+      std::vector<int> rev(S.lo_nodes.rbegin(), S.lo_nodes.rend());
+      if (upv(ticks(rev, false), &d_tick_lo_rev, "sweep tickets")) return -1;
+    }
+    GB_CU(cudaMalloc(&d_sweep_cols, sizeof(int) * (size_t)nnz), "sweep columns");
+    owned.push_back(d_sweep_cols);
+    GB_CU(cudaMemset(d_sweep_cols, 0, sizeof(int) * (size_t)nnz), "sweep columns");
+    sweep_gather_kernel<int><<<(N + 7) / 8, 256>>>(N, d_segL, d_segU, d_sweep_rel, P.colidx,
+                                                   d_sweep_cols);
+    GB_CU(cudaGetLastError(), "sweep columns");
+    GB_CU(cudaDeviceSynchronize(), "sweep columns");
   }
   GB_CU(cudaMalloc(&d_lo_nodes, sizeof(int) * S.lo_nodes.size()), "sched");
   GB_CU(cudaMemcpy(d_lo_nodes, S.lo_nodes.data(), sizeof(int) * S.lo_nodes.size(),
@@ -1269,11 +1327,18 @@ int Solver::factor(const double *vals, bool fp32, cudaStream_t st) {
   GB_CU(cudaGetLastError(), "ILU(0) factorisation");
   {
     const TrsvArgs a = trsv_args(this);
+    const int gs = (N + 7) / 8;
     if (fp32) {
       if (!d_binv32) GB_CU(cudaMalloc(&d_binv32, sizeof(float) * inv_len), "block inverses");
+      if (!d_lus32) GB_CU(cudaMalloc(&d_lus32, sizeof(float) * nnz), "sweep-ordered factors");
       block_inverse_kernel<float><<<(C->L.num_nodes + 7) / 8, 256, 0, st>>>(a, d_lu32, d_binv32);
+      sweep_gather_kernel<float><<<gs, 256, 0, st>>>(N, d_segL, d_segU, d_sweep_rel, d_lu32,
+                                                     d_lus32);
     } else {
+      if (!d_lus) GB_CU(cudaMalloc(&d_lus, sizeof(double) * nnz), "sweep-ordered factors");
       block_inverse_kernel<double><<<(C->L.num_nodes + 7) / 8, 256, 0, st>>>(a, d_lu, d_binv);
+      sweep_gather_kernel<double><<<gs, 256, 0, st>>>(N, d_segL, d_segU, d_sweep_rel, d_lu,
+                                                      d_lus);
     }
     GB_CU(cudaGetLastError(), "block inverses");
   }
@@ -1319,10 +1384,10 @@ int Solver::copy_factors(double *host, bool fp32, cudaStream_t st) {
 }
 
 template <class T>
-static int sync_free_apply(Solver *S, const T *lu, const T *binv, T *z, cudaStream_t st) {
+static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStream_t st) {
   if (!S->d_flags) {
-    GB_CU(cudaMalloc(&S->d_flags, 16 * sizeof(unsigned)), "trsv tickets");
-    GB_CU(cudaMemsetAsync(S->d_flags, 0, 16 * sizeof(unsigned), st), "trsv tickets");
+    GB_CU(cudaMalloc(&S->d_flags, 16 * sizeof(unsigned)), "trsv error word");
+    GB_CU(cudaMemsetAsync(S->d_flags, 0, 16 * sizeof(unsigned), st), "trsv error word");
     GB_CU(cudaMalloc(&S->d_sweep_y, sizeof(double) * (size_t)S->N), "trsv scratch");
     int per_sm = 1 << 30, dev = 0, sms = 0;
     const void *fns[4] = {(const void *)trsv_sync_free_kernel<double, true>,
@@ -1339,33 +1404,28 @@ static int sync_free_apply(Solver *S, const T *lu, const T *binv, T *z, cudaStre
     S->trsv_grid = std::max(1, per_sm) * sms;
     S->prep_grid = 2 * sms;
   }
-  TrsvArgs g = trsv_args(S);  // the order is set per sweep below
-  g.tickets = S->d_flags;
+  TrsvArgs g = trsv_args(S);  // the tickets and segments are set per sweep below
   g.error = (int *)(S->d_flags + 4);
+  g.cols = S->d_sweep_cols;
   T *y = static_cast<T *>(S->d_sweep_y);
   // the host-injected fault of gb_set_sweep_fault: the lower sweep's nodes in
   // reverse order (every dependency after its dependant) on one CTA, whose
   // first wait can then only end by running out
-  const int *lo_order = S->d_lo_nodes;
+  const longlong2 *lo_tick = S->d_tick_lo;
   int grid = S->trsv_grid;
   if (S->C->sweep_reverse_lower) {
-    if (!S->d_lo_nodes_rev) {
-      std::vector<int> rev(S->lo_nodes_host.rbegin(), S->lo_nodes_host.rend());
-      GB_CU(cudaMalloc(&S->d_lo_nodes_rev, sizeof(int) * rev.size()), "reversed order");
-      S->owned.push_back(S->d_lo_nodes_rev);
-      GB_CU(cudaMemcpy(S->d_lo_nodes_rev, rev.data(), sizeof(int) * rev.size(),
-                       cudaMemcpyHostToDevice), "reversed order");
-    }
-    lo_order = S->d_lo_nodes_rev;
+    lo_tick = S->d_tick_lo_rev;
     grid = 1;
   }
   // L: z -> y, then U: y -> z; each output starts all unpublished
-  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y, g.tickets + 0);
-  g.order = lo_order;
-  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lu, binv, z, y);
-  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z, g.tickets + 1);
-  g.order = S->d_up_nodes;
-  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lu, binv, y, z);
+  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y);
+  g.tick = lo_tick;
+  g.seg = S->d_segL;
+  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, z, y);
+  trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z);
+  g.tick = S->d_tick_up;
+  g.seg = S->d_segU;
+  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, y, z);
   GB_CU(cudaGetLastError(), "trsv");
   return 0;
 }
@@ -1386,7 +1446,7 @@ int Solver::check_trsv_error() {
 }
 
 template <class T>
-static int apply_prec(Solver *S, const T *lu, const T *binv, T *t, T *tp,
+static int apply_prec(Solver *S, const T *lus, const T *binv, T *t, T *tp,
                       cudaGraphExec_t graph, cudaStream_t st) {
   T *z = t;
   if (S->ordering == 1) {  // t -> P t, solve, P^T
@@ -1394,7 +1454,7 @@ static int apply_prec(Solver *S, const T *lu, const T *binv, T *t, T *tp,
     z = tp;
   }
   if (!S->use_level_graph()) {
-    if (sync_free_apply<T>(S, lu, binv, z, st)) return -1;
+    if (sync_free_apply<T>(S, lus, binv, z, st)) return -1;
   } else {
     GB_CU(cudaGraphLaunch(graph, st), "ILU apply");
   }
@@ -1404,10 +1464,10 @@ static int apply_prec(Solver *S, const T *lu, const T *binv, T *t, T *tp,
 }
 
 int Solver::apply_prec64(cudaStream_t st) {
-  return apply_prec<double>(this, d_lu, d_binv, d_t, d_tp, prec64, st);
+  return apply_prec<double>(this, d_lus, d_binv, d_t, d_tp, prec64, st);
 }
 int Solver::apply_prec32(cudaStream_t st) {
-  return apply_prec<float>(this, d_lu32, d_binv32, d_t32, d_tp32, prec32, st);
+  return apply_prec<float>(this, d_lus32, d_binv32, d_t32, d_tp32, prec32, st);
 }
 
 // ------------------------------------------------------------ helpers

@@ -71,13 +71,18 @@ struct Solver {
   float *d_binv32 = nullptr;
   int64_t *d_inv_ptr = nullptr;
   int64_t inv_len = 0;
+  // the sync-free sweeps' tables (see trsv_sync_free_kernel): factors and
+  // column indices in sweep order, per-row off-node segments, tickets
+  double *d_lus = nullptr;
+  float *d_lus32 = nullptr;
+  int *d_sweep_cols = nullptr;
+  longlong2 *d_segL = nullptr, *d_segU = nullptr;
+  longlong2 *d_tick_lo = nullptr, *d_tick_up = nullptr, *d_tick_lo_rev = nullptr;
   int64_t *d_diag = nullptr;    // position of the diagonal in every row
   int *d_fu = nullptr;          // first unknown per node (shared with C)
   int *d_lo_nodes = nullptr, *d_up_nodes = nullptr;
   std::vector<int> lo_ptr, up_ptr;
-  std::vector<int> lo_nodes_host;  // the lower sweep's order (host copy)
   uint16_t *d_sweep_rel = nullptr; // level-sorted entry order of the sweeps (build_sweep_order)
-  int *d_lo_nodes_rev = nullptr;   // it reversed, for the injected sweep fault
   const double *d_A = nullptr;  // scaled FP64 matrix the factors were built from
   double pivot_tau = 1e-4;      // ILU(0) pivot floor on the row-scaled matrix
   int maxnb = 0, lmax = 0;      // largest node neighbourhood / block-row length
@@ -90,7 +95,7 @@ struct Solver {
   double *d_t = nullptr, *d_w = nullptr, *d_r = nullptr, *d_xs = nullptr;
   float *d_t32 = nullptr, *d_w32 = nullptr;
   cudaGraphExec_t prec64 = nullptr, prec32 = nullptr;  // captured ILU solves on d_t / d_t32
-  unsigned *d_flags = nullptr;  // sync-free sweeps: [0..1] tickets, [4] error word
+  unsigned *d_flags = nullptr;  // sync-free sweeps: [4] error word
   void *d_sweep_y = nullptr;    // sync-free sweeps: the L sweep's output (N values)
   int trsv_grid = 0, prep_grid = 0;
   int check_trsv_error();
