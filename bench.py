@@ -151,16 +151,18 @@ def cpu_baseline(nel=NEL, threads=None, steps=1):
     return out
 
 
-def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=150,
+def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, krylov=300,
                   forcing=1, reference_solver=True, modes=None, budget_s=None,
-                  factorization_reuse=0, max_linear_its=4000):
+                  factorization_reuse=0, max_linear_its=4000, inner_tol=1e-3):
     """Wall-clock time to the converged Boussinesq cube at Ra = ra1, by Ra
     continuation from rest at Ra = ra0 in nsteps log-uniform steps: plain
     FP64 Newton (ILU(0)-GMRES in FP64, zeroth-order predictor, the
     reference's ALC_ZEROTH) against the learned predictor (secant fallback)
-    with FP64 GMRES and with FP32-inner GMRES inside FP64 refinement; the
-    secant_fp32 run is the learned_fp32 run without the network (the plain
-    secant guess), so the two isolate what the network gains.  All use the same
+    with FP64 GMRES and with FP32 GMRES: the _fp32 runs are FP64 flexible
+    GMRES with the ILU(0) factorised and swept in FP32, the _fp32r runs FP32
+    GMRES inside FP64 iterative refinement; the secant_fp32 run is the
+    learned_fp32 run without the network (the plain secant guess), so the
+    two isolate what the network gains.  All use the same
     linear-solver settings: ILU(0), GMRES(krylov), Eisenstat-Walker forcing
     (the converged solution does not depend on them).  ilu_ordering -1
     chooses the node order by size: the multicoloured one up to 12^3 (few
@@ -171,7 +173,8 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
     order, GMRES(30), every linear solve to 1e-8).  `modes` selects runs;
     `budget_s` ends each run's sweep after that many seconds (reported as
     steps done).  factorization_reuse (GB_FACTOR_*) applies to every run
-    but the one with the reference's settings.  Returns a dict with the times, Newton/Krylov counts,
+    but the one with the reference's settings; inner_tol is the FP32 runs'
+    tightest inner tolerance.  Returns a dict with the times, Newton/Krylov counts,
     per-phase splits and the relative difference of the converged
     solutions."""
     if ilu_ordering < 0:
@@ -188,7 +191,9 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
 
     out = {"workload": "%d^3 HEX27 Boussinesq cube, Ra %g -> %g in %d log-uniform continuation "
                        "steps from rest, Pr=%g, scaled |R| < %g" % (nel, ra0, ra1, nsteps, PR, tol),
-           "linear_solver": "ILU(0) in the %s node order, GMRES(%d), %s, factors %s" % (
+           "linear_solver": "ILU(0) in the %s node order, GMRES(%d), %s, factors %s; the _fp32 "
+                            "runs: FP64 flexible GMRES with the ILU(0) factorised and swept in "
+                            "FP32" % (
                "reference's" if ilu_ordering == 0 else "multicoloured", krylov,
                "Eisenstat-Walker forcing (1e-8 .. 1e-2)" if forcing else "linear tol 1e-8",
                ["at every Newton step", "once per Newton solve", "reused across solves"][
@@ -213,7 +218,8 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
         gn.set_ilu_ordering(0 if refs else ilu_ordering)
         opts = dict(residual_tol=tol, linear_tol=1e-8, max_newton=30,
                     max_linear_its=max_linear_its,
-                    fp32_inner=mode.endswith("_fp32"), inner_tol=1e-3,
+                    fp32_preconditioner=mode.endswith("_fp32"),
+                    fp32_inner=mode.endswith("_fp32r"), inner_tol=inner_tol,
                     krylov_dim=30 if refs else krylov, forcing=0 if refs else forcing,
                     forcing_max=1e-2, factorization_reuse=0 if refs else factorization_reuse)
         torch.cuda.synchronize()
@@ -338,8 +344,9 @@ def reacting_channel_solve(nx=64, ny=64, nz=32, tol=1e-8, max_newton=15, max_lin
     """The reacting channel (HEX27 Q2/P1 Navier-Stokes + energy + 2 Arrhenius
     species, 7.0 M unknowns at 64 x 64 x 32) solved by Newton from the inflow
     state (u = 1, T = 1.5, Y_0 = 1, Y_1 = 0 inside, the Dirichlet values on
-    the boundary) to the scaled residual `tol`, with FP32-inner ILU(0)-GMRES
-    inside FP64 refinement and Eisenstat-Walker forcing: time, Newton and
+    the boundary) to the scaled residual `tol`, with FP64 flexible GMRES
+    whose ILU(0) preconditioner is factorised and swept in FP32, and
+    Eisenstat-Walker forcing: time, Newton and
     Krylov counts and the per-phase split.  The reference's 32-bit MSR cannot
     hold this problem."""
     import time as _time
@@ -364,13 +371,13 @@ def reacting_channel_solve(nx=64, ny=64, nz=32, tol=1e-8, max_newton=15, max_lin
     t1 = _time.perf_counter()
     x, conv, st = gn.solve_nonlinear_problem(
         x, residual_tol=tol, linear_tol=1e-8, max_newton=max_newton,
-        max_linear_its=max_linear_its, krylov_dim=krylov, fp32_inner=True, inner_tol=1e-3,
+        max_linear_its=max_linear_its, krylov_dim=krylov, fp32_preconditioner=True,
         forcing=1, forcing_max=1e-2)
     torch.cuda.synchronize()
     dt = _time.perf_counter() - t1
     out = {"workload": "reacting channel %dx%dx%d HEX27 Q2/P1 NS + energy + 2 Arrhenius species, "
-                       "Newton from the inflow state to scaled |R| < %g, FP32-inner "
-                       "ILU(0)-GMRES(%d), forcing rule" % (nx, ny, nz, tol, krylov),
+                       "Newton from the inflow state to scaled |R| < %g, FP64 flexible "
+                       "GMRES(%d) with FP32 ILU(0), forcing rule" % (nx, ny, nz, tol, krylov),
            "unknowns": gn.N, "csr_nnz": gn.nnz, "converged": conv, "seconds": dt,
            "layout_and_upload_s": setup_s, "newton_its": st["newton_its"],
            "linear_its": st["linear_its"], "residual_l2": st["residual_l2"],
@@ -770,6 +777,7 @@ def main():
     ap.add_argument("--solve-modes", default="",
                     help="comma-separated runs of the time-to-solve leg: plain_fp64, "
                          "learned_fp64, learned_fp32, secant_fp32, secant_fp64, "
+                         "learned_fp32r, secant_fp32r (FP32 GMRES inside FP64 refinement), "
                          "plain_fp64_reference_solver "
                          "(default: plain_fp64, secant_fp32, learned_fp32)")
     ap.add_argument("--solve-budget", type=float, default=0.0,
@@ -777,10 +785,12 @@ def main():
     ap.add_argument("--bfs-budget", type=float, default=150.0,
                     help="seconds per predictor of the bfs workload (the 200-step sweep stops "
                          "there)")
-    ap.add_argument("--solve-krylov", type=int, default=150,
+    ap.add_argument("--solve-krylov", type=int, default=300,
                     help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
                     help="Krylov iteration limit of one linear solve in the time-to-solve leg")
+    ap.add_argument("--solve-inner-tol", type=float, default=1e-3,
+                    help="the _fp32r runs' tightest inner GMRES tolerance")
     ap.add_argument("--solve-reuse", type=int, default=0,
                     help="ILU(0) factorisation reuse of the time-to-solve leg: 0 every Newton "
                          "step, 1 once per Newton solve, 2 across solves")
@@ -795,7 +805,8 @@ def main():
                          "node orders, 8^3 to 24^3), cpu_solve (the 8^3 time-to-solve sweep on "
                          "one host core with the oracle's ILU(0)-GMRES(30)), krylovN (the "
                          "linear-solver kernels on one N^3 cube system: factorisation + 30 "
-                         "GMRES iterations, FP64 and FP32)")
+                         "GMRES(30) iterations, FP64 and FP32; krylovNxM: M GMRES(M) "
+                         "iterations)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -972,7 +983,8 @@ def main():
                 args.solve_nel, ilu_ordering=args.solve_ilu, reference_solver=args.solve_nel <= 8,
                 modes=[m for m in args.solve_modes.split(",") if m] or None,
                 budget_s=args.solve_budget or None, factorization_reuse=args.solve_reuse,
-                max_linear_its=args.solve_max_linear, krylov=args.solve_krylov)
+                max_linear_its=args.solve_max_linear, krylov=args.solve_krylov,
+                inner_tol=args.solve_inner_tol)
         except RuntimeError as exc:   # a continuation step that did not converge
             line["time_to_solve"] = {"error": str(exc)}
     if rank == 0 and args.workloads:
@@ -1001,7 +1013,8 @@ def main():
             elif w == "reacting_solve":
                 extra[w] = reacting_channel_solve()
             elif w.startswith("krylov"):
-                extra[w] = krylov_kernels(int(w[len("krylov"):] or 16))
+                nel_s, _, its_s = w[len("krylov"):].partition("x")
+                extra[w] = krylov_kernels(int(nel_s or 16), int(its_s or 30))
         line["workloads"] = extra
     if rank == 0:
         print(json.dumps(line))

@@ -252,7 +252,8 @@ def continuation(gn, lam0, lam1, nsteps, predictor="zeroth", x0=None, set_param=
                               log_lambda=(spacing == "log"), **(learned_opts or {}))
         lp.add(lams[0], x)
     hist = [(lams[0], x)]
-    lin_keys = ("linear_tol", "fp32_inner", "krylov_dim", "max_linear_its", "inner_tol")
+    lin_keys = ("linear_tol", "fp32_inner", "fp32_preconditioner", "krylov_dim", "max_linear_its",
+                "inner_tol")
     x_old, lam_old = x, lams[0]
     targets = lams[1:]
     k = 0

@@ -54,6 +54,7 @@ static LinearOpts linear_opts(const gb_newton_opts &o) {
   l.maxit = o.max_linear_its > 0 ? o.max_linear_its : 500;
   l.tol = o.linear_tol > 0 ? o.linear_tol : 1e-6;
   l.fp32_inner = o.linear_precision == GB_LINEAR_FP32_REFINED;
+  l.fp32_prec = o.linear_precision == GB_LINEAR_FP32_PRECONDITIONER;
   l.inner_tol = o.inner_tol > 0 ? o.inner_tol : 1e-3;
   l.max_refinements = o.max_refinements > 0 ? o.max_refinements : 20;
   return l;
@@ -166,10 +167,10 @@ int newton(Context *C, double *d_x, const gb_newton_opts &o, int *converged,
       prev_norm = n3[0];
     }
     // the preconditioner: new factors, or the last ones (factorization_reuse)
-    const bool refactor = reuse == GB_FACTOR_CALC || !S.has_factors(lo.fp32_inner) ||
+    const bool refactor = reuse == GB_FACTOR_CALC || !S.has_factors(lo.fp32_factors()) ||
                           (reuse == GB_FACTOR_PER_SOLVE && !factored);
-    if (refactor ? S.factor(C->d_vals, lo.fp32_inner, s)
-                 : S.refresh(C->d_vals, lo.fp32_inner, s)) {
+    if (refactor ? S.factor(C->d_vals, lo.fp32_factors(), s)
+                 : S.refresh(C->d_vals, lo.fp32_factors(), s)) {
       rc = -1;
       break;
     }
@@ -294,9 +295,9 @@ int gb_linear_solve_device(gb_ctx *ctx, const double *d_vals, const double *d_rh
   // GB_FACTOR_REUSE keeps the last factors when there are any (a second
   // solve with the same matrix, or a lagged preconditioner)
   const bool reuse = o.factorization_reuse == GB_FACTOR_REUSE &&
-                     c.solver->has_factors(lo.fp32_inner);
-  if (reuse ? c.solver->refresh(d_vals, lo.fp32_inner, c.stream)
-            : c.solver->factor(d_vals, lo.fp32_inner, c.stream))
+                     c.solver->has_factors(lo.fp32_factors());
+  if (reuse ? c.solver->refresh(d_vals, lo.fp32_factors(), c.stream)
+            : c.solver->factor(d_vals, lo.fp32_factors(), c.stream))
     return -1;
   gb::LinearStats ls;
   if (gb::linear_solve(&c, d_rhs, d_dx, lo, &ls, c.stream)) return -1;

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gb_context.h"
@@ -136,25 +137,40 @@ __global__ void norms_final_kernel(int nblocks, const double *__restrict__ part,
   out[2] = mx;
 }
 
-// partial dots of w with the k columns V[0..k) (column stride ld)
+// Partial dots of w with the k columns V[0..k) (column stride ld), kMdCols
+// columns per block row (blockIdx.y): a thread reads w once per group of
+// columns and keeps one running sum per column, and the block reduces all
+// of them with one barrier per halving.  Grid (nblocks, column groups);
+// block b's sum for column j goes to part[j * gridDim.x + b].
+static constexpr int kMdCols = 8;
 template <class T>
-__global__ void multidot_partial_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
-                                        const T *__restrict__ w, double *__restrict__ part) {
-  __shared__ double sh[kRedThreads];
+__global__ void __launch_bounds__(kRedThreads)
+    multidot_tile_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
+                         const T *__restrict__ w, double *__restrict__ part) {
+  __shared__ double sh[kMdCols][kRedThreads];
   using A = acc_t<T>;
-  for (int j = 0; j < k; j++) {
-    A s = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
-      s = fmx((A)V[j * ld + i], (A)w[i], s);
-    sh[threadIdx.x] = (double)s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-      __syncthreads();
+  const int j0 = blockIdx.y * kMdCols;
+  const int nc = min(kMdCols, k - j0);
+  A s[kMdCols];
+#pragma unroll
+  for (int c = 0; c < kMdCols; c++) s[c] = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const A wi = (A)w[i];
+#pragma unroll
+    for (int c = 0; c < kMdCols; c++)
+      if (c < nc) s[c] = fmx((A)V[(int64_t)(j0 + c) * ld + i], wi, s[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < kMdCols; c++) sh[c][threadIdx.x] = (double)s[c];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+#pragma unroll
+      for (int c = 0; c < kMdCols; c++) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
     }
-    if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = sh[0];
     __syncthreads();
   }
+  if (threadIdx.x < nc) part[(int64_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = sh[threadIdx.x][0];
 }
 
 __global__ void multidot_final_kernel(int k, int nblocks, const double *__restrict__ part,
@@ -259,6 +275,12 @@ __global__ void to_f32_kernel(int64_t n, const double *__restrict__ x, float *__
     y[i] = (float)x[i];
 }
 
+__global__ void to_f64_kernel(int64_t n, const float *__restrict__ x, double *__restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
 // ------------------------------------------------------------ SpMV
 
 // y = A x, LPR lanes per row (LPR divides 32)
@@ -328,8 +350,8 @@ struct IluArgs {
 // Shared memory of one ilu0_block_kernel CTA (element type of size tsize).
 static size_t ilu_smem_bytes(size_t tsize, int maxnb, int maxnr, int lmax) {
   return sizeof(int64_t) * (size_t)maxnb * maxnr +                          // srow
-         tsize * ((size_t)maxnr * lmax + 2 * kMaxNodeDofs * kMaxNodeDofs + kMaxNodeDofs) +
-         sizeof(int) * (11 * (size_t)maxnb + 4);
+         tsize * ((size_t)maxnr * lmax + 3 * kMaxNodeDofs * kMaxNodeDofs + 2 * kMaxNodeDofs) +
+         sizeof(int) * (15 * (size_t)maxnb + 4);
 }
 
 // ILU(0) of one node's block row (one CTA per node, the nodes of one
@@ -342,12 +364,52 @@ static size_t ilu_smem_bytes(size_t tsize, int maxnb, int maxnr, int lmax) {
 // then the diagonal block is factorised in place and the row written back.
 // Everything that depends only on the node graph and on finished nodes is
 // loaded up front for all m at once (their neighbour-list bounds, own
-// positions and row starts); per m one round of loads brings m's neighbour
-// list (with each neighbour's slot in n's list, found in shared memory) and
-// U_mm, and a second one the U_mq entries.  Step 2 runs over the compacted
-// list of shared neighbours, one thread per (neighbour, column), each thread
-// loading its U column once and updating all rows of n.  Step 1 multiplies
-// by reciprocal pivots computed once per m.
+// positions and row starts).  Per m, "round A" loads m's neighbour list
+// (each neighbour's slot in n's list found by binary search in shared
+// memory, the shared ones listed through a shared-memory counter), U_mm and
+// its reciprocal pivots; it only reads finished nodes, so round A of m+1
+// runs during step 2 of m, into the other half of double-buffered tables.
+// Step 2 gives each thread one (shared neighbour, column) pair: it loads
+// that column of U_mq once and updates every row of n (each target is
+// updated once per m, so the list order does not matter).
+struct IluRoundA {
+  int *tslot, *toff, *toffT, *plist, *np;
+};
+
+template <class T>
+__device__ __forceinline__ void ilu_round_a(const IluArgs &g, int tid, int nt, int m, int mb,
+                                            int mnb, int nm, int Tr, const int64_t *mrow,
+                                            int moff, int moffT, const int *snb, int nb,
+                                            const T *__restrict__ lu, IluRoundA bufs, T *umm,
+                                            T *rdm) {
+  for (int t = tid; t < mnb; t += nt) {
+    const int q = g.nbr_node[mb + t];
+    int slot = -1;
+    if (q > m) {
+      int lo = 0, hi = nb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (snb[mid] < q) lo = mid + 1; else hi = mid;
+      }
+      if (snb[lo] == q) slot = lo;
+    }
+    bufs.tslot[t] = slot;
+    if (slot >= 0) {
+      bufs.toff[t] = g.nbr_off[mb + t];
+      bufs.toffT[t] = g.nbr_offT[mb + t];
+      bufs.plist[atomicAdd(bufs.np, 1)] = t;
+    }
+  }
+  for (int w = tid; w < nm * nm; w += nt) {
+    const int dk = w / nm, d2 = w - dk * nm;
+    const bool rowkT = dk == Tr;
+    T u = (T)0;
+    if (d2 >= dk && !(rowkT && d2 >= g.nvn)) u = lu[mrow[dk] + (rowkT ? moffT : moff) + d2];
+    umm[dk * kMaxNodeDofs + d2] = u;
+    if (d2 == dk) rdm[dk] = (T)1 / u;
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(256)
     ilu0_block_kernel(const int *__restrict__ nodes, IluArgs g, const double *__restrict__ A,
@@ -356,26 +418,28 @@ __global__ void __launch_bounds__(256)
   int64_t *srow = reinterpret_cast<int64_t *>(sm_raw);          // [maxnb][maxnr] row starts of m
   T *blk = reinterpret_cast<T *>(srow + (size_t)g.maxnb * g.maxnr);  // [maxnr][lmax]
   T *lnm = blk + (size_t)g.maxnr * g.lmax;                       // [16][16] L_nm
-  T *umm = lnm + kMaxNodeDofs * kMaxNodeDofs;                    // [16][16] U_mm
-  T *rdm = umm + kMaxNodeDofs * kMaxNodeDofs;                    // [16] 1 / U_mm diagonal
-  int *snb = reinterpret_cast<int *>(rdm + kMaxNodeDofs);        // [maxnb] neighbours of n
+  T *umm2 = lnm + kMaxNodeDofs * kMaxNodeDofs;                   // [2][16][16] U_mm
+  T *rdm2 = umm2 + 2 * kMaxNodeDofs * kMaxNodeDofs;              // [2][16] 1 / U_mm diagonal
+  int *snb = reinterpret_cast<int *>(rdm2 + 2 * kMaxNodeDofs);   // [maxnb] neighbours of n
   int *soff = snb + g.maxnb;                                     // their column offsets
   int *sndof = soff + g.maxnb;                                   // their unknown counts
   int *smb = sndof + g.maxnb;        // lower neighbour m: start of its neighbour list
   int *smnb = smb + g.maxnb;         // its length
   int *smoff = smnb + g.maxnb;       // m's own block in m's rows (offset, energy-row offset)
   int *smoffT = smoff + g.maxnb;
-  int *tslot = smoffT + g.maxnb;     // per neighbour t of m: slot in n's list, or -1
-  int *toff = tslot + g.maxnb;       //   its column offsets in m's rows
-  int *toffT = toff + g.maxnb;
-  int *plist = toffT + g.maxnb;      // compacted t with tslot[t] >= 0
-  int *s_np = plist + g.maxnb;
+  int *tab = smoffT + g.maxnb;       // [2][4][maxnb] round-A tables, then [2] counters
+  int *s_np = tab + 8 * g.maxnb;
+  auto bufs = [&](int h) {
+    int *b0 = tab + 4 * h * g.maxnb;
+    return IluRoundA{b0, b0 + g.maxnb, b0 + 2 * g.maxnb, b0 + 3 * g.maxnb, s_np + h};
+  };
   const int n = nodes[blockIdx.x];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+  const int tid = threadIdx.x, nt = blockDim.x;
   const int base = g.nbr_ptr[n], nb = g.nbr_ptr[n + 1] - base;
   const int f0 = g.fu[n], nr = g.fu[n + 1] - f0;
   const int Tr = g.energy ? g.dim : -1;  // local index of the energy row
   const int self = g.nbr_self[n];
+  if (tid < 2) s_np[tid] = 0;
   for (int s2 = tid; s2 < nb; s2 += nt) {
     const int q = g.nbr_node[base + s2];
     snb[s2] = q;
@@ -411,54 +475,17 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
+  if (self > 0)
+    ilu_round_a<T>(g, tid, nt, snb[0], smb[0], smnb[0], sndof[0], Tr, srow, smoff[0], smoffT[0],
+                   snb, nb, lu, bufs(0), umm2, rdm2);
   __syncthreads();
   for (int sm = 0; sm < self; sm++) {
-    const int m = snb[sm], mb = smb[sm], mnb = smnb[sm];
+    const int h = sm & 1;
+    const IluRoundA cur = bufs(h);
+    const T *umm = umm2 + h * kMaxNodeDofs * kMaxNodeDofs;
+    const T *rdm = rdm2 + h * kMaxNodeDofs;
     const int nm = sndof[sm], cm = soff[sm];
     const int64_t *mrow = srow + (size_t)sm * g.maxnr;
-    // round A: m's neighbours q > m that are also neighbours of n (slot in
-    // n's list by binary search in shared memory), their column offsets,
-    // and U_mm
-    for (int t = tid; t < mnb; t += nt) {
-      const int q = g.nbr_node[mb + t];
-      int slot = -1;
-      if (q > m) {
-        int lo = 0, hi = nb - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (snb[mid] < q) lo = mid + 1; else hi = mid;
-        }
-        if (snb[lo] == q) slot = lo;
-      }
-      tslot[t] = slot;
-      if (slot >= 0) {
-        toff[t] = g.nbr_off[mb + t];
-        toffT[t] = g.nbr_offT[mb + t];
-      }
-    }
-    for (int w = tid; w < nm * nm; w += nt) {
-      const int dk = w / nm, d2 = w - dk * nm;
-      const bool rowkT = dk == Tr;
-      T u = (T)0;
-      if (d2 >= dk && !(rowkT && d2 >= g.nvn))
-        u = lu[mrow[dk] + (rowkT ? smoffT[sm] : smoff[sm]) + d2];
-      umm[dk * kMaxNodeDofs + d2] = u;
-    }
-    __syncthreads();
-    if (tid < nm) rdm[tid] = (T)1 / umm[tid * kMaxNodeDofs + tid];
-    if (tid < 32) {
-      // compact the shared neighbours (ascending t)
-      int cnt = 0;
-      for (int t0 = 0; t0 < mnb; t0 += 32) {
-        const int t = t0 + lane;
-        const bool hit = t < mnb && tslot[t] >= 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, hit);
-        if (hit) plist[cnt + __popc(bal & ((1u << lane) - 1u))] = t;
-        cnt += __popc(bal);
-      }
-      if (lane == 0) *s_np = cnt;
-    }
-    __syncthreads();
     // step 1: L_nm = A_nm U_mm^-1, one thread per row, from shared memory
     if (tid < nr) {
       const int r = tid;
@@ -478,14 +505,21 @@ __global__ void __launch_bounds__(256)
       }
     }
     __syncthreads();
+    // round A of the next neighbour, into the other half of the tables
+    // (its counter was reset before the barrier that ended its last use)
+    if (sm + 1 < self)
+      ilu_round_a<T>(g, tid, nt, snb[sm + 1], smb[sm + 1], smnb[sm + 1], sndof[sm + 1], Tr,
+                     srow + (size_t)(sm + 1) * g.maxnr, smoff[sm + 1], smoffT[sm + 1], snb, nb,
+                     lu, bufs(h ^ 1), umm2 + (h ^ 1) * kMaxNodeDofs * kMaxNodeDofs,
+                     rdm2 + (h ^ 1) * kMaxNodeDofs);
     // step 2: A_nq -= L_nm U_mq, one thread per (shared neighbour, column d)
     // loading the column of U_mq once and updating every row of n
-    const int np = *s_np;
+    const int np = *cur.np;
     for (int f = tid; f < np * g.maxnr; f += nt) {
       const int k = f / g.maxnr, d = f - k * g.maxnr;
-      const int t = plist[k], slot = tslot[t];
+      const int t = cur.plist[k], slot = cur.tslot[t];
       if (d >= sndof[slot]) continue;
-      const int off = toff[t], offT = toffT[t];
+      const int off = cur.toff[t], offT = cur.toffT[t];
       T u[kMaxNodeDofs];
 #pragma unroll
       for (int dk = 0; dk < kMaxNodeDofs; dk++) {
@@ -506,6 +540,7 @@ __global__ void __launch_bounds__(256)
       }
     }
     __syncthreads();
+    if (tid == 0) *cur.np = 0;  // free for the round A of neighbour sm + 2
   }
   // own diagonal block and the rest of the row
   const int cs = soff[self];
@@ -621,7 +656,6 @@ struct TrsvArgs {
   const int64_t *rowptr;
   const int *colidx;
   const int64_t *diag;
-  const uint16_t *rel; // entry p of an off-node segment is taken from segment start + rel[p]
   const int64_t *inv_ptr;  // node n's diagonal-block inverses start at inv_ptr[n] (L's, then U's)
   int num_nodes;
   int Tr;              // local index of the energy row, -1 without energy
@@ -860,6 +894,108 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
   }
 }
 
+// The same sweep with one warp per node, for meshes whose nodes have few
+// unknowns and short rows (QUAD9 problems: 2-6 rows of at most a few dozen
+// off-node entries).  A node's rows go to lane groups of G = 32 / R lanes
+// (R: the row count rounded up to a power of two), a group sums its row in
+// a fixed order (lane by lane, then a butterfly within the group), and the
+// block inverse is applied with one shuffle per row -- no shared memory and
+// no barrier, so a warp needs far fewer resources than a CTA and many more
+// nodes are in flight (each 128-thread CTA holds four).  Warp w of the grid
+// takes tickets w, w + W, ... (W warps in all), with the same progress
+// argument as the CTA sweep.  Used when every node has at most kWarpMaxRows
+// rows and every row's off-node segment fits its group's prefetch window.
+static constexpr int kWarpMaxRows = 8;
+static constexpr int kPrefetchW = 8;
+static constexpr int kWarpSweepThreads = 128;
+
+template <class T, bool LOWER>
+__global__ void __launch_bounds__(kWarpSweepThreads)
+    trsv_sync_free_warp_kernel(TrsvArgs g, const T *__restrict__ lus,
+                               const T *__restrict__ binv, const T *__restrict__ b, T *x) {
+  using A = acc_t<T>;
+  const int lane = threadIdx.x & 31;
+  const unsigned nt = (unsigned)g.num_nodes;
+  const unsigned wpb = blockDim.x >> 5, stride = gridDim.x * wpb;
+  unsigned t = blockIdx.x * wpb + (threadIdx.x >> 5);
+  longlong2 tk = t < nt ? g.tick[t] : make_longlong2(0, 0);
+  for (; t < nt; t += stride) {
+    const int f0 = (int)(tk.x & 0xffffffffll), nr = (int)(tk.x >> 32);
+    const int64_t inv_off = tk.y;
+    int R = 1;
+    while (R < nr) R <<= 1;
+    const int G = 32 / R;                     // lanes per row
+    const int r = lane / G, gl = lane - r * G;
+    const bool act = r < nr;
+    A pv[kPrefetchW];
+    int pc[kPrefetchW];
+    int64_t pr0 = 0, pr1 = 0;
+    if (act) {
+      const longlong2 sg = g.seg[f0 + r];
+      pr0 = sg.x;
+      pr1 = sg.y;
+    }
+#pragma unroll
+    for (int k = 0; k < kPrefetchW; k++) {
+      const int64_t p = pr0 + gl + (int64_t)G * k;
+      pv[k] = p < pr1 ? (A)lus[p] : (A)0;
+      pc[k] = p < pr1 ? g.cols[p] : -1;
+    }
+    // lane c < nr holds row c of the block inverse
+    A dv[kWarpMaxRows];
+#pragma unroll
+    for (int c = 0; c < kWarpMaxRows; c++)
+      dv[c] = (lane < nr && c < nr) ? (A)binv[inv_off + (int64_t)c * nr + lane] : (A)0;
+    const A rhs_r = act ? (A)__ldcg(b + f0 + r) : (A)0;
+    if (t + stride < nt) tk = g.tick[t + stride];
+    // stage A: the row's off-node sum, values added in the fixed order as
+    // they arrive (a wait re-polls only its own value)
+    bool gave_up = false;
+    A zv[kPrefetchW];
+    unsigned pending = 0;
+#pragma unroll
+    for (int k = 0; k < kPrefetchW; k++) {
+      zv[k] = 0;
+      if (pc[k] >= 0) {
+        const T v = ld_relaxed(x + pc[k]);
+        if (unpublished(v)) pending |= 1u << k; else zv[k] = (A)v;
+      }
+    }
+    A s0 = 0;
+    long long polls = 0;
+#pragma unroll
+    for (int k = 0; k < kPrefetchW; k++) {
+      while (!gave_up && (pending & (1u << k))) {
+        if (++polls > g.spin_limit || ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
+          gave_up = true;
+          break;
+        }
+        const T v = ld_relaxed(x + pc[k]);
+        if (!unpublished(v)) {
+          zv[k] = (A)v;
+          pending &= ~(1u << k);
+        }
+      }
+      if (pc[k] >= 0) s0 = fmx(pv[k], zv[k], s0);
+    }
+    for (int64_t p = pr0 + gl + (int64_t)G * kPrefetchW; p < pr1; p += G)
+      s0 = fmx((A)lus[p], (A)poll_value(x + g.cols[p], gave_up, g.error, g.spin_limit), s0);
+    for (int o = G >> 1; o > 0; o >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    const A bvr = rhs_r - s0;
+    // stage B: x_n = D^-1 (rhs - off-node part), products in column order
+    A v = 0;
+#pragma unroll
+    for (int c = 0; c < kWarpMaxRows; c++) {
+      if (c < nr) {
+        const A bc = __shfl_sync(0xffffffffu, bvr, c * G);
+        if (lane < nr && (LOWER ? c <= lane : c >= lane)) v = fmx(dv[c], bc, v);
+      }
+    }
+    if (lane < nr) st_relaxed(x + f0 + lane, (T)v);
+    if (__any_sync(0xffffffffu, gave_up) && lane == 0) atomicExch(g.error, 1);
+  }
+}
+
 // One dependency level of a triangular sweep, one CTA per node: the nodes of
 // a level do not depend on each other, so the launch boundary is the only
 // synchronisation.  Same two stages as the sync-free sweep (rows over the
@@ -921,7 +1057,6 @@ static TrsvArgs trsv_args(const Solver *S) {
   g.rowptr = S->P.rowptr;
   g.colidx = S->P.colidx;
   g.diag = S->P.diag;
-  g.rel = S->d_sweep_rel;
   g.inv_ptr = S->d_inv_ptr;
   g.num_nodes = S->C->L.num_nodes;
   g.Tr = S->C->L.energy ? S->C->L.dim : -1;
@@ -982,7 +1117,7 @@ void build_ilu_schedule(const Layout &L, IluSchedule &S) {
 Solver::~Solver() {
   if (prec64) cudaGraphExecDestroy(prec64);
   if (prec32) cudaGraphExecDestroy(prec32);
-  void *p[] = {d_lu, d_lu32, d_lus, d_lus32, d_binv, d_binv32, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
+  void *p[] = {d_lu, d_lu32, d_lus, d_lus32, d_binv, d_binv32, d_Z, d_a32, d_diag, d_lo_nodes, d_up_nodes, d_scale, d_work, d_flags,
                d_sweep_y, d_V, d_V32, d_t, d_w, d_r, d_xs, d_t32, d_w32};
   for (void *q : p)
     if (q) cudaFree(q);
@@ -1116,6 +1251,21 @@ int Solver::init(Context *c, int krylov) {
         sl[i] = make_longlong2(LP->rowptr[i], di - r);
         su[i] = make_longlong2(di + 1 + na, LP->rowptr[i + 1]);
       }
+    }
+    // one warp per node when every node has at most kWarpMaxRows rows and
+    // every row's off-node segments fit its lane group's prefetch window
+    {
+      bool fits = true;
+      for (int n = 0; n < LP->num_nodes && fits; n++) {
+        const int f0 = LP->fu[n], nr = LP->fu[n + 1] - f0;
+        int R = 1;
+        while (R < nr) R <<= 1;
+        const int64_t cap = (int64_t)(32 / R) * kPrefetchW;
+        if (nr > kWarpMaxRows) fits = false;
+        for (int r = 0; r < nr && fits; r++)
+          if (sl[f0 + r].y - sl[f0 + r].x > cap || su[f0 + r].y - su[f0 + r].x > cap) fits = false;
+      }
+      warp_sweep = fits;
     }
     auto ticks = [&](const std::vector<int> &order, bool upper) {
       std::vector<longlong2> tk(order.size());
@@ -1394,9 +1544,14 @@ static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStr
                           (const void *)trsv_sync_free_kernel<double, false>,
                           (const void *)trsv_sync_free_kernel<float, true>,
                           (const void *)trsv_sync_free_kernel<float, false>};
-    for (const void *f : fns) {
+    const void *wfns[4] = {(const void *)trsv_sync_free_warp_kernel<double, true>,
+                           (const void *)trsv_sync_free_warp_kernel<double, false>,
+                           (const void *)trsv_sync_free_warp_kernel<float, true>,
+                           (const void *)trsv_sync_free_warp_kernel<float, false>};
+    const int threads = S->warp_sweep ? kWarpSweepThreads : kTrsvThreads;
+    for (const void *f : S->warp_sweep ? wfns : fns) {
       int b = 0;
-      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kTrsvThreads, 0), "occupancy");
+      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, 0), "occupancy");
       per_sm = std::min(per_sm, b);
     }
     cudaGetDevice(&dev);
@@ -1421,11 +1576,17 @@ static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStr
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y);
   g.tick = lo_tick;
   g.seg = S->d_segL;
-  trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, z, y);
+  if (S->warp_sweep)
+    trsv_sync_free_warp_kernel<T, true><<<grid, kWarpSweepThreads, 0, st>>>(g, lus, binv, z, y);
+  else
+    trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, z, y);
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z);
   g.tick = S->d_tick_up;
   g.seg = S->d_segU;
-  trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, y, z);
+  if (S->warp_sweep)
+    trsv_sync_free_warp_kernel<T, false><<<grid, kWarpSweepThreads, 0, st>>>(g, lus, binv, y, z);
+  else
+    trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, y, z);
   GB_CU(cudaGetLastError(), "trsv");
   return 0;
 }
@@ -1501,7 +1662,7 @@ int row_sum_scale(Context *C, double *vals, double *R, cudaStream_t st) {
 // system's true residual <= tol * ||b|| or after maxit iterations.
 template <class T>
 static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int *its,
-                 double *relres, cudaStream_t st) {
+                 double *relres, cudaStream_t st, bool flexible = false) {
   Solver &S = *C->solver;
   const Layout &L = C->L;
   const int N = L.N, lpr = lanes_per_row(L);
@@ -1544,18 +1705,32 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
     int j = 0;
     bool done = false;
     for (; j < m && total < maxit; j++) {
-      GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
-      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
-      GB_CU(spmv<T>(C, lpr, A, t, w, st), "spmv");
+      const T *zj = t;  // M^-1 v_j
+      if constexpr (std::is_same<T, double>::value) {
+        if (flexible) {
+          // the preconditioner in FP32: v_j -> FP32, sweeps, z_j kept in FP64
+          to_f32_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, V + j * ld, S.d_t32);
+          if (S.apply_prec32(st)) return -1;
+          to_f64_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, S.d_t32, S.d_Z + j * ld);
+          zj = S.d_Z + j * ld;
+        }
+      }
+      if (!flexible) {
+        GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
+        if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      }
+      GB_CU(spmv<T>(C, lpr, A, zj, w, st), "spmv");
       // CGS2 on the device; the host reads both passes and the norm in one copy
       std::vector<double> hcol(j + 2, 0.0);
       double *dh1 = dh, *dh2 = dh + (m + 2), *dnrm = dh + 2 * (m + 2);
-      multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
+      multidot_tile_kernel<T><<<dim3(kRedBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
+          N, j + 1, V, ld, w, dpart);
       // one thread per coefficient (restart lengths up to 1023)
       const int fin = ((j + 1 + 31) / 32) * 32;
       multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh1);
       gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
-      multidot_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, w, dpart);
+      multidot_tile_kernel<T><<<dim3(kRedBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
+          N, j + 1, V, ld, w, dpart);
       multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh2);
       gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
       norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dred);
@@ -1597,8 +1772,14 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
     }
     memcpy(hh, y.data(), sizeof(double) * j);
     GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double) * j, cudaMemcpyHostToDevice, st), "y");
-    gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, V, ld, dh, t);
-    if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+    if constexpr (std::is_same<T, double>::value) {
+      // flexible: x += Z y, the preconditioned vectors as they were applied
+      if (flexible) gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, S.d_Z, ld, dh, t);
+    }
+    if (!flexible) {
+      gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, V, ld, dh, t);
+      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+    }
     add_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, t, x);
     // true residual r = b - A x into V0
     GB_CU(spmv<T>(C, lpr, A, x, V, st), "spmv");
@@ -1876,6 +2057,17 @@ static int linear_solve_impl(Context *C, const double *R, double *dx, const Line
   const int N = C->L.N;
   s->iterations = 0;
   s->refinements = 0;
+  if (o.fp32_prec) {
+    if (S.nseg > 1)
+      return fail("the FP32 preconditioner mode serves one system per context");
+    if (!S.d_Z) GB_CU(cudaMalloc(&S.d_Z, sizeof(double) * (size_t)S.max_krylov * N), "Z basis");
+    int its;
+    double rr;
+    if (gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st, true)) return -1;
+    s->iterations = its;
+    s->relres = rr;
+    return 0;
+  }
   if (!o.fp32_inner) {
     int its;
     double rr;
@@ -1903,9 +2095,12 @@ static int linear_solve_impl(Context *C, const double *R, double *dx, const Line
     int its;
     double rr;
     float *sol32 = (float *)S.d_xs + N;
-    if (S.nseg > 1 ? gmres_seg<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr,
-                                      st)
-                   : gmres<float>(C, r32, sol32, o.inner_tol, o.maxit, o.krylov, &its, &rr, st))
+    // each inner solve goes no further than the outer target needs (a loose
+    // forcing-rule tolerance is met by one inner solve), nor further than
+    // inner_tol (beyond it FP32 arithmetic limits what a solve attains)
+    const double itol = std::max(o.inner_tol, o.tol * bnorm / rn);
+    if (S.nseg > 1 ? gmres_seg<float>(C, r32, sol32, itol, o.maxit, o.krylov, &its, &rr, st)
+                   : gmres<float>(C, r32, sol32, itol, o.maxit, o.krylov, &its, &rr, st))
       return -1;
     s->iterations += its;
     s->refinements++;

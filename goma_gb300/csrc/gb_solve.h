@@ -94,10 +94,12 @@ struct Solver {
   float *d_V32 = nullptr;       // (m+1) x N Krylov basis (FP32)
   double *d_t = nullptr, *d_w = nullptr, *d_r = nullptr, *d_xs = nullptr;
   float *d_t32 = nullptr, *d_w32 = nullptr;
+  double *d_Z = nullptr;        // m x N preconditioned vectors (flexible GMRES)
   cudaGraphExec_t prec64 = nullptr, prec32 = nullptr;  // captured ILU solves on d_t / d_t32
   unsigned *d_flags = nullptr;  // sync-free sweeps: [4] error word
   void *d_sweep_y = nullptr;    // sync-free sweeps: the L sweep's output (N values)
   int trsv_grid = 0, prep_grid = 0;
+  bool warp_sweep = false;      // sync-free sweeps with one warp per node (short rows)
   int check_trsv_error();
   // level-scheduled sweeps from a captured graph (else the sync-free ones)
   bool use_level_graph() const;
@@ -122,7 +124,9 @@ struct LinearOpts {
   int maxit = 500;          // "Maximum Linear Solve Iterations"
   double tol = 1e-6;        // "Linear Solver Tolerance" (relative residual)
   bool fp32_inner = false;  // FP32 GMRES inside FP64 iterative refinement
+  bool fp32_prec = false;   // FP64 flexible GMRES, ILU(0) factorised and applied in FP32
   double inner_tol = 1e-3;  // FP32 inner relative tolerance
+  bool fp32_factors() const { return fp32_inner || fp32_prec; }
   int max_refinements = 20;
 };
 struct LinearStats {

@@ -218,14 +218,20 @@ class GomaNewton:
 
     def newton_opts(self, **kw):
         """gb_newton_opts with the defaults of gb_newton_opts_default and the
-        given fields (fp32_inner sets linear_precision); an unknown name is an
-        error rather than a silently ignored attribute."""
+        given fields (fp32_inner=True sets linear_precision to FP32 inner
+        GMRES inside FP64 refinement, fp32_preconditioner=True to FP64
+        flexible GMRES with the ILU(0) factorised and applied in FP32); an
+        unknown name is an error rather than a silently ignored attribute."""
         o = _lib.NewtonOpts()
         self._L.gb_newton_opts_default(ctypes.byref(o))
         fields = {f[0] for f in o._fields_}
         for k, v in kw.items():
-            if k == "fp32_inner":
-                o.linear_precision = 1 if v else 0
+            if k in ("fp32_inner", "fp32_preconditioner"):
+                mode = 1 if k == "fp32_inner" else 2
+                if v:
+                    o.linear_precision = mode
+                elif o.linear_precision == mode:
+                    o.linear_precision = 0
             elif k in fields:
                 setattr(o, k, v)
             else:

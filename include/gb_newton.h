@@ -201,6 +201,14 @@ int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
 
 #define GB_LINEAR_FP64 0
 #define GB_LINEAR_FP32_REFINED 1
+/* FP64 flexible GMRES (the Krylov basis, Gram-Schmidt and the matrix in
+ * FP64) whose ILU(0) preconditioner is factorised and applied in FP32: the
+ * triangular sweeps, the cost of an iteration, run at the FP32 rate while
+ * the Krylov process keeps FP64 accuracy; the flexible form (the
+ * preconditioned vectors kept) makes the FP32 rounding of the sweeps
+ * harmless to convergence.  One system per context (not for several
+ * independent problems in one matrix). */
+#define GB_LINEAR_FP32_PRECONDITIONER 2
 
 /* ILU(0) factorisation reuse, the reference's "Matrix Factorization Reuse"
  * card (src/mm_sol_nonlinear.c:1688-1709, src/sl_util.c:721-734):
@@ -225,8 +233,10 @@ typedef struct gb_newton_opts {
                               context) */
   int max_linear_its;      /* "Maximum Linear Solve Iterations" */
   double linear_tol;       /* "Linear Solver Tolerance" (relative residual) */
-  int linear_precision;    /* GB_LINEAR_FP64 or GB_LINEAR_FP32_REFINED */
-  double inner_tol;        /* FP32 inner GMRES tolerance (refined mode) */
+  int linear_precision;    /* GB_LINEAR_FP64, _FP32_REFINED or _FP32_PRECONDITIONER */
+  double inner_tol;        /* refined mode: the tightest relative tolerance of one
+                              FP32 inner GMRES solve (an inner solve stops sooner
+                              when the outer tolerance allows it) */
   int max_refinements;     /* FP64 refinement steps (refined mode) */
   int verbose;             /* 1: one line per Newton step on stdout */
   /* Inexact Newton: 0 solves every linear system to linear_tol; 1 chooses

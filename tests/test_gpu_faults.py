@@ -32,9 +32,14 @@ def _scaled_system(prob, seed):
     return o, a_s, R_s
 
 
+@pytest.mark.parametrize("prob_fn", [lambda: pb.boussinesq_cube_3d(3, 1e4, 0.71),
+                                     lambda: pb.lid_cavity_2d(8, 100.0)],
+                         ids=["cube_cta_per_node", "cavity_warp_per_node"])
 @pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
-def test_sweep_wait_gives_up_and_the_context_recovers(fp32):
-    prob = pb.boussinesq_cube_3d(3, 1e4, 0.71)
+def test_sweep_wait_gives_up_and_the_context_recovers(fp32, prob_fn):
+    """Both sync-free sweep kernels: a CTA per node (the HEX27 cube's long
+    rows) and a warp per node (the QUAD9 cavity's short rows)."""
+    prob = prob_fn()
     o, a_s, R_s = _scaled_system(prob, 2)
     gn = GomaNewton(prob)
     gn.set_triangular_solve(0)   # the sync-free sweeps

@@ -1,6 +1,8 @@
-"""GPU Newton (assembly + row-sum scaling + ILU(0)-GMRES, FP64 and FP32
-refined) against the reference's converged solutions: fields within 1e-8
-relative of the reference's FP64 Newton solution."""
+"""GPU Newton (assembly + row-sum scaling + ILU(0)-GMRES in FP64, FP32
+inner GMRES inside FP64 refinement, and FP64 flexible GMRES with the
+ILU(0) factorised and applied in FP32) against the reference's converged
+solutions: fields within 1e-8 relative of the reference's FP64 Newton
+solution."""
 import numpy as np
 import pytest
 
@@ -11,12 +13,14 @@ from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
 TOL_X = 1e-8
+PRECISIONS = {"fp64": {}, "fp32_refined": {"fp32_inner": True},
+              "fp32_preconditioner": {"fp32_preconditioner": True}}
 
 
 @pytest.mark.parametrize("ordering", [0, 1], ids=["ilu_natural", "ilu_multicolour"])
-@pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
+@pytest.mark.parametrize("precision", list(PRECISIONS))
 @pytest.mark.parametrize("name", gc.names("solve"))
-def test_gpu_newton_matches_reference_solution(name, fp32_inner, ordering):
+def test_gpu_newton_matches_reference_solution(name, precision, ordering):
     """Both ILU(0) node orders: the preconditioner changes the Krylov
     iterates, never the converged Newton solution."""
     g, case = gc.load(name)
@@ -24,15 +28,15 @@ def test_gpu_newton_matches_reference_solution(name, fp32_inner, ordering):
     gn.set_ilu_ordering(ordering)
     x0 = g["x0"] if "x0" in g else None
     x, conv, st = gn.solve_nonlinear_problem(x0, residual_tol=1e-11, linear_tol=1e-10,
-                                             fp32_inner=fp32_inner, max_newton=30)
+                                             max_newton=30, **PRECISIONS[precision])
     assert conv, st
     xc = g["x_converged"]
     assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
 
 
-@pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
+@pytest.mark.parametrize("precision", list(PRECISIONS))
 @pytest.mark.parametrize("name", gc.names("solve", compact=True))
-def test_gpu_newton_matches_reference_solution_at_benchmark_size(name, fp32_inner):
+def test_gpu_newton_matches_reference_solution_at_benchmark_size(name, precision):
     """The 32 x 32 lid-driven cavity at Re 100 (the benchmark size, 11,522
     unknowns) from rest to the scaled residual 1e-10, against the reference's
     converged fields, with the reference's solver settings (ILU(0) in its
@@ -41,8 +45,8 @@ def test_gpu_newton_matches_reference_solution_at_benchmark_size(name, fp32_inne
     gn = GomaNewton(gc.problem_from_case(case))
     gn.set_ilu_ordering(0)
     x, conv, st = gn.solve_nonlinear_problem(None, residual_tol=case["tol"], linear_tol=1e-10,
-                                             fp32_inner=fp32_inner, max_newton=30,
-                                             krylov_dim=30, max_linear_its=3000)
+                                             max_newton=30, krylov_dim=30, max_linear_its=3000,
+                                             **PRECISIONS[precision])
     assert conv, st
     xc = g["x_converged"]
     assert np.abs(x - xc).max() <= TOL_X * np.abs(xc).max()
