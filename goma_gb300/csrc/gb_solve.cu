@@ -904,7 +904,8 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
 // nodes are in flight (each 128-thread CTA holds four).  Warp w of the grid
 // takes tickets w, w + W, ... (W warps in all), with the same progress
 // argument as the CTA sweep.  Used when every node has at most kWarpMaxRows
-// rows and every row's off-node segment fits its group's prefetch window.
+// rows and every row's off-node segment fits its group's prefetch window:
+// always in FP32, in FP64 only for wide levels (Solver::init).
 static constexpr int kWarpMaxRows = 8;
 static constexpr int kPrefetchW = 8;
 static constexpr int kWarpSweepThreads = 128;
@@ -1265,7 +1266,12 @@ int Solver::init(Context *c, int krylov) {
         for (int r = 0; r < nr && fits; r++)
           if (sl[f0 + r].y - sl[f0 + r].x > cap || su[f0 + r].y - su[f0 + r].x > cap) fits = false;
       }
-      warp_sweep = fits;
+      // FP32 sweeps take the warp form whenever it fits; FP64 ones only when
+      // the levels are wide (several independent problems interleaved), as
+      // the FP64 warp form's 85 registers a thread cost more than its
+      // shorter critical path saves on a single mesh
+      warp_sweep32 = fits;
+      warp_sweep64 = fits && LP->num_nodes > 300LL * (int64_t)lo_ptr.size();
     }
     auto ticks = [&](const std::vector<int> &order, bool upper) {
       std::vector<longlong2> tk(order.size());
@@ -1548,15 +1554,22 @@ static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStr
                            (const void *)trsv_sync_free_warp_kernel<double, false>,
                            (const void *)trsv_sync_free_warp_kernel<float, true>,
                            (const void *)trsv_sync_free_warp_kernel<float, false>};
-    const int threads = S->warp_sweep ? kWarpSweepThreads : kTrsvThreads;
-    for (const void *f : S->warp_sweep ? wfns : fns) {
+    int wper_sm = 1 << 30;
+    for (const void *f : fns) {
       int b = 0;
-      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, threads, 0), "occupancy");
+      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kTrsvThreads, 0), "occupancy");
       per_sm = std::min(per_sm, b);
+    }
+    for (const void *f : wfns) {
+      int b = 0;
+      GB_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f, kWarpSweepThreads, 0),
+            "occupancy");
+      wper_sm = std::min(wper_sm, b);
     }
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     S->trsv_grid = std::max(1, per_sm) * sms;
+    S->trsv_grid_warp = std::max(1, wper_sm) * sms;
     S->prep_grid = 2 * sms;
   }
   TrsvArgs g = trsv_args(S);  // the tickets and segments are set per sweep below
@@ -1567,7 +1580,8 @@ static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStr
   // reverse order (every dependency after its dependant) on one CTA, whose
   // first wait can then only end by running out
   const longlong2 *lo_tick = S->d_tick_lo;
-  int grid = S->trsv_grid;
+  const bool warp = sizeof(T) == 4 ? S->warp_sweep32 : S->warp_sweep64;
+  int grid = warp ? S->trsv_grid_warp : S->trsv_grid;
   if (S->C->sweep_reverse_lower) {
     lo_tick = S->d_tick_lo_rev;
     grid = 1;
@@ -1576,14 +1590,14 @@ static int sync_free_apply(Solver *S, const T *lus, const T *binv, T *z, cudaStr
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, y);
   g.tick = lo_tick;
   g.seg = S->d_segL;
-  if (S->warp_sweep)
+  if (warp)
     trsv_sync_free_warp_kernel<T, true><<<grid, kWarpSweepThreads, 0, st>>>(g, lus, binv, z, y);
   else
     trsv_sync_free_kernel<T, true><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, z, y);
   trsv_prepare_kernel<T><<<S->prep_grid, 256, 0, st>>>(S->N, z);
   g.tick = S->d_tick_up;
   g.seg = S->d_segU;
-  if (S->warp_sweep)
+  if (warp)
     trsv_sync_free_warp_kernel<T, false><<<grid, kWarpSweepThreads, 0, st>>>(g, lus, binv, y, z);
   else
     trsv_sync_free_kernel<T, false><<<grid, kTrsvThreads, 0, st>>>(g, lus, binv, y, z);

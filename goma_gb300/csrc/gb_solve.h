@@ -99,7 +99,9 @@ struct Solver {
   unsigned *d_flags = nullptr;  // sync-free sweeps: [4] error word
   void *d_sweep_y = nullptr;    // sync-free sweeps: the L sweep's output (N values)
   int trsv_grid = 0, prep_grid = 0;
-  bool warp_sweep = false;      // sync-free sweeps with one warp per node (short rows)
+  int trsv_grid_warp = 0;
+  // sync-free sweeps with one warp per node (short rows), per precision
+  bool warp_sweep32 = false, warp_sweep64 = false;
   int check_trsv_error();
   // level-scheduled sweeps from a captured graph (else the sync-free ones)
   bool use_level_graph() const;

@@ -34,11 +34,12 @@ def _scaled_system(prob, seed):
 
 @pytest.mark.parametrize("prob_fn", [lambda: pb.boussinesq_cube_3d(3, 1e4, 0.71),
                                      lambda: pb.lid_cavity_2d(8, 100.0)],
-                         ids=["cube_cta_per_node", "cavity_warp_per_node"])
+                         ids=["cube", "cavity"])
 @pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32_refined"])
 def test_sweep_wait_gives_up_and_the_context_recovers(fp32, prob_fn):
     """Both sync-free sweep kernels: a CTA per node (the HEX27 cube's long
-    rows) and a warp per node (the QUAD9 cavity's short rows)."""
+    rows, and the cavity's FP64 sweeps) and a warp per node (the QUAD9
+    cavity's FP32 sweeps: short rows)."""
     prob = prob_fn()
     o, a_s, R_s = _scaled_system(prob, 2)
     gn = GomaNewton(prob)
