@@ -143,6 +143,7 @@ __global__ void norms_final_kernel(int nblocks, const double *__restrict__ part,
 // of them with one barrier per halving.  Grid (nblocks, column groups);
 // block b's sum for column j goes to part[j * gridDim.x + b].
 static constexpr int kMdCols = 8;
+static constexpr int kMdBlocks = 2 * kRedBlocks;  // block rows of a column group
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
     multidot_tile_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
@@ -189,6 +190,7 @@ __global__ void gemv_sub_kernel(int N, int k, const T *__restrict__ V, int64_t l
   using A = acc_t<T>;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     A s = (A)w[i];
+#pragma unroll 4
     for (int j = 0; j < k; j++) s = fmx((A)-h[j], (A)V[j * ld + i], s);
     w[i] = (T)s;
   }
@@ -201,6 +203,7 @@ __global__ void gemv_kernel(int N, int k, const T *__restrict__ V, int64_t ld,
   using A = acc_t<T>;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     A s = 0;
+#pragma unroll 4
     for (int j = 0; j < k; j++) s = fmx((A)c[j], (A)V[j * ld + i], s);
     y[i] = (T)s;
   }
@@ -486,23 +489,25 @@ __global__ void __launch_bounds__(256)
     const T *rdm = rdm2 + h * kMaxNodeDofs;
     const int nm = sndof[sm], cm = soff[sm];
     const int64_t *mrow = srow + (size_t)sm * g.maxnr;
-    // step 1: L_nm = A_nm U_mm^-1, one thread per row, from shared memory
-    if (tid < nr) {
-      const int r = tid;
+    // step 1: L_nm = A_nm U_mm^-1, a warp per row (lane d holds the row's
+    // entry in m's column d): per pivot one shuffle, then every later
+    // column updated at once
+    for (int r = tid >> 5; r < nr; r += nt >> 5) {
+      const int lane = tid & 31;
       T *br = blk + (size_t)r * g.lmax + cm;
+      T v = lane < nm ? br[lane] : (T)0;
       for (int dk = 0; dk < nm; dk++) {
-        if (r == Tr && dk >= g.nvn) {
-          lnm[r * kMaxNodeDofs + dk] = (T)0;
+        if (r == Tr && dk >= g.nvn) {  // energy row: no pressure columns
+          if (lane == 0) lnm[r * kMaxNodeDofs + dk] = (T)0;
           continue;
         }
-        const T l = br[dk] * rdm[dk];
-        br[dk] = l;
-        lnm[r * kMaxNodeDofs + dk] = l;
-        for (int d2 = dk + 1; d2 < nm; d2++) {
-          if (r == Tr && d2 >= g.nvn) continue;
-          br[d2] -= l * umm[dk * kMaxNodeDofs + d2];  // zero where U_mm has no entry
-        }
+        const T l = __shfl_sync(0xffffffffu, v, dk) * rdm[dk];
+        if (lane == dk) v = l;
+        if (lane == 0) lnm[r * kMaxNodeDofs + dk] = l;
+        if (lane > dk && lane < nm && !(r == Tr && lane >= g.nvn))
+          v -= l * umm[dk * kMaxNodeDofs + lane];  // zero where U_mm has no entry
       }
+      if (lane < nm) br[lane] = v;
     }
     __syncthreads();
     // round A of the next neighbour, into the other half of the tables
@@ -1332,7 +1337,7 @@ int Solver::init(Context *c, int krylov) {
   }
   GB_CU(cudaMalloc(&d_lu, sizeof(double) * nnz), "ILU factors");
   GB_CU(cudaMalloc(&d_scale, sizeof(double) * N), "scale");
-  const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kRedBlocks + 4 * (krylov + 2) + 96);
+  const size_t wk = (size_t)(kRedBlocks * 3 + (krylov + 2) * kMdBlocks + 4 * (krylov + 2) + 96);
   GB_CU(cudaMalloc(&d_work, sizeof(double) * wk), "work");
   GB_CU(cudaMallocHost(&h_work, sizeof(double) * 4 * (krylov + 2) + 64 * sizeof(double)), "host");
   GB_CU(cudaMalloc(&d_V, sizeof(double) * (size_t)(krylov + 1) * N), "Krylov basis");
@@ -1688,7 +1693,10 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
   const int64_t ld = N;
   double *dred = S.d_work;                           // partials
   double *dh = S.d_work + kRedBlocks * 3 + 16;       // (m+2) results
-  double *dpart = dh + (m + 2) * 2 + 8;              // (m+2) * kRedBlocks
+  double *dpart = dh + (m + 2) * 2 + 8;              // (m+2) * kMdBlocks
+  // the row-parallel kernels (w -= V h, y = V c) get a thread per unknown:
+  // enough loads in flight to stream the basis at HBM speed
+  const int rows_grid = (N + kRedThreads - 1) / kRedThreads;
   double *hh = S.h_work;
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
   auto norm = [&](const T *v, double *out) -> int {
@@ -1737,16 +1745,16 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
       // CGS2 on the device; the host reads both passes and the norm in one copy
       std::vector<double> hcol(j + 2, 0.0);
       double *dh1 = dh, *dh2 = dh + (m + 2), *dnrm = dh + 2 * (m + 2);
-      multidot_tile_kernel<T><<<dim3(kRedBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
+      multidot_tile_kernel<T><<<dim3(kMdBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
           N, j + 1, V, ld, w, dpart);
       // one thread per coefficient (restart lengths up to 1023)
       const int fin = ((j + 1 + 31) / 32) * 32;
-      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh1);
-      gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
-      multidot_tile_kernel<T><<<dim3(kRedBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
+      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kMdBlocks, dpart, dh1);
+      gemv_sub_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
+      multidot_tile_kernel<T><<<dim3(kMdBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
           N, j + 1, V, ld, w, dpart);
-      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kRedBlocks, dpart, dh2);
-      gemv_sub_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
+      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kMdBlocks, dpart, dh2);
+      gemv_sub_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
       norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dred);
       norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, dred, dnrm);
       scale_copy_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dnrm, V + (j + 1) * ld);
@@ -1788,10 +1796,10 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
     GB_CU(cudaMemcpyAsync(dh, hh, sizeof(double) * j, cudaMemcpyHostToDevice, st), "y");
     if constexpr (std::is_same<T, double>::value) {
       // flexible: x += Z y, the preconditioned vectors as they were applied
-      if (flexible) gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, S.d_Z, ld, dh, t);
+      if (flexible) gemv_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j, S.d_Z, ld, dh, t);
     }
     if (!flexible) {
-      gemv_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, j, V, ld, dh, t);
+      gemv_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j, V, ld, dh, t);
       if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
     }
     add_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, t, x);
