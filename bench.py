@@ -680,14 +680,15 @@ def krylov_kernels(nel, iters=30, ra=1e4):
 
 
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
-                     predictors=("zeroth", "secant", "learned"), krylov=150):
+                     predictors=("zeroth", "secant", "learned"), krylov=150, fp32=True):
     """The learned-predictor configuration: backward-facing step, nx x ny
     QUAD9 Q2/P1, Carreau-Yasuda fluid (mu0 = 1, mu_inf = 0.01, lambda = 1,
     a = 2, n = 0.5), Re re0 -> re1 in nsteps uniform continuation steps, the
-    Newton solve to scaled |R| < 1e-10 at every step.  Each predictor runs
-    the same sweep (stopped after budget_s seconds); reported: steps done,
-    Newton and Krylov iterations, wall time, and for the learned run the
-    ratio of its guess residual to the secant guess's."""
+    Newton solve to scaled |R| < 1e-10 at every step (FP64 flexible GMRES
+    with the ILU(0) in FP32, or plain FP64 with fp32=False).  Each predictor
+    runs the same sweep (stopped after budget_s seconds); reported: steps
+    done, Newton and Krylov iterations, wall time, and for the learned run
+    the ratio of its guess residual to the secant guess's."""
     import time as _time
 
     import torch
@@ -695,11 +696,14 @@ def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150
     from goma_gb300.continuation import continuation
     from goma_gb300.newton import GomaNewton
     out = {"workload": "backward-facing step %dx%d QUAD9 Q2/P1, Carreau-Yasuda, Re %g -> %g in "
-                       "%d steps, scaled |R| < 1e-10" % (nx, ny, re0, re1, nsteps)}
+                       "%d steps, scaled |R| < 1e-10, %s" % (
+                           nx, ny, re0, re1, nsteps,
+                           "FP64 flexible GMRES(%d) with FP32 ILU(0)" % krylov if fp32
+                           else "FP64 ILU(0)-GMRES(%d)" % krylov)}
     for pred in predictors:
         gn = GomaNewton(pb.carreau_step_2d(nx, ny, re0))
         opts = dict(residual_tol=1e-10, linear_tol=1e-8, max_newton=25, max_linear_its=3000,
-                    krylov_dim=krylov, forcing=1, forcing_max=1e-2)
+                    krylov_dim=krylov, forcing=1, forcing_max=1e-2, fp32_preconditioner=fp32)
         t0 = _time.perf_counter()
         recs, _ = continuation(gn, re0, re1, nsteps, predictor=pred, newton_opts=opts,
                                learned_opts=dict(steps=300, batch=4096, lr=2e-3),
@@ -785,6 +789,9 @@ def main():
     ap.add_argument("--bfs-budget", type=float, default=150.0,
                     help="seconds per predictor of the bfs workload (the 200-step sweep stops "
                          "there)")
+    ap.add_argument("--bfs-fp64", action="store_true",
+                    help="the bfs workload's linear solves in FP64 (default: FP64 flexible "
+                         "GMRES with the ILU(0) in FP32)")
     ap.add_argument("--solve-krylov", type=int, default=300,
                     help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
@@ -1003,7 +1010,7 @@ def main():
                                              max_ratio=1.6, budget_s=900.0, check=1,
                                              max_linear_its=2500)
             elif w == "bfs":
-                extra[w] = bfs_continuation(budget_s=args.bfs_budget)
+                extra[w] = bfs_continuation(budget_s=args.bfs_budget, fp32=not args.bfs_fp64)
             elif w == "ilu_orders":
                 extra[w] = ilu_orders()
             elif w == "reuse":
