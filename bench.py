@@ -680,14 +680,17 @@ def krylov_kernels(nel, iters=30, ra=1e4):
 
 
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
-                     predictors=("zeroth", "secant", "learned"), krylov=150, fp32=True):
+                     predictors=("zeroth", "secant", "learned"), krylov=150, fp32=True,
+                     warm_steps=75):
     """The learned-predictor configuration: backward-facing step, nx x ny
     QUAD9 Q2/P1, Carreau-Yasuda fluid (mu0 = 1, mu_inf = 0.01, lambda = 1,
     a = 2, n = 0.5), Re re0 -> re1 in nsteps uniform continuation steps, the
     Newton solve to scaled |R| < 1e-10 at every step (FP64 flexible GMRES
     with the ILU(0) in FP32, or plain FP64 with fp32=False).  Each predictor
-    runs the same sweep (stopped after budget_s seconds); reported: steps
-    done, Newton and Krylov iterations, wall time, and for the learned run
+    runs the same sweep (stopped after budget_s seconds); the network is
+    trained with 300 Adam steps at its first training and warm_steps at each
+    later one (it carries over between steps).  Reported: steps done, Newton
+    and Krylov iterations, wall time and its split, and for the learned run
     the ratio of its guess residual to the secant guess's."""
     import time as _time
 
@@ -706,13 +709,18 @@ def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150
                     krylov_dim=krylov, forcing=1, forcing_max=1e-2, fp32_preconditioner=fp32)
         t0 = _time.perf_counter()
         recs, _ = continuation(gn, re0, re1, nsteps, predictor=pred, newton_opts=opts,
-                               learned_opts=dict(steps=300, batch=4096, lr=2e-3),
+                               learned_opts=dict(steps=300, batch=4096, lr=2e-3,
+                                                 warm_steps=warm_steps),
                                time_budget_s=budget_s)
         torch.cuda.synchronize()
         dt = _time.perf_counter() - t0
         res = {"steps_done": len(recs) - 1, "last_re": recs[-1]["lam"], "seconds": dt,
                "newton_its": sum(r["newton_its"] for r in recs[1:]),
                "linear_its": sum(r.get("linear_its", 0) for r in recs[1:]),
+               "newton_seconds": sum(r["newton_ms"]["total_ms"] for r in recs[1:]) * 1e-3,
+               "predictor_seconds": sum(r.get("predictor_s", 0.0) for r in recs[1:]),
+               "candidate_residual_seconds": sum(r.get("residuals_s", 0.0) for r in recs[1:]),
+               "training_seconds": sum(r.get("train_s", 0.0) for r in recs[1:]),
                "guesses": {g: sum(1 for r in recs[1:] if r["guess"] == g)
                            for g in ("zeroth", "secant", "learned")}}
         if pred == "learned":
@@ -792,6 +800,8 @@ def main():
     ap.add_argument("--bfs-fp64", action="store_true",
                     help="the bfs workload's linear solves in FP64 (default: FP64 flexible "
                          "GMRES with the ILU(0) in FP32)")
+    ap.add_argument("--bfs-predictors", default="zeroth,secant,learned",
+                    help="the bfs workload's predictors, comma separated")
     ap.add_argument("--solve-krylov", type=int, default=300,
                     help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
@@ -1010,7 +1020,8 @@ def main():
                                              max_ratio=1.6, budget_s=900.0, check=1,
                                              max_linear_its=2500)
             elif w == "bfs":
-                extra[w] = bfs_continuation(budget_s=args.bfs_budget, fp32=not args.bfs_fp64)
+                extra[w] = bfs_continuation(budget_s=args.bfs_budget, fp32=not args.bfs_fp64,
+                                            predictors=tuple(args.bfs_predictors.split(",")))
             elif w == "ilu_orders":
                 extra[w] = ilu_orders()
             elif w == "reuse":

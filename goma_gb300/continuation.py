@@ -77,7 +77,7 @@ class LearnedPredictor:
     scaled per field by the RMS of r1."""
 
     def __init__(self, gn, lam_range, width=256, hidden=3, seed=0, steps=1500, batch=4096,
-                 lr=2e-3, log_lambda=False):
+                 lr=2e-3, log_lambda=False, warm_steps=None):
         from .mlp import GpuMLP
         self.lay = FieldLayout(gn)
         self.N = gn.N
@@ -85,6 +85,9 @@ class LearnedPredictor:
         self.net = GpuMLP(self.n_in, width, hidden, 1, seed=seed)
         self.log_lambda = log_lambda
         self.steps, self.batch, self.lr = steps, batch, lr
+        # the network carries over from one continuation step to the next:
+        # after the first training, warm_steps Adam steps (default: steps)
+        self.warm_steps = steps if warm_steps is None else warm_steps
         self.sols = []
         self.X, self.T = [], []
         self.trained = 0
@@ -140,12 +143,21 @@ class LearnedPredictor:
         import torch
         if not self.X:
             return None
-        dx = torch.tensor(np.vstack(self.X), device="cuda")
-        dt = torch.tensor(np.vstack(self.T), device="cuda")
-        dm = torch.ones_like(dt)
+        # the training set stays on the device; only the samples added since
+        # the last training are copied (a sweep's set grows by N rows a step)
+        n_dev = getattr(self, "_n_dev", 0)
+        if n_dev < len(self.X):
+            nx = torch.tensor(np.vstack(self.X[n_dev:]), device="cuda")
+            nt = torch.tensor(np.vstack(self.T[n_dev:]), device="cuda")
+            self._dX = nx if n_dev == 0 else torch.cat([self._dX, nx])
+            self._dT = nt if n_dev == 0 else torch.cat([self._dT, nt])
+            self._dM = torch.ones_like(self._dT)
+            self._n_dev = len(self.X)
+        dx, dt, dm = self._dX, self._dT, self._dM
         # Adam at the given rate, then a quarter as many steps at a tenth of it
-        self.net.train(dx, dt, dm, steps=self.steps, batch=self.batch, lr=self.lr, seed=seed)
-        loss = self.net.train(dx, dt, dm, steps=max(self.steps // 4, 1), batch=self.batch,
+        steps = self.steps if self.trained == 0 else self.warm_steps
+        self.net.train(dx, dt, dm, steps=steps, batch=self.batch, lr=self.lr, seed=seed)
+        loss = self.net.train(dx, dt, dm, steps=max(steps // 4, 1), batch=self.batch,
                               lr=0.1 * self.lr, seed=seed + 7919)
         self.trained += 1
         return loss

@@ -646,7 +646,9 @@ __global__ void __launch_bounds__(256)
 // before it, and those above are the next nr-1-r entries (nvn-1-r for the
 // energy row).
 static constexpr long long kSpinLimit = 1LL << 22;
-static constexpr int kPrefetch = 10;  // row entries per lane loaded before the wait (320 a row)
+// row entries per lane loaded before the wait: 320 a row in FP32, 256 in
+// FP64 (where ten would spill at the 64 registers of four CTAs per SM)
+template <class T> constexpr int kPrefetchOf = sizeof(T) == 4 ? 10 : 8;
 static constexpr int kTrsvThreads = 256;
 
 struct TrsvArgs {
@@ -806,6 +808,7 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
     trsv_sync_free_kernel(TrsvArgs g, const T *__restrict__ lus, const T *__restrict__ binv,
                           const T *__restrict__ b, T *x) {
   using A = acc_t<T>;
+  constexpr int kPf = kPrefetchOf<T>;
   __shared__ A bv[kMaxNodeDofs];                      // per row: rhs less the off-node part
   __shared__ A inv_s[kMaxNodeDofs * kMaxNodeDofs];    // the node's block inverse, by column
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -817,15 +820,15 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
     const int f0 = (int)(tk.x & 0xffffffffll), nr = (int)(tk.x >> 32);
     const int64_t inv_off = tk.y;
     // before polling: everything that does not depend on the sweep
-    A pv[kPrefetch];
-    int pc[kPrefetch];
+    A pv[kPf];
+    int pc[kPf];
     int64_t pr0 = 0, pr1 = 0;
     if (warp < nr) {
       const longlong2 sg = g.seg[f0 + warp];
       pr0 = sg.x;
       pr1 = sg.y;
 #pragma unroll
-      for (int k = 0; k < kPrefetch; k++) {
+      for (int k = 0; k < kPf; k++) {
         const int64_t p = pr0 + lane + 32 * k;
         pv[k] = p < pr1 ? (A)lus[p] : (A)0;
         pc[k] = p < pr1 ? g.cols[p] : -1;
@@ -850,10 +853,10 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
         // ago are added while the newest ones are still awaited; a wait
         // re-polls only the value it waits for, so waiting warps issue few
         // instructions
-        A zv[kPrefetch];
+        A zv[kPf];
         unsigned pending = 0;
 #pragma unroll
-        for (int k = 0; k < kPrefetch; k++) {
+        for (int k = 0; k < kPf; k++) {
           zv[k] = 0;
           if (pc[k] >= 0) {
             const T v = ld_relaxed(x + pc[k]);
@@ -862,7 +865,7 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
         }
         long long polls = 0;
 #pragma unroll
-        for (int k = 0; k < kPrefetch; k++) {
+        for (int k = 0; k < kPf; k++) {
           while (!gave_up && (pending & (1u << k))) {
             if (++polls > g.spin_limit ||
                 ((polls & 1023) == 0 && *(volatile const int *)g.error)) {
@@ -877,7 +880,7 @@ __global__ void __launch_bounds__(kTrsvThreads, 4)
           }
           if (pc[k] >= 0) s0 = fmx(pv[k], zv[k], s0);
         }
-        p = pr0 + lane + 32 * kPrefetch;
+        p = pr0 + lane + 32 * kPf;
         p1 = pr1;
       } else {
         const longlong2 sg = g.seg[f0 + r];
