@@ -174,13 +174,15 @@ __global__ void __launch_bounds__(kRedThreads)
   if (threadIdx.x < nc) part[(int64_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = sh[threadIdx.x][0];
 }
 
+// out[j] = sum over the nblocks partial sums of column j, a warp per column
 __global__ void multidot_final_kernel(int k, int nblocks, const double *__restrict__ part,
                                       double *__restrict__ out) {
-  const int j = threadIdx.x;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (j >= k) return;
   double s = 0.0;
-  for (int b = 0; b < nblocks; b++) s += part[j * nblocks + b];
-  out[j] = s;
+  for (int b = lane; b < nblocks; b += 32) s += part[(int64_t)j * nblocks + b];
+  s = warp_sum(s);
+  if (lane == 0) out[j] = s;
 }
 
 // w -= sum_j h[j] V[:, j]
@@ -1750,13 +1752,13 @@ static int gmres(Context *C, const T *b, T *x, double tol, int maxit, int m, int
       double *dh1 = dh, *dh2 = dh + (m + 2), *dnrm = dh + 2 * (m + 2);
       multidot_tile_kernel<T><<<dim3(kMdBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
           N, j + 1, V, ld, w, dpart);
-      // one thread per coefficient (restart lengths up to 1023)
-      const int fin = ((j + 1 + 31) / 32) * 32;
-      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kMdBlocks, dpart, dh1);
+      // a warp per coefficient, eight a block
+      const int fin = (j + 1 + 7) / 8;
+      multidot_final_kernel<<<fin, 256, 0, st>>>(j + 1, kMdBlocks, dpart, dh1);
       gemv_sub_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh1, w);
       multidot_tile_kernel<T><<<dim3(kMdBlocks, (j + kMdCols) / kMdCols), kRedThreads, 0, st>>>(
           N, j + 1, V, ld, w, dpart);
-      multidot_final_kernel<<<1, fin, 0, st>>>(j + 1, kMdBlocks, dpart, dh2);
+      multidot_final_kernel<<<fin, 256, 0, st>>>(j + 1, kMdBlocks, dpart, dh2);
       gemv_sub_kernel<T><<<rows_grid, kRedThreads, 0, st>>>(N, j + 1, V, ld, dh2, w);
       norms_partial_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, w, dred);
       norms_final_kernel<<<1, 32, 0, st>>>(kRedBlocks, dred, dnrm);
