@@ -437,7 +437,7 @@ def batch_sweep_assembly(num=512, seed=0, steps=3, warmup=2):
 
 def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, check=2,
                       ilu_ordering=0, budget_s=240.0, nmin=16, nmax=32, re_max=100.0,
-                      max_ratio=None, max_linear_its=600):
+                      max_ratio=None, max_linear_its=600, fp32_preconditioner=False):
     """The 512-problem sweep: unit-square QUAD9 Q2/P1 cavities and channels,
     meshes n x n with n uniform in [16, 64], Re log-uniform in [10, 1000]
     (seeded), all held in one context as a disjoint union with per-element
@@ -478,7 +478,8 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
         ts = _time.perf_counter()
         x, conv, st = gn.solve_nonlinear_problem(
             x, residual_tol=tol, linear_tol=1e-8, max_newton=15, max_linear_its=max_linear_its,
-            fp32_inner=fp32_inner, inner_tol=1e-3, forcing=1, forcing_max=1e-2)
+            fp32_inner=fp32_inner, fp32_preconditioner=fp32_preconditioner, inner_tol=1e-3,
+            forcing=1, forcing_max=1e-2)
         print("batch stage %d: converged %s, %d Newton, %d Krylov, %.1f s, |R| %s" % (
             k, conv, st["newton_its"], st["linear_its"], _time.perf_counter() - ts,
             st["residual_l2"][-1] if st["residual_l2"] else None), file=sys.stderr, flush=True)
@@ -498,7 +499,7 @@ def batch_sweep_solve(num=64, seed=0, stages=2, tol=1e-10, fp32_inner=False, che
            "elements": nelem, "unknowns": gn.N, "csr_nnz": gn.nnz,
            "seconds_to_solve_all": solve_s, "layout_and_upload_s": setup_s,
            "converged": all(r["converged"] for r in recs), "stages": recs,
-           "fp32_inner": fp32_inner,
+           "fp32_inner": fp32_inner, "fp32_preconditioner": fp32_preconditioner,
            "ilu_order": "multicoloured" if ilu_ordering == 1 else "the reference's"}
     if check and out["converged"]:
         import oracle
@@ -802,6 +803,9 @@ def main():
                          "GMRES with the ILU(0) in FP32)")
     ap.add_argument("--bfs-predictors", default="zeroth,secant,learned",
                     help="the bfs workload's predictors, comma separated")
+    ap.add_argument("--batch-fp64", action="store_true",
+                    help="the batch512_solve workload's linear solves in FP64 (default: FP64 "
+                         "flexible GMRES with the ILU(0) in FP32)")
     ap.add_argument("--solve-krylov", type=int, default=300,
                     help="GMRES restart length (Krylov subspace size) of the time-to-solve leg")
     ap.add_argument("--solve-max-linear", type=int, default=4000,
@@ -1018,7 +1022,8 @@ def main():
             elif w == "batch512_solve":
                 extra[w] = batch_sweep_solve(512, nmin=16, nmax=64, re_max=1000.0,
                                              max_ratio=1.6, budget_s=900.0, check=1,
-                                             max_linear_its=2500)
+                                             max_linear_its=2500,
+                                             fp32_preconditioner=not args.batch_fp64)
             elif w == "bfs":
                 extra[w] = bfs_continuation(budget_s=args.bfs_budget, fp32=not args.bfs_fp64,
                                             predictors=tuple(args.bfs_predictors.split(",")))

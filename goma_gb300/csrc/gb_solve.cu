@@ -1903,7 +1903,8 @@ __global__ void seg_scale_kernel(const T *__restrict__ src, const double *__rest
 
 template <class T>
 static int gmres_seg(Context *C, const T *b, T *x, double tol, int maxit, int m, int *its,
-                     double *relres, cudaStream_t st) {
+                     double *relres, cudaStream_t st,
+                     bool flexible = false) {
   Solver &S = *C->solver;
   const Layout &L = C->L;
   const int N = L.N, lpr = lanes_per_row(L), ns = S.nseg, nt = S.ntiles;
@@ -1961,9 +1962,21 @@ static int gmres_seg(Context *C, const T *b, T *x, double tol, int maxit, int m,
     }
     int j = 0;
     for (; j < m && total < maxit; j++) {
-      GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
-      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
-      GB_CU(spmv<T>(C, lpr, A, t, w, st), "spmv");
+      const T *zj = t;  // M^-1 v_j
+      if constexpr (std::is_same<T, double>::value) {
+        if (flexible) {
+          // the (block-diagonal) preconditioner in FP32, z_j kept in FP64
+          to_f32_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, V + j * ld, S.d_t32);
+          if (S.apply_prec32(st)) return -1;
+          to_f64_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(N, S.d_t32, S.d_Z + j * ld);
+          zj = S.d_Z + j * ld;
+        }
+      }
+      if (!flexible) {
+        GB_CU(cudaMemcpyAsync(t, V + j * ld, sizeof(T) * N, cudaMemcpyDeviceToDevice, st), "t");
+        if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      }
+      GB_CU(spmv<T>(C, lpr, A, zj, w, st), "spmv");
       dots(j + 1, V, w, o1);
       seg_gemv_kernel<T, true><<<nt, 256, 0, st>>>(j + 1, V, ld, o1, S.d_tile_seg,
                                                    S.d_tile_beg, S.d_tile_end, w);
@@ -2032,9 +2045,18 @@ static int gmres_seg(Context *C, const T *b, T *x, double tol, int maxit, int m,
     if (kmax > 0) {
       GB_CU(cudaMemcpyAsync(S.d_segcoef, coef.data(), sizeof(double) * 32 * ns,
                             cudaMemcpyHostToDevice, st), "y");
-      seg_gemv_kernel<T, false><<<nt, 256, 0, st>>>(kmax, V, ld, S.d_segcoef, S.d_tile_seg,
-                                                    S.d_tile_beg, S.d_tile_end, t);
-      if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      if constexpr (std::is_same<T, double>::value) {
+        // flexible: x += Z y, the preconditioned vectors as they were applied
+        if (flexible)
+          seg_gemv_kernel<T, false><<<nt, 256, 0, st>>>(kmax, S.d_Z, ld, S.d_segcoef,
+                                                        S.d_tile_seg, S.d_tile_beg,
+                                                        S.d_tile_end, t);
+      }
+      if (!flexible) {
+        seg_gemv_kernel<T, false><<<nt, 256, 0, st>>>(kmax, V, ld, S.d_segcoef, S.d_tile_seg,
+                                                      S.d_tile_beg, S.d_tile_end, t);
+        if (f32 ? S.apply_prec32(st) : S.apply_prec64(st)) return -1;
+      }
       add_kernel<T><<<kRedBlocks, kRedThreads, 0, st>>>(N, t, x);
     }
     // true residual per block
@@ -2085,12 +2107,12 @@ static int linear_solve_impl(Context *C, const double *R, double *dx, const Line
   s->iterations = 0;
   s->refinements = 0;
   if (o.fp32_prec) {
-    if (S.nseg > 1)
-      return fail("the FP32 preconditioner mode serves one system per context");
     if (!S.d_Z) GB_CU(cudaMalloc(&S.d_Z, sizeof(double) * (size_t)S.max_krylov * N), "Z basis");
     int its;
     double rr;
-    if (gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st, true)) return -1;
+    if (S.nseg > 1 ? gmres_seg<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st, true)
+                   : gmres<double>(C, R, dx, o.tol, o.maxit, o.krylov, &its, &rr, st, true))
+      return -1;
     s->iterations = its;
     s->relres = rr;
     return 0;

@@ -206,8 +206,8 @@ int gb_csr_to_msr_host(gb_ctx *ctx, const double *d_vals, double *a_msr);
  * triangular sweeps, the cost of an iteration, run at the FP32 rate while
  * the Krylov process keeps FP64 accuracy; the flexible form (the
  * preconditioned vectors kept) makes the FP32 rounding of the sweeps
- * harmless to convergence.  One system per context (not for several
- * independent problems in one matrix). */
+ * harmless to convergence.  Several independent problems in one matrix
+ * run the batched form (one flexible GMRES per problem). */
 #define GB_LINEAR_FP32_PRECONDITIONER 2
 
 /* ILU(0) factorisation reuse, the reference's "Matrix Factorization Reuse"

@@ -68,15 +68,18 @@ def test_batch_newton_equals_members(batch):
         assert np.abs(x[lo:hi] - xo).max() <= 1e-8 * np.abs(xo).max(), p
 
 
-def test_batch_refuses_the_fp32_preconditioner_mode(batch):
-    """The FP32-preconditioner mode (flexible GMRES) serves one system per
-    context; several independent problems in one matrix get a clear error,
-    and the context then solves in another mode as before."""
-    from goma_gb300 import _lib
+def test_batch_newton_fp32_preconditioner_equals_members(batch):
+    """The batched GMRES in the FP32-preconditioner mode (one flexible GMRES
+    per member, the block-diagonal ILU(0) in FP32): every member's solution
+    equals the oracle's for that problem on its own."""
     b, gn, fu = batch
-    with pytest.raises(_lib.GbError, match="one system per context"):
-        gn.solve_nonlinear_problem(residual_tol=1e-10, linear_tol=1e-10, max_newton=3,
-                                   fp32_preconditioner=True)
     x, conv, st = gn.solve_nonlinear_problem(residual_tol=1e-10, linear_tol=1e-10,
-                                             max_newton=30, max_linear_its=3000)
+                                             max_newton=30, max_linear_its=3000,
+                                             fp32_preconditioner=True)
     assert conv
+    for p, mb in enumerate(b.members):
+        lo, hi = fu[mb.nodes[0]], fu[mb.nodes[1]]
+        o = oracle.Oracle(pb.batch_member_problem(b, p))
+        xo, its, _ = o.newton(o.dirichlet_init(np.zeros(o.N)))
+        assert its >= 0
+        assert np.abs(x[lo:hi] - xo).max() <= 1e-8 * np.abs(xo).max(), p
