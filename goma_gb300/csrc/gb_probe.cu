@@ -1,5 +1,5 @@
 // FP64 throughput probe: the roofline denominators for the FP64 element
-// kernels (the measured peaks cover HBM and bf16 only).  Two short
+// kernels (MEASURED_PEAKS.json holds HBM and bf16 figures only).  Two short
 // kernels of independent FP64 work: scalar FMA chains and mma.sync
 // m8n8k4 f64 (DMMA) chains, timed with CUDA events.
 #include <cuda_runtime.h>
