@@ -90,7 +90,10 @@ int gb_dirichlet_init(const gb_ctx *ctx, double *x);
  * Host arrays; R and a_msr are overwritten (the reference's caller zeroes
  * them before the call, src/mm_sol_nonlinear.c:1114-1120, so the result is
  * the same).  Returns -1 when an element has a non-positive Jacobian
- * determinant, as matrix_fill_full does (src/mm_fill.c:217-312). */
+ * determinant, as matrix_fill_full does (src/mm_fill.c:217-312).  A
+ * page-locked a_msr (cudaHostAlloc / cudaHostRegister), 16-byte aligned, is
+ * written by a copy kernel at the host link's rate; a pageable one goes
+ * through a staged copy. */
 int gb_matrix_fill_full(gb_ctx *ctx, const double *x, double *resid_vector, double *a_msr);
 
 /* Device form: d_x (N), d_R (N) and d_vals (CSR values, gb_csr_nnz()) are
