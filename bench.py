@@ -680,6 +680,29 @@ def krylov_kernels(nel, iters=30, ra=1e4):
     return out
 
 
+def krylov_step2d(iters=60):
+    """The linear-solver kernels on one Newton system of the 96 x 32 Carreau
+    step at Re 100 (the state at rest), in the FP32-preconditioner mode:
+    a factorisation plus exactly `iters` GMRES(iters) iterations (the
+    warp-per-node sweeps of a QUAD9 mesh)."""
+    import torch
+    from goma_gb300 import problem as pb
+    from goma_gb300.newton import GomaNewton
+    gn = GomaNewton(pb.carreau_step_2d(96, 32, 100.0))
+    gn.set_ilu_ordering(0)
+    torch.cuda.synchronize()
+    x, conv, st = gn.solve_nonlinear_problem(
+        None, residual_tol=1e-300, linear_tol=1e-300, max_newton=1, max_linear_its=iters,
+        krylov_dim=iters, fp32_preconditioner=True)
+    torch.cuda.synchronize()
+    out = {"workload": "96x32 Carreau step, one Newton step from rest (Re 100), FP32 "
+                       "preconditioner, %d GMRES(%d) iterations" % (iters, iters),
+           "unknowns": gn.N, "linear_its": st["linear_its"], "factor_ms": st["factor_ms"],
+           "ms_per_iteration": st["solve_ms"] / max(1, st["linear_its"])}
+    gn.close()
+    return out
+
+
 def bfs_continuation(nx=96, ny=32, re0=10.0, re1=800.0, nsteps=200, budget_s=150.0,
                      predictors=("zeroth", "secant", "learned"), krylov=150, fp32=True,
                      warm_steps=75):
@@ -827,7 +850,8 @@ def main():
                          "one host core with the oracle's ILU(0)-GMRES(30)), krylovN (the "
                          "linear-solver kernels on one N^3 cube system: factorisation + 30 "
                          "GMRES(30) iterations, FP64 and FP32; krylovNxM: M GMRES(M) "
-                         "iterations)")
+                         "iterations), krylov_step2d (the same for the 96x32 Carreau step "
+                         "in the FP32-preconditioner mode)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -1035,6 +1059,8 @@ def main():
                 extra[w] = cpu_time_to_solve(8)
             elif w == "reacting_solve":
                 extra[w] = reacting_channel_solve()
+            elif w == "krylov_step2d":
+                extra[w] = krylov_step2d()
             elif w.startswith("krylov"):
                 nel_s, _, its_s = w[len("krylov"):].partition("x")
                 extra[w] = krylov_kernels(int(nel_s or 16), int(its_s or 30))
