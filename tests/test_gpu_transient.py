@@ -8,7 +8,7 @@ against the oracle's transient loop on a larger mesh.
   derivative (mass terms of momentum, energy and species; both 3-D kernels);
 - time loop: the solution after every step within 1e-8 of the reference's
   (three backward-Euler steps, then Crank-Nicolson with its second-order
-  predictor), FP64 and FP32-inner linear solves.
+  predictor), with FP64, FP32-refined and FP32-preconditioner linear solves.
 """
 import numpy as np
 import pytest
@@ -39,15 +39,19 @@ def test_gpu_transient_assembly_matches_reference(name, path):
     assert np.abs(R2 - g["R"]).max() <= TOL * np.abs(g["R"]).max()
 
 
-@pytest.mark.parametrize("fp32_inner", [False, True], ids=["fp64", "fp32_refined"])
+PRECISIONS = {"fp64": {}, "fp32_refined": {"fp32_inner": True},
+              "fp32_preconditioner": {"fp32_preconditioner": True}}
+
+
+@pytest.mark.parametrize("precision", list(PRECISIONS))
 @pytest.mark.parametrize("name", gc.names("transient"))
-def test_gpu_time_loop_matches_reference(name, fp32_inner):
+def test_gpu_time_loop_matches_reference(name, precision):
     g, case = gc.load(name)
     tr = case["transient"]
     gn = GomaNewton(gc.problem_from_case(case))
     xs, st = gn.solve_transient(tr["steps"], tr["dt"], tr["theta"], residual_tol=case["tol"],
                                 linear_tol=1e-13, max_linear_its=3000, krylov_dim=60,
-                                fp32_inner=fp32_inner, max_newton=30)
+                                max_newton=30, **PRECISIONS[precision])
     assert st["steps_done"] == tr["steps"]
     ref = g["x_steps"]
     for k in range(tr["steps"]):
