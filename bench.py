@@ -228,7 +228,8 @@ def time_to_solve(nel, ra0=1e4, ra1=1e5, nsteps=6, tol=1e-10, ilu_ordering=-1, k
                                predictor={"plain": "zeroth", "secant": "secant",
                                           "learned": "learned"}[mode.split("_")[0]],
                                set_param=set_ra, newton_opts=opts, spacing="log",
-                               learned_opts=dict(steps=300, batch=4096, lr=2e-3),
+                               learned_opts=dict(steps=300, batch=4096, lr=2e-3,
+                                                 warm_steps=75),
                                time_budget_s=budget_s)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t
