@@ -163,8 +163,9 @@ int gb_set_ilu_ordering(gb_ctx *ctx, int ordering);
 int gb_set_element_density(gb_ctx *ctx, const double *rho);
 
 /* ILU(0) triangular solves of later linear solves: 0 = sync-free sweeps
- * (one launch per factor; each node waits on flags of the nodes it depends
- * on, bounded, then publishes), 1 = level-scheduled sweeps (one launch per
+ * (one launch per factor; each node polls the solution values it depends
+ * on, bounded, then publishes its own; a CTA per node, or a warp per node
+ * on meshes with short rows), 1 = level-scheduled sweeps (one launch per
  * dependency level, a CTA per node) replayed as a CUDA graph, 2 = automatic
  * (the default: the graph when the schedule has at most 64 levels, as in
  * the multicoloured order; the sync-free sweeps otherwise).  All give the
